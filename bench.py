@@ -1,0 +1,445 @@
+#!/usr/bin/env python3
+"""GST decode benchmark on GB300: decoded Mpix/s and DXT1 GB/s, batched vs per-image.
+
+Headline (``value``): the batched workload -- 64 synthetic images, width and
+height drawn independently from {512, 1024, 2048} (seeds 1000+i), decoded in
+one device-resident call (gst_load_compressed_dxts) per step, compressed input
+and DXT1 output resident in HBM.  L2 is flushed (a 256 MiB write) before every
+timed step, outside the timed events.  Also reported on the same line:
+
+* ``per_image``: the same 64 images decoded one call per image;
+* ``e2e``: the same batch through the public API with host buffers --
+  pinned H2D of the packed streams, decode, D2H of the DXT1 blocks, all inside
+  the timed region;
+* ``workloads``: the 8192x8192 texture (10 % 1-8 px checker regions), the
+  plain 512x512 image (seed 0), and the rANS-only section of 2^26 Laplace(6)
+  bytes (table build + decode);
+* ``roofline``: HBM-bound; algorithmic bytes = GST bytes read (28 + 2048 +
+  sections) + DXT1 bytes written, per decode call, over the call's kernel time;
+* ``cpu_baseline``: the C oracle (a restatement of the reference's decoder)
+  on the host's cores on a bounded sample of the same batch.
+
+``--impl reference`` times the reference's CPU decode path instead (the C
+oracle port, all host threads) on bounded samples of the same workload.
+
+Multi-GPU (torchrun): every rank decodes its own replica of the batch (images
+are independent; no collective); value = all ranks' pixels / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "decoded Mpix/s & DXT1 GB/s, batched vs per-image, bit-exact; p50/p99 latency"
+FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=("gst", "reference"), default="gst")
+    p.add_argument("--skip-extra", action="store_true", help="headline workload only")
+    p.add_argument("--cpu-sample", type=int, default=16, help="images of the batch the CPU baseline decodes")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_init(n_gpus: int):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(prefix="gst_clocks_", suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            for line in self.path.read_text().splitlines():
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        finally:
+            self.path.unlink(missing_ok=True)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+class Batch:
+    """Packed, device-resident batch of GST streams with its expected output."""
+
+    def __init__(self, images, device):
+        import torch
+        from gst_gb300 import decoder
+        self.images = images
+        self.hdrs, packed = decoder.pack_batch([im.stream for im in images])
+        self.d_cmp = torch.from_numpy(packed).to(device)
+        self.h_cmp = torch.from_numpy(packed).pin_memory()
+        self.out_bytes = sum(h.dxt_bytes for h in self.hdrs)
+        self.d_out = torch.zeros(self.out_bytes, dtype=torch.uint8, device=device)
+        self.h_out = torch.empty(self.out_bytes, dtype=torch.uint8).pin_memory()
+        self.pixels = sum(im.pixels for im in images)
+        self.gst_bytes = sum(len(im.stream) for im in images)
+        self.alg_bytes = self.gst_bytes + self.out_bytes
+        # Per-image device views for the per-image path.
+        self.views = []
+        cmp_off, out_off = 0, 0
+        for im, h in zip(images, self.hdrs):
+            _, one = decoder.pack_batch([im.stream])
+            self.views.append((h, torch.from_numpy(one).to(device), out_off))
+            out_off += h.dxt_bytes
+
+    def expected(self) -> np.ndarray:
+        return np.concatenate([im.blocks for im in self.images])
+
+
+def time_steps(fn, steps, warmup, stream, flush, ctx=None):
+    """Runs fn() warmup + steps times; returns per-step device ms (CUDA events
+    on `stream`, L2 flushed before each step outside the events) and the
+    per-kernel ms of each step."""
+    import torch
+    kern = []
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+        if ctx is not None:
+            kern.append(ctx.kernel_times())
+    return times, kern
+
+
+def kernel_summary(kern_steps):
+    agg = {}
+    for step in kern_steps:
+        for name, ms in step:
+            agg.setdefault(name, []).append(ms)
+    total = sum(sum(v) for v in agg.values()) or 1.0
+    return {name: {"avg_ms": statistics.mean(v), "launches": len(v), "share": sum(v) / total}
+            for name, v in agg.items()}
+
+
+def run_gst(args, rank, world, local):
+    import torch
+    from gst_gb300 import decoder, workloads
+
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    t0 = time.time()
+    images = workloads.batched(64)
+    encode_s = time.time() - t0
+    batch = Batch(images, device)
+    ctx = decoder.GPUContext(local)
+    ctx.set_profiling(True)
+    stream = torch.cuda.Stream(device)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=device)
+
+    def step_batched():
+        decoder.load_compressed_dxts(ctx, batch.hdrs, batch.d_cmp, batch.d_out, stream)
+
+    def step_per_image():
+        base = batch.d_out.data_ptr()
+        for h, d_one, off in batch.views:
+            decoder.load_compressed_dxt(ctx, h, d_one, base + off, stream)
+
+    def step_e2e():
+        with torch.cuda.stream(stream):
+            batch.d_cmp.copy_(batch.h_cmp, non_blocking=True)
+        decoder.load_compressed_dxts(ctx, batch.hdrs, batch.d_cmp, batch.d_out, stream)
+        with torch.cuda.stream(stream):
+            batch.h_out.copy_(batch.d_out, non_blocking=True)
+
+    peak, peak_kind = measured_peak_hbm()
+    barrier(world)
+    with ClockSampler(local) as clocks:
+        times, kern = time_steps(step_batched, args.steps, args.warmup, stream, flush, ctx)
+    clock = clocks.summary()
+    launches_per_step = ctx.last_launch_count()
+    stream.synchronize()
+    got = batch.d_out.cpu().numpy().view(np.uint64)
+    bit_exact = bool(np.array_equal(got, batch.expected()))
+    status = decoder.sync_status(ctx, stream)
+
+    total_ms = max_over_ranks(sum(times), world)
+    ms_per_step = total_ms / args.steps
+    value = world * batch.pixels * args.steps / (total_ms / 1e3) / 1e6
+    ksum = kernel_summary(kern)
+    kernel_ms = sum(k["avg_ms"] for k in ksum.values())
+    dominant = max(ksum.items(), key=lambda kv: kv[1]["share"])[0] if ksum else None
+
+    # per-image path
+    t_img, k_img = time_steps(step_per_image, max(3, args.steps // 4), 2, stream, flush, ctx)
+    per_image_ms = statistics.mean(t_img)
+    got_pi = batch.d_out.cpu().numpy().view(np.uint64)
+    per_image_exact = bool(np.array_equal(got_pi, batch.expected()))
+
+    # e2e through the public API with host buffers
+    t_e2e, _ = time_steps(step_e2e, args.steps, args.warmup, stream, flush)
+    e2e_total = max_over_ranks(sum(t_e2e), world)
+    e2e_value = world * batch.pixels * args.steps / (e2e_total / 1e3) / 1e6
+    e2e_exact = bool(np.array_equal(batch.h_out.numpy().view(np.uint64), batch.expected()))
+
+    line = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "Mpix/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u8",
+        "data": "synthetic",
+        "config": {
+            "workload": "batched: 64 synthetic images, w,h in {512,1024,2048}, seeds 1000+i, one call per step",
+            "images": len(images),
+            "pixels_per_step": batch.pixels,
+            "gst_bytes_per_step": batch.gst_bytes,
+            "dxt1_bytes_per_step": batch.out_bytes,
+            "l2": "flushed by a 256 MiB write before each timed step (outside the timed events)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+        },
+        "dxt1_gbs": round(batch.out_bytes * args.steps / (total_ms / 1e3) / 1e9 * world, 2),
+        "bit_exact": bit_exact and status == 0,
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clock,
+        "roofline": {
+            "bound": "hbm",
+            "kernel": "one decode call (" + " + ".join(ksum) + ")",
+            "achieved": round(batch.alg_bytes / (kernel_ms / 1e3) / 1e9, 1),
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": round(batch.alg_bytes / (kernel_ms / 1e3) / 1e9 / peak, 4),
+            "peak_source": f"{peak_kind} hbm_gbs",
+            "traffic": None,
+            "algorithmic_bytes_per_launch": batch.alg_bytes,
+            "dominant_kernel": dominant,
+            "kernels": {k: {"avg_ms": round(v["avg_ms"], 4), "share": round(v["share"], 3)} for k, v in ksum.items()},
+        },
+        "per_image": {
+            "value": round(world * batch.pixels / (per_image_ms / 1e3) / 1e6, 2),
+            "unit": "Mpix/s",
+            "ms_per_step": round(per_image_ms, 4),
+            "calls_per_step": len(images),
+            "bit_exact": per_image_exact,
+        },
+        "e2e": {
+            "value": round(e2e_value, 2),
+            "unit": "Mpix/s",
+            "ms_per_step": round(e2e_total / args.steps, 4),
+            "h2d_bytes_per_step": int(batch.h_cmp.numel()),
+            "d2h_bytes_per_step": int(batch.out_bytes),
+            "bit_exact": e2e_exact,
+        },
+        "encode_seconds": round(encode_s, 1),
+    }
+    if not args.skip_extra:
+        line["workloads"] = extra_workloads(ctx, stream, flush, device, peak, args)
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(images[: args.cpu_sample])
+    ctx.close()
+    return line
+
+
+def extra_workloads(ctx, stream, flush, device, peak, args):
+    import torch
+    from gst_gb300 import decoder, workloads
+    out = {}
+    steps = max(5, args.steps // 2)
+    for name, imgs in (("large_8192", [workloads.large()]), ("plain_512", [workloads.plain(0)])):
+        b = Batch(imgs, device)
+        fn = lambda b=b: decoder.load_compressed_dxts(ctx, b.hdrs, b.d_cmp, b.d_out, stream)  # noqa: E731
+        t, k = time_steps(fn, steps, 3, stream, flush, ctx)
+        ks = kernel_summary(k)
+        kms = sum(v["avg_ms"] for v in ks.values())
+        ok = bool(np.array_equal(b.d_out.cpu().numpy().view(np.uint64), b.expected()))
+        out[name] = {
+            "value": round(b.pixels / (statistics.mean(t) / 1e3) / 1e6, 2), "unit": "Mpix/s",
+            "ms_per_call": round(statistics.mean(t), 4),
+            "p50_ms": round(float(np.percentile(t, 50)), 4), "p99_ms": round(float(np.percentile(t, 99)), 4),
+            "dxt1_gbs": round(b.out_bytes / (statistics.mean(t) / 1e3) / 1e9, 2),
+            "hbm_frac_of_kernels": round(b.alg_bytes / (kms / 1e3) / 1e9 / peak, 4),
+            "kernels": {kk: round(v["avg_ms"], 4) for kk, v in ks.items()},
+            "gst_bytes": b.gst_bytes, "bit_exact": ok,
+        }
+    sec = workloads.rans_section()
+    d_f = torch.from_numpy(np.frombuffer(sec.section[:512], np.uint8).copy()).to(device)
+    d_b = torch.from_numpy(np.frombuffer(sec.section[512:], np.uint8).copy()).to(device)
+    d_o = torch.empty(sec.symbols.size, dtype=torch.uint8, device=device)
+    fn = lambda: decoder.decode_rans_groups(ctx, d_f, d_b, len(sec.section) - 512, sec.n_groups, 32, d_o, stream)  # noqa: E731
+    t, _ = time_steps(fn, steps, 3, stream, flush, ctx)
+    ok = bool(np.array_equal(d_o.cpu().numpy(), sec.symbols))
+    alg = len(sec.section) + sec.symbols.size
+    out["rans_2^26"] = {
+        "value": round(sec.symbols.size / (statistics.mean(t) / 1e3) / 1e9, 3), "unit": "Gsym/s",
+        "ms_per_call": round(statistics.mean(t), 4),
+        "gbs": round(alg / (statistics.mean(t) / 1e3) / 1e9, 1),
+        "hbm_frac": round(alg / (statistics.mean(t) / 1e3) / 1e9 / peak, 4),
+        "bits_per_symbol": round(8 * (len(sec.section) - 512) / sec.symbols.size, 3), "bit_exact": ok,
+    }
+    return out
+
+
+def cpu_baseline(images):
+    """The C oracle (restating the reference's decoder) on all host cores."""
+    import oracle
+    threads = os.cpu_count() or 1
+    oracle.load()
+    px = sum(im.pixels for im in images)
+    t0 = time.perf_counter()
+    for im in images:
+        st, _ = oracle.decode(im.stream, oracle.SCAN_EXACT, nthreads=threads)
+        assert st == 0
+    dt = time.perf_counter() - t0
+    return {"value": round(px / dt / 1e6, 2), "unit": "Mpix/s", "cores": threads, "kind": "port",
+            "sample": f"first {len(images)} images of the batched workload ({px / 1e6:.1f} Mpix), oracle decode "
+                      f"with {threads} threads, {dt:.2f} s"}
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU decode path (the oracle port), all host threads."""
+    from gst_gb300 import workloads
+    import oracle
+    if rank != 0:
+        return None
+    images = workloads.batched(64)[: args.cpu_sample]
+    threads = os.cpu_count() or 1
+    oracle.load()
+    px = sum(im.pixels for im in images)
+    for _ in range(max(1, min(args.warmup, 2))):
+        oracle.decode(images[0].stream, oracle.SCAN_REFERENCE, nthreads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for im in images:
+            st, _ = oracle.decode(im.stream, oracle.SCAN_REFERENCE, nthreads=threads)
+            assert st == 0
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = px * args.steps / total / 1e6
+    sample = (f"first {len(images)} of the 64 batched images ({px / 1e6:.1f} Mpix) per step, oracle port of the "
+              f"reference decoder, {threads} threads")
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": "Mpix/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "batched: 64 synthetic images, w,h in {512,1024,2048}, seeds 1000+i",
+                   "sample_images": len(images)},
+        "cpu_baseline": {"value": round(value, 2), "unit": "Mpix/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_init(args.gpus)
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_gst(args, rank, world, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,615 @@
+// gst_api.cpp -- C ABI of the GB300 GST decoder (include/gst_decoder.h).
+//
+// Host half of the decode path: header parsing and stream validation, the
+// per-call work plan (gst_plan.h), scratch management and the launches.  It
+// replaces codec/decoder.cpp:41-591 and the OpenCL context of gpu/gpu.cpp; the
+// device work is in gst_kernels.cu.  No CPU fallback exists: every decode goes
+// through the CUDA kernels or fails with GST_E_CUDA.
+#include "gst_decoder.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "gst_plan.h"
+
+namespace gst {
+const char *kernel_name(int i);
+cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, const GstPlanView &plan,
+                          cudaStream_t stream, int *launches, cudaEvent_t *ev);
+}
+
+constexpr int kMaxTimedKernels = 4;
+
+using namespace gst;
+
+namespace {
+
+constexpr size_t kAlign = 256;
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+uint32_t rd32(const uint8_t *p) {
+  return uint32_t(p[0]) | (uint32_t(p[1]) << 8) | (uint32_t(p[2]) << 16) | (uint32_t(p[3]) << 24);
+}
+
+// Dimension and size rules a header must meet before anything is launched
+// (README.md:67-71 of the reference; blocks < 2^28 keeps every offset in u32).
+gst_status check_header(const gst_header &h) {
+  if (h.width == 0 || h.height == 0 || h.width % 128 || h.height % 128) return GST_E_FORMAT;
+  const uint64_t px = uint64_t(h.width) * h.height;
+  if (px % (16u * 256u * 32u)) return GST_E_FORMAT;
+  const uint64_t B = px / 16;
+  if (B >= (1u << 28)) return GST_E_FORMAT;
+  if (h.palette_bytes == 0 || h.palette_bytes % kSymsPerGroup) return GST_E_FORMAT;
+  if (7 * B + h.palette_bytes >= (1ull << 32)) return GST_E_FORMAT;
+  const uint32_t lens[4] = {h.y_cmp_sz, h.chroma_cmp_sz, h.palette_sz, h.indices_sz};
+  const uint64_t syms[4] = {2 * B, 4 * B, h.palette_bytes, B};
+  for (int i = 0; i < 4; ++i) {
+    const uint64_t G = syms[i] / kSymsPerGroup;
+    if (lens[i] % 4 || G * (4 + 4 * kStreamsPerGroup) > lens[i]) return GST_E_FORMAT;
+  }
+  return GST_OK;
+}
+
+uint64_t image_blocks(const gst_header &h) { return uint64_t(h.width / 4) * (h.height / 4); }
+uint64_t section_bytes(const gst_header &h) {
+  return uint64_t(h.y_cmp_sz) + h.chroma_cmp_sz + h.palette_sz + h.indices_sz;
+}
+
+// Scratch layout of one image: decoded symbols, chunk prefixes, group sums.
+struct ScratchLayout {
+  size_t sym, chunk, gsum, total;
+};
+ScratchLayout scratch_layout(const gst_header &h) {
+  const uint64_t B = image_blocks(h);
+  ScratchLayout s;
+  s.sym = 0;
+  s.chunk = align_up(7 * B + h.palette_bytes, kAlign);
+  s.gsum = s.chunk + align_up(B / 32 * 4, kAlign);
+  s.total = s.gsum + align_up(2 * (B / kSymsPerGroup) * 4, kAlign);
+  return s;
+}
+
+size_t offsets_page_bytes(int n) { return align_up(size_t(n) * 8 * 4, 512); }
+
+struct Slot {
+  uint8_t *scratch = nullptr;
+  size_t scratch_cap = 0;
+  uint8_t *plan_d = nullptr;
+  size_t plan_cap = 0;
+  uint8_t *plan_h = nullptr;  // pinned
+  size_t plan_h_cap = 0;
+  cudaEvent_t plan_copied = nullptr;  // the pinned plan may be rewritten once this fires
+  cudaEvent_t done = nullptr;         // scratch and plan_d are free once this fires
+  bool used = false;
+};
+
+}  // namespace
+
+struct gst_ctx {
+  int device = 0;
+  std::mutex mu;
+  Slot slot;
+  bool preallocated = false;
+  cudaStream_t own_stream = nullptr;
+  // Staging for the host-buffer path (gst_decompress_dxt).
+  uint8_t *cmp_d = nullptr;
+  size_t cmp_cap = 0;
+  uint8_t *out_d = nullptr;
+  size_t out_cap = 0;
+  uint8_t *cmp_h = nullptr;  // pinned
+  size_t cmp_h_cap = 0;
+  uint8_t *out_h = nullptr;  // pinned
+  size_t out_h_cap = 0;
+  int last_launches = 0;
+  // Instrumentation: events around each kernel of the last decode call.
+  bool profiling = false;
+  cudaEvent_t ev[kMaxTimedKernels + 1] = {};
+  int timed_kernels = 0;
+};
+
+namespace {
+
+gst_status cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return GST_OK;
+  if (e == cudaErrorMemoryAllocation) return GST_E_OOM;
+  return GST_E_CUDA;
+}
+
+gst_status grow_device(uint8_t **p, size_t *cap, size_t need) {
+  if (*cap >= need) return GST_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  const size_t sz = std::max(need, size_t(1) << 20);
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), sz);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_status(e);
+  }
+  *cap = sz;
+  return GST_OK;
+}
+
+gst_status grow_pinned(uint8_t **p, size_t *cap, size_t need) {
+  if (*cap >= need) return GST_OK;
+  if (*p) cudaFreeHost(*p);
+  *p = nullptr;
+  *cap = 0;
+  const size_t sz = std::max(need, size_t(1) << 16);
+  cudaError_t e = cudaMallocHost(reinterpret_cast<void **>(p), sz);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_status(e);
+  }
+  *cap = sz;
+  return GST_OK;
+}
+
+bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &st) != cudaSuccess) return false;
+  return st != cudaStreamCaptureStatusNone;
+}
+
+// Builds the plan for n images whose compressed data sit in the reference's
+// layout at d_cmp, then launches.  hdrs have passed check_header.
+gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8_t *d_cmp, uint8_t *d_out,
+                        cudaStream_t stream) {
+  Slot &sl = ctx->slot;
+  const bool cap = capturing(stream);
+  // Per-image scratch and plan sizes.
+  std::vector<ScratchLayout> lay(n);
+  size_t scratch_need = 0;
+  uint32_t n_rans = 0, n_tiles = 0;
+  for (int i = 0; i < n; ++i) {
+    lay[i] = scratch_layout(hdrs[i]);
+    scratch_need += lay[i].total;
+    const uint64_t B = image_blocks(hdrs[i]);
+    const uint64_t groups[4] = {2 * B / kSymsPerGroup, 4 * B / kSymsPerGroup, hdrs[i].palette_bytes / kSymsPerGroup,
+                                B / kSymsPerGroup};
+    for (uint64_t G : groups) n_rans += uint32_t((G + kGroupsPerRansCta - 1) / kGroupsPerRansCta);
+    n_tiles += uint32_t(B / 1024);
+  }
+  const size_t off_images = align_up(sizeof(GstPlanHead), 128);
+  const size_t off_rans = off_images + sizeof(GstImageDesc) * n;
+  const size_t off_tiles = align_up(off_rans + sizeof(GstRansItem) * n_rans, 16);
+  const size_t off_counters = align_up(off_tiles + sizeof(GstTileItem) * n_tiles, 16);
+  const size_t plan_bytes = align_up(off_counters + 4 * size_t(n), 16);
+
+  // The previous call may still be using this slot's buffers: wait on the
+  // device for its completion, and on the host for its plan upload.
+  if (sl.used && !cap) {
+    cudaEventSynchronize(sl.plan_copied);
+    cudaStreamWaitEvent(stream, sl.done, 0);
+  }
+  if (sl.scratch_cap < scratch_need || sl.plan_cap < plan_bytes) {
+    if (ctx->preallocated && sl.scratch_cap < scratch_need) return GST_E_OOM;
+    if (cap) return GST_E_ARG;  // buffers cannot be reallocated during stream capture
+    if (sl.used) cudaEventSynchronize(sl.done);
+    gst_status st = grow_device(&sl.scratch, &sl.scratch_cap, scratch_need);
+    if (st != GST_OK) return st;
+    st = grow_device(&sl.plan_d, &sl.plan_cap, plan_bytes);
+    if (st != GST_OK) return st;
+  }
+  if (sl.plan_h_cap < plan_bytes) {
+    if (cap) return GST_E_ARG;
+    gst_status st = grow_pinned(&sl.plan_h, &sl.plan_h_cap, plan_bytes);
+    if (st != GST_OK) return st;
+  }
+
+  uint8_t *ph = sl.plan_h;
+  memset(ph, 0, plan_bytes);
+  GstPlanHead *head = reinterpret_cast<GstPlanHead *>(ph);
+  head->n_images = uint32_t(n);
+  head->n_rans = n_rans;
+  head->n_tiles = n_tiles;
+  GstImageDesc *imgs = reinterpret_cast<GstImageDesc *>(ph + off_images);
+  GstRansItem *rans = reinterpret_cast<GstRansItem *>(ph + off_rans);
+  GstTileItem *tiles = reinterpret_cast<GstTileItem *>(ph + off_tiles);
+  // codec/decoder.cpp:132-149 and demo/photos_sf.cpp:753-791: offsets page,
+  // then 4n frequency tables, then each image's four sections.
+  const size_t page = offsets_page_bytes(n);
+  uint64_t body = page + size_t(n) * 4 * kFreqTableBytes;
+  uint64_t scratch_off = 0, out_off = 0;
+  uint32_t ri = 0, ti = 0;
+  for (int i = 0; i < n; ++i) {
+    const gst_header &h = hdrs[i];
+    GstImageDesc &d = imgs[i];
+    const uint32_t B = uint32_t(image_blocks(h));
+    d.freq_off = page + size_t(i) * 4 * kFreqTableBytes;
+    d.body_off = body;
+    d.sym_off = scratch_off + lay[i].sym;
+    d.chunk_off = scratch_off + lay[i].chunk;
+    d.gsum_off = scratch_off + lay[i].gsum;
+    d.out_off = out_off;
+    const uint32_t lens[4] = {h.y_cmp_sz, h.chroma_cmp_sz, h.palette_sz, h.indices_sz};
+    const uint32_t syms[4] = {2 * B, 4 * B, h.palette_bytes, B};
+    uint32_t in = 0, o = 0;
+    for (int s = 0; s < 4; ++s) {
+      d.sec_in[s] = in;
+      d.sec_len[s] = lens[s];
+      d.sec_groups[s] = syms[s] / kSymsPerGroup;
+      d.sec_out[s] = o;
+      in += lens[s];
+      o += syms[s];
+      for (uint32_t g = 0; g < d.sec_groups[s]; g += kGroupsPerRansCta)
+        rans[ri++] = {uint32_t(i), uint32_t(s), g, uint16_t(std::min(kGroupsPerRansCta, d.sec_groups[s] - g)),
+                      uint16_t(kStreamsPerGroup)};
+    }
+    d.bx = h.width / 4;
+    d.by = h.height / 4;
+    d.palette_words = h.palette_bytes / 4;
+    d.tiles_x = d.bx / kWaveletDim;
+    for (uint32_t t = 0; t < B / 1024; ++t) tiles[ti++] = {uint32_t(i), t};
+    body += section_bytes(h);
+    scratch_off += lay[i].total;
+    out_off += 8ull * B;
+  }
+
+  cudaError_t e = cudaMemcpyAsync(sl.plan_d, ph, plan_bytes, cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (!cap) cudaEventRecord(sl.plan_copied, stream);
+  GstPlanView view;
+  view.head = reinterpret_cast<GstPlanHead *>(sl.plan_d);
+  view.images = reinterpret_cast<const GstImageDesc *>(sl.plan_d + off_images);
+  view.rans = reinterpret_cast<const GstRansItem *>(sl.plan_d + off_rans);
+  view.tiles = reinterpret_cast<const GstTileItem *>(sl.plan_d + off_tiles);
+  view.counters = reinterpret_cast<uint32_t *>(sl.plan_d + off_counters);
+  view.n_rans = n_rans;
+  view.n_tiles = n_tiles;
+  cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
+  e = launch_decode(d_cmp, sl.scratch, d_out, view, stream, &ctx->last_launches, ev);
+  ctx->timed_kernels = ev ? ctx->last_launches : 0;
+  if (e != cudaSuccess) return cuda_status(e);
+  if (!cap) cudaEventRecord(sl.done, stream);
+  sl.used = true;
+  return GST_OK;
+}
+
+gst_status read_device_status(gst_ctx *ctx, cudaStream_t stream) {
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (!ctx->slot.used) return GST_OK;
+  GstPlanHead head;
+  e = cudaMemcpy(&head, ctx->slot.plan_d, sizeof(head), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (head.err) {
+    const uint32_t zero = 0;
+    cudaMemcpy(ctx->slot.plan_d + offsetof(GstPlanHead, err), &zero, 4, cudaMemcpyHostToDevice);
+    return GST_E_FORMAT;
+  }
+  return GST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gst_status_string(gst_status s) {
+  switch (s) {
+    case GST_OK: return "ok";
+    case GST_E_ARG: return "bad argument";
+    case GST_E_FORMAT: return "malformed GST stream";
+    case GST_E_OOM: return "out of memory";
+    case GST_E_CUDA: return "CUDA error";
+    case GST_E_TIMEOUT: return "device wait timed out";
+  }
+  return "unknown status";
+}
+
+gst_status gst_init(int device, gst_ctx **out) {
+  if (!out) return GST_E_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return GST_E_CUDA;
+  if (device < 0 || device >= count) return GST_E_ARG;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_status(e);
+  gst_ctx *ctx = new gst_ctx();
+  ctx->device = device;
+  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->slot.plan_copied, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->slot.done, cudaEventDisableTiming) != cudaSuccess) {
+    gst_destroy(ctx);
+    return GST_E_CUDA;
+  }
+  *out = ctx;
+  return GST_OK;
+}
+
+void gst_destroy(gst_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+  if (ctx->slot.used) cudaEventSynchronize(ctx->slot.done);
+  cudaFree(ctx->slot.scratch);
+  cudaFree(ctx->slot.plan_d);
+  cudaFreeHost(ctx->slot.plan_h);
+  cudaFree(ctx->cmp_d);
+  cudaFree(ctx->out_d);
+  cudaFreeHost(ctx->cmp_h);
+  cudaFreeHost(ctx->out_h);
+  if (ctx->slot.plan_copied) cudaEventDestroy(ctx->slot.plan_copied);
+  if (ctx->slot.done) cudaEventDestroy(ctx->slot.done);
+  for (auto &e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+gst_status gst_initialize_decoder(gst_ctx *ctx) {
+  if (!ctx) return GST_E_ARG;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, ctx->device);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (prop.major * 10 + prop.minor < 100) return GST_E_CUDA;
+  if (prop.sharedMemPerBlock < 48 * 1024) return GST_E_CUDA;
+  return GST_OK;
+}
+
+gst_status gst_parse_header(const uint8_t *gst, size_t len, gst_header *hdr) {
+  if (!gst || !hdr) return GST_E_ARG;
+  if (len < 28 + 4 * kFreqTableBytes) return GST_E_FORMAT;
+  uint32_t *w = reinterpret_cast<uint32_t *>(hdr);
+  for (int i = 0; i < 7; ++i) w[i] = rd32(gst + 4 * i);
+  gst_status st = check_header(*hdr);
+  if (st != GST_OK) return st;
+  if (28 + 4 * kFreqTableBytes + section_bytes(*hdr) > len) return GST_E_FORMAT;
+  const uint8_t *freqs = gst + 28;
+  const uint8_t *body = freqs + 4 * kFreqTableBytes;
+  const uint64_t B = image_blocks(*hdr);
+  const uint32_t lens[4] = {hdr->y_cmp_sz, hdr->chroma_cmp_sz, hdr->palette_sz, hdr->indices_sz};
+  const uint64_t syms[4] = {2 * B, 4 * B, hdr->palette_bytes, B};
+  for (int s = 0; s < 4; ++s) {
+    uint32_t sum = 0;
+    for (int k = 0; k < 256; ++k) sum += uint32_t(freqs[s * 512 + 2 * k]) | (uint32_t(freqs[s * 512 + 2 * k + 1]) << 8);
+    if (sum != kTableSize) return GST_E_FORMAT;
+    const uint32_t G = uint32_t(syms[s] / kSymsPerGroup);
+    uint32_t prev = 4 * G;
+    for (uint32_t g = 0; g < G; ++g) {
+      const uint32_t e = rd32(body + 4 * g);
+      if (e % 4 || e < prev + 4 * kStreamsPerGroup || e > lens[s]) return GST_E_FORMAT;
+      prev = e;
+    }
+    body += lens[s];
+  }
+  return GST_OK;
+}
+
+size_t gst_required_scratch(const gst_header *hdr) {
+  if (!hdr || check_header(*hdr) != GST_OK) return 0;
+  return scratch_layout(*hdr).total;
+}
+
+gst_status gst_preallocate(gst_ctx *ctx, size_t bytes) {
+  if (!ctx) return GST_E_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  Slot &sl = ctx->slot;
+  if (sl.used) cudaEventSynchronize(sl.done);
+  if (sl.scratch) cudaFree(sl.scratch);
+  sl.scratch = nullptr;
+  sl.scratch_cap = 0;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&sl.scratch), std::max<size_t>(bytes, 256));
+  if (e != cudaSuccess) return cuda_status(e);
+  sl.scratch_cap = std::max<size_t>(bytes, 256);
+  ctx->preallocated = true;
+  return GST_OK;
+}
+
+gst_status gst_free_decompressor(gst_ctx *ctx) {
+  if (!ctx) return GST_E_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  Slot &sl = ctx->slot;
+  if (sl.used) cudaEventSynchronize(sl.done);
+  cudaFree(sl.scratch);
+  sl.scratch = nullptr;
+  sl.scratch_cap = 0;
+  ctx->preallocated = false;
+  return GST_OK;
+}
+
+size_t gst_batch_layout_bytes(const gst_header *hdrs, int n) {
+  if (!hdrs || n <= 0) return 0;
+  size_t total = offsets_page_bytes(n) + size_t(n) * 4 * kFreqTableBytes;
+  for (int i = 0; i < n; ++i) total += section_bytes(hdrs[i]);
+  return total;
+}
+
+gst_status gst_pack_batch(const uint8_t *const *gst, const size_t *len, int n, uint8_t *dst, size_t dst_cap) {
+  if (!gst || !len || !dst || n <= 0) return GST_E_ARG;
+  std::vector<gst_header> hdrs(n);
+  for (int i = 0; i < n; ++i) {
+    gst_status st = gst_parse_header(gst[i], len[i], &hdrs[i]);
+    if (st != GST_OK) return st;
+  }
+  const size_t need = gst_batch_layout_bytes(hdrs.data(), n);
+  if (dst_cap < need) return GST_E_ARG;
+  memset(dst, 0, offsets_page_bytes(n));
+  uint32_t *out_offsets = reinterpret_cast<uint32_t *>(dst);
+  uint32_t *in_offsets = out_offsets + 4 * n;
+  uint8_t *freqs = dst + offsets_page_bytes(n);
+  uint8_t *body = freqs + size_t(n) * 4 * kFreqTableBytes;
+  uint32_t in = 0, out = 0;
+  for (int i = 0; i < n; ++i) {
+    const gst_header &h = hdrs[i];
+    const uint32_t B = uint32_t(image_blocks(h));
+    const uint32_t lens[4] = {h.y_cmp_sz, h.chroma_cmp_sz, h.palette_sz, h.indices_sz};
+    const uint32_t syms[4] = {2 * B, 4 * B, h.palette_bytes, B};
+    for (int s = 0; s < 4; ++s) {
+      out_offsets[4 * i + s] = out;
+      in_offsets[4 * i + s] = in;
+      out += syms[s];
+      in += lens[s];
+    }
+    memcpy(freqs + size_t(i) * 4 * kFreqTableBytes, gst[i] + 28, 4 * kFreqTableBytes);
+    const size_t sb = section_bytes(h);
+    memcpy(body, gst[i] + 28 + 4 * kFreqTableBytes, sb);
+    body += sb;
+  }
+  return GST_OK;
+}
+
+gst_status gst_load_compressed_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const void *d_cmp, void *d_out,
+                                    void *stream) {
+  if (!ctx || !hdrs || n <= 0 || !d_cmp || !d_out) return GST_E_ARG;
+  if ((reinterpret_cast<uintptr_t>(d_cmp) & 15) || (reinterpret_cast<uintptr_t>(d_out) & 7)) return GST_E_ARG;
+  for (int i = 0; i < n; ++i) {
+    gst_status st = check_header(hdrs[i]);
+    if (st != GST_OK) return st;
+  }
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  return decode_batch(ctx, hdrs, n, static_cast<const uint8_t *>(d_cmp), static_cast<uint8_t *>(d_out),
+                      static_cast<cudaStream_t>(stream));
+}
+
+gst_status gst_load_compressed_dxt(gst_ctx *ctx, const gst_header *hdr, const void *d_cmp, void *d_out,
+                                   void *stream) {
+  return gst_load_compressed_dxts(ctx, hdr, 1, d_cmp, d_out, stream);
+}
+
+gst_status gst_decompress_dxt(gst_ctx *ctx, const uint8_t *gst, size_t len, uint8_t *dxt_out, size_t out_cap) {
+  if (!ctx || !gst || !dxt_out) return GST_E_ARG;
+  gst_header h;
+  gst_status st = gst_parse_header(gst, len, &h);
+  if (st != GST_OK) return st;
+  const size_t out_bytes = size_t(image_blocks(h)) * 8;
+  if (out_cap < out_bytes) return GST_E_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  // codec/decoder.cpp:430-476 (UploadData): the offsets page at byte 0, the
+  // stream minus its 28-byte header from byte 512.
+  const size_t body = 28 + 4 * kFreqTableBytes + section_bytes(h);
+  const size_t cmp_bytes = 512 + body - 28;
+  if ((st = grow_device(&ctx->cmp_d, &ctx->cmp_cap, cmp_bytes)) != GST_OK) return st;
+  if ((st = grow_device(&ctx->out_d, &ctx->out_cap, out_bytes)) != GST_OK) return st;
+  if ((st = grow_pinned(&ctx->cmp_h, &ctx->cmp_h_cap, cmp_bytes)) != GST_OK) return st;
+  if ((st = grow_pinned(&ctx->out_h, &ctx->out_h_cap, out_bytes)) != GST_OK) return st;
+  cudaStream_t s = ctx->own_stream;
+  cudaStreamSynchronize(s);  // the pinned staging buffers may still feed the previous call
+  memset(ctx->cmp_h, 0, 512);
+  memcpy(ctx->cmp_h + 512, gst + 28, body - 28);
+  cudaError_t e = cudaMemcpyAsync(ctx->cmp_d, ctx->cmp_h, cmp_bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_status(e);
+  st = decode_batch(ctx, &h, 1, ctx->cmp_d, ctx->out_d, s);
+  if (st != GST_OK) return st;
+  e = cudaMemcpyAsync(ctx->out_h, ctx->out_d, out_bytes, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_status(e);
+  st = read_device_status(ctx, s);
+  memcpy(dxt_out, ctx->out_h, out_bytes);
+  return st;
+}
+
+gst_status gst_decode_rans_groups(gst_ctx *ctx, const void *d_freqs, const void *d_body, uint32_t body_bytes,
+                                  uint32_t n_groups, uint32_t streams_per_group, void *d_out, void *stream) {
+  if (!ctx || !d_freqs || !d_body || !d_out || n_groups == 0) return GST_E_ARG;
+  if (streams_per_group < 1 || streams_per_group > kStreamsPerGroup) return GST_E_ARG;
+  if ((reinterpret_cast<uintptr_t>(d_freqs) & 1) || (reinterpret_cast<uintptr_t>(d_body) & 3) ||
+      (reinterpret_cast<uintptr_t>(d_out) & 15))
+    return GST_E_ARG;
+  if (uint64_t(n_groups) * 4 > body_bytes) return GST_E_FORMAT;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  Slot &sl = ctx->slot;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool cap = capturing(st);
+  const uint32_t n_rans = (n_groups + kGroupsPerRansCta - 1) / kGroupsPerRansCta;
+  const size_t off_images = align_up(sizeof(GstPlanHead), 128);
+  const size_t off_rans = off_images + sizeof(GstImageDesc);
+  const size_t off_counters = align_up(off_rans + sizeof(GstRansItem) * n_rans, 16);
+  const size_t plan_bytes = align_up(off_counters + 4, 16);
+  if (sl.used && !cap) {
+    cudaEventSynchronize(sl.plan_copied);
+    cudaStreamWaitEvent(st, sl.done, 0);
+  }
+  if (sl.plan_cap < plan_bytes) {
+    if (cap) return GST_E_ARG;
+    if (sl.used) cudaEventSynchronize(sl.done);
+    gst_status s2 = grow_device(&sl.plan_d, &sl.plan_cap, plan_bytes);
+    if (s2 != GST_OK) return s2;
+  }
+  if (sl.plan_h_cap < plan_bytes) {
+    if (cap) return GST_E_ARG;
+    gst_status s2 = grow_pinned(&sl.plan_h, &sl.plan_h_cap, plan_bytes);
+    if (s2 != GST_OK) return s2;
+  }
+  uint8_t *ph = sl.plan_h;
+  memset(ph, 0, plan_bytes);
+  GstPlanHead *head = reinterpret_cast<GstPlanHead *>(ph);
+  head->n_images = 1;
+  head->n_rans = n_rans;
+  GstImageDesc *d = reinterpret_cast<GstImageDesc *>(ph + off_images);
+  // Addresses are carried as offsets from a null base.
+  d->freq_off = reinterpret_cast<uintptr_t>(d_freqs);
+  d->body_off = reinterpret_cast<uintptr_t>(d_body);
+  d->sym_off = reinterpret_cast<uintptr_t>(d_out);
+  d->sec_len[0] = body_bytes;
+  d->sec_groups[0] = n_groups;
+  GstRansItem *rans = reinterpret_cast<GstRansItem *>(ph + off_rans);
+  for (uint32_t g = 0, r = 0; g < n_groups; g += kGroupsPerRansCta, ++r)
+    rans[r] = {0u, 0u, g, uint16_t(std::min(kGroupsPerRansCta, n_groups - g)), uint16_t(streams_per_group)};
+  cudaError_t e = cudaMemcpyAsync(sl.plan_d, ph, plan_bytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (!cap) cudaEventRecord(sl.plan_copied, st);
+  GstPlanView view;
+  view.head = reinterpret_cast<GstPlanHead *>(sl.plan_d);
+  view.images = reinterpret_cast<const GstImageDesc *>(sl.plan_d + off_images);
+  view.rans = reinterpret_cast<const GstRansItem *>(sl.plan_d + off_rans);
+  view.tiles = nullptr;
+  view.counters = reinterpret_cast<uint32_t *>(sl.plan_d + off_counters);
+  view.n_rans = n_rans;
+  view.n_tiles = 0;
+  cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
+  e = launch_decode(nullptr, nullptr, nullptr, view, st, &ctx->last_launches, ev);
+  ctx->timed_kernels = ev ? ctx->last_launches : 0;
+  if (e != cudaSuccess) return cuda_status(e);
+  if (!cap) cudaEventRecord(sl.done, st);
+  sl.used = true;
+  return GST_OK;
+}
+
+gst_status gst_sync_status(gst_ctx *ctx, void *stream) {
+  if (!ctx) return GST_E_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  return read_device_status(ctx, static_cast<cudaStream_t>(stream));
+}
+
+int gst_last_launch_count(gst_ctx *ctx) { return ctx ? ctx->last_launches : 0; }
+
+gst_status gst_set_profiling(gst_ctx *ctx, int enable) {
+  if (!ctx) return GST_E_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (enable && !ctx->ev[0]) {
+    for (auto &e : ctx->ev) {
+      cudaError_t err = cudaEventCreate(&e);
+      if (err != cudaSuccess) return cuda_status(err);
+    }
+  }
+  ctx->profiling = enable != 0;
+  ctx->timed_kernels = 0;
+  return GST_OK;
+}
+
+int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap) {
+  if (!ctx || !ms || cap <= 0) return 0;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const int n = std::min(cap, ctx->timed_kernels);
+  if (n == 0) return 0;
+  if (cudaEventSynchronize(ctx->ev[n]) != cudaSuccess) return 0;
+  for (int i = 0; i < n; ++i) {
+    if (cudaEventElapsedTime(&ms[i], ctx->ev[i], ctx->ev[i + 1]) != cudaSuccess) return 0;
+    if (names) names[i] = gst::kernel_name(ctx->last_launches == 1 ? 0 : i);
+  }
+  return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,295 @@
+"""The reference's decoder API (codec/decoder.h, namespace GenTC) over the C ABI.
+
+Names, argument meaning and error behaviour mirror ``GenTC``:
+
+=====================================  ==========================================
+reference                              here
+=====================================  ==========================================
+``gpu::GPUContext::InitializeOpenCL``  :class:`GPUContext` (a CUDA device)
+``GenTCHeader`` / ``LoadFrom``         :class:`GenTCHeader` / ``load_from``
+``InitializeDecoder``                  :func:`initialize_decoder`
+``DecompressDXT``                      :func:`decompress_dxt`
+``LoadCompressedDXT(s)``               :func:`load_compressed_dxt(s)`
+``RequiredScratchMem``                 :func:`required_scratch_mem`
+``PreallocateDecompressor``            :func:`preallocate_decompressor`
+``FreeDecompressor``                   :func:`free_decompressor`
+=====================================  ==========================================
+
+Device buffers are passed as integers or objects with ``data_ptr()`` (torch
+tensors); streams as ``None``, an integer ``cudaStream_t`` or an object with a
+``cuda_stream`` attribute (``torch.cuda.Stream``).  The library is the in-tree
+``libgst_gb300.so``; if it is missing the calls raise -- there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from .build import DECODER_LIB
+
+GST_OK, GST_E_ARG, GST_E_FORMAT, GST_E_OOM, GST_E_CUDA, GST_E_TIMEOUT = range(6)
+STATUS_NAMES = {
+    GST_OK: "GST_OK", GST_E_ARG: "GST_E_ARG", GST_E_FORMAT: "GST_E_FORMAT",
+    GST_E_OOM: "GST_E_OOM", GST_E_CUDA: "GST_E_CUDA", GST_E_TIMEOUT: "GST_E_TIMEOUT",
+}
+
+# Every symbol include/gst_decoder.h declares.
+EXPORTED_SYMBOLS = (
+    "gst_init", "gst_destroy", "gst_initialize_decoder", "gst_parse_header",
+    "gst_required_scratch", "gst_preallocate", "gst_free_decompressor",
+    "gst_decompress_dxt", "gst_load_compressed_dxt", "gst_load_compressed_dxts",
+    "gst_batch_layout_bytes", "gst_pack_batch", "gst_decode_rans_groups",
+    "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times",
+    "gst_status_string",
+)
+
+
+class GstError(RuntimeError):
+    """A C-ABI call returned a status other than GST_OK."""
+
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: {STATUS_NAMES.get(status, status)}")
+
+
+class GenTCHeader(ctypes.Structure):
+    """codec/codec_base.h:9-20 -- seven little-endian u32 words."""
+
+    _fields_ = [(name, ctypes.c_uint32) for name in (
+        "width", "height", "palette_bytes", "y_cmp_sz", "chroma_cmp_sz", "palette_sz", "indices_sz")]
+
+    @classmethod
+    def load_from(cls, buf: bytes) -> "GenTCHeader":
+        """codec/codec_base.cpp:18-25, without validation (see :func:`parse_header`)."""
+        if len(buf) < 28:
+            raise GstError(GST_E_FORMAT, "GenTCHeader.load_from")
+        return cls.from_buffer_copy(bytes(buf[:28]))
+
+    @property
+    def num_blocks(self) -> int:
+        return (self.width // 4) * (self.height // 4)
+
+    @property
+    def dxt_bytes(self) -> int:
+        return self.num_blocks * 8
+
+    @property
+    def compressed_bytes(self) -> int:
+        return self.y_cmp_sz + self.chroma_cmp_sz + self.palette_sz + self.indices_sz
+
+    def as_tuple(self):
+        return tuple(getattr(self, f) for f, _ in self._fields_)
+
+
+_lib = None
+
+
+def load_library() -> ctypes.CDLL:
+    """Loads libgst_gb300.so (building it first if the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    from .build import build_all
+    build_all()
+    if not Path(DECODER_LIB).exists():
+        raise RuntimeError(f"gst_gb300: CUDA decoder library missing at {DECODER_LIB}")
+    lib = ctypes.CDLL(str(DECODER_LIB))
+    P, S, U32, I = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_int
+    HP = ctypes.POINTER(GenTCHeader)
+    sig = {
+        "gst_init": (I, [I, ctypes.POINTER(P)]),
+        "gst_destroy": (None, [P]),
+        "gst_initialize_decoder": (I, [P]),
+        "gst_parse_header": (I, [P, S, HP]),
+        "gst_required_scratch": (S, [HP]),
+        "gst_preallocate": (I, [P, S]),
+        "gst_free_decompressor": (I, [P]),
+        "gst_decompress_dxt": (I, [P, P, S, P, S]),
+        "gst_load_compressed_dxt": (I, [P, HP, P, P, P]),
+        "gst_load_compressed_dxts": (I, [P, HP, I, P, P, P]),
+        "gst_batch_layout_bytes": (S, [HP, I]),
+        "gst_pack_batch": (I, [ctypes.POINTER(P), ctypes.POINTER(S), I, P, S]),
+        "gst_decode_rans_groups": (I, [P, P, P, U32, U32, U32, P, P]),
+        "gst_sync_status": (I, [P, P]),
+        "gst_last_launch_count": (I, [P]),
+        "gst_set_profiling": (I, [P, I]),
+        "gst_kernel_times": (I, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p), I]),
+        "gst_status_string": (ctypes.c_char_p, [I]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(status: int, what: str) -> None:
+    if status != GST_OK:
+        raise GstError(status, what)
+
+
+def _ptr(x) -> int:
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    if hasattr(x, "__cuda_array_interface__"):
+        return int(x.__cuda_array_interface__["data"][0])
+    raise TypeError(f"cannot take a device pointer from {type(x)!r}")
+
+
+def _stream(s) -> int:
+    if s is None:
+        return 0
+    if isinstance(s, int):
+        return s
+    if hasattr(s, "cuda_stream"):
+        return int(s.cuda_stream)
+    raise TypeError(f"cannot take a CUDA stream from {type(s)!r}")
+
+
+def _as_bytes(data) -> bytes:
+    if isinstance(data, (bytes, bytearray, memoryview)):
+        return bytes(data)
+    return np.ascontiguousarray(data, dtype=np.uint8).tobytes()
+
+
+class GPUContext:
+    """One CUDA device and its decoder context (gpu::GPUContext, gpu/gpu.h:35-176)."""
+
+    def __init__(self, device: int = 0):
+        lib = load_library()
+        h = ctypes.c_void_p()
+        _check(lib.gst_init(device, ctypes.byref(h)), "gst_init")
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        if self._h is None:
+            raise GstError(GST_E_ARG, "GPUContext is closed")
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            load_library().gst_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_launch_count(self) -> int:
+        return int(load_library().gst_last_launch_count(self.handle))
+
+    def set_profiling(self, enable: bool) -> None:
+        _check(load_library().gst_set_profiling(self.handle, int(enable)), "gst_set_profiling")
+
+    def kernel_times(self) -> list[tuple[str, float]]:
+        """(kernel name, milliseconds) of each kernel of the last decode call."""
+        ms = (ctypes.c_float * 8)()
+        names = (ctypes.c_char_p * 8)()
+        n = load_library().gst_kernel_times(self.handle, ms, names, 8)
+        return [(names[i].decode(), float(ms[i])) for i in range(n)]
+
+
+def parse_header(data) -> GenTCHeader:
+    """GenTCHeader::LoadFrom plus validation of the whole stream (raises GstError)."""
+    buf = _as_bytes(data)
+    hdr = GenTCHeader()
+    _check(load_library().gst_parse_header(buf, len(buf), ctypes.byref(hdr)), "gst_parse_header")
+    return hdr
+
+
+def initialize_decoder(ctx: GPUContext) -> bool:
+    """codec/decoder.cpp:558-591: True if the device can run the kernels."""
+    return load_library().gst_initialize_decoder(ctx.handle) == GST_OK
+
+
+def decompress_dxt(ctx: GPUContext, cmp_data) -> np.ndarray:
+    """codec/decoder.cpp:525-532: GST bytes -> DXT1 bytes (w*h/2, uint8), blocking."""
+    buf = _as_bytes(cmp_data)
+    hdr = GenTCHeader.load_from(buf)
+    out = np.empty(hdr.dxt_bytes, dtype=np.uint8)
+    _check(load_library().gst_decompress_dxt(ctx.handle, buf, len(buf), out.ctypes.data, out.nbytes),
+           "gst_decompress_dxt")
+    return out
+
+
+def load_compressed_dxts(ctx: GPUContext, hdrs: Sequence[GenTCHeader], cmp_data, output, stream=None) -> None:
+    """codec/decoder.cpp:540-544: device-resident batch decode, enqueued on `stream`."""
+    arr = (GenTCHeader * len(hdrs))(*hdrs)
+    _check(load_library().gst_load_compressed_dxts(ctx.handle, arr, len(hdrs), _ptr(cmp_data), _ptr(output),
+                                                   _stream(stream)), "gst_load_compressed_dxts")
+
+
+def load_compressed_dxt(ctx: GPUContext, hdr: GenTCHeader, cmp_data, output, stream=None) -> None:
+    """codec/decoder.cpp:534-538."""
+    _check(load_library().gst_load_compressed_dxt(ctx.handle, ctypes.byref(hdr), _ptr(cmp_data), _ptr(output),
+                                                  _stream(stream)), "gst_load_compressed_dxt")
+
+
+def decode_rans_groups(ctx: GPUContext, freqs, body, body_bytes: int, n_groups: int, streams_per_group: int,
+                       output, stream=None) -> None:
+    """rANS stage alone (ans::ocl::OpenCLDecoder::Decode, ans/ans_ocl.h:26-72)."""
+    _check(load_library().gst_decode_rans_groups(ctx.handle, _ptr(freqs), _ptr(body), body_bytes, n_groups,
+                                                 streams_per_group, _ptr(output), _stream(stream)),
+           "gst_decode_rans_groups")
+
+
+def sync_status(ctx: GPUContext, stream=None) -> int:
+    """Waits for `stream`; GST_OK or the device-side status of the last decode."""
+    return int(load_library().gst_sync_status(ctx.handle, _stream(stream)))
+
+
+def required_scratch_mem(hdr: GenTCHeader) -> int:
+    """codec/decoder.cpp:41-47 (this decoder's own requirement)."""
+    return int(load_library().gst_required_scratch(ctypes.byref(hdr)))
+
+
+def preallocate_decompressor(ctx: GPUContext, req_sz: int) -> None:
+    """codec/decoder.cpp:478-481."""
+    _check(load_library().gst_preallocate(ctx.handle, req_sz), "gst_preallocate")
+
+
+def free_decompressor(ctx: GPUContext) -> None:
+    """codec/decoder.cpp:483-485."""
+    _check(load_library().gst_free_decompressor(ctx.handle), "gst_free_decompressor")
+
+
+def batch_layout_bytes(hdrs: Sequence[GenTCHeader]) -> int:
+    arr = (GenTCHeader * len(hdrs))(*hdrs)
+    return int(load_library().gst_batch_layout_bytes(arr, len(hdrs)))
+
+
+def pack_batch(streams: Iterable[bytes]) -> tuple[list[GenTCHeader], np.ndarray]:
+    """Writes the reference's device layout for a batch of complete GST streams
+    (offsets page, 4N frequency tables, sections; demo/photos_sf.cpp:753-791)."""
+    bufs = [_as_bytes(s) for s in streams]
+    hdrs = [parse_header(b) for b in bufs]
+    n = len(bufs)
+    out = np.zeros(batch_layout_bytes(hdrs), dtype=np.uint8)
+    keep = [ctypes.create_string_buffer(b, len(b)) for b in bufs]
+    ptrs = (ctypes.c_void_p * n)(*[ctypes.addressof(k) for k in keep])
+    lens = (ctypes.c_size_t * n)(*[len(b) for b in bufs])
+    _check(load_library().gst_pack_batch(ptrs, lens, n, out.ctypes.data, out.nbytes), "gst_pack_batch")
+    return hdrs, out
+
+
+def blocks_u64(dxt_bytes: np.ndarray) -> np.ndarray:
+    """View DXT1 output bytes as one u64 per block (PhysicalDXTBlock::dxt_block)."""
+    return np.ascontiguousarray(dxt_bytes).view(np.uint64)

@@ -1,0 +1,146 @@
+/*
+ * gst_decoder.h -- C ABI of the GB300 GST decoder (GST stream -> DXT1 blocks).
+ *
+ * Drop-in replacement for the reference's decoder entry points,
+ * codec/decoder.h:12-38 (namespace GenTC), with plain pointers, sizes and
+ * status codes instead of std::unique_ptr<gpu::GPUContext>, std::vector and
+ * OpenCL handles:
+ *
+ *   reference (codec/decoder.h)              this header
+ *   ---------------------------------------  ----------------------------------
+ *   gpu::GPUContext::InitializeOpenCL        gst_init / gst_destroy
+ *     (gpu/gpu.h:35-60, gpu/gpu.cpp:394-529)
+ *   InitializeDecoder             :15        gst_initialize_decoder
+ *   DecompressDXT                 :16-17     gst_decompress_dxt
+ *   LoadCompressedDXT             :19-21     gst_load_compressed_dxt
+ *   LoadCompressedDXTs            :23-25     gst_load_compressed_dxts
+ *   RequiredScratchMem            :35        gst_required_scratch
+ *   PreallocateDecompressor       :36        gst_preallocate
+ *   FreeDecompressor              :37        gst_free_decompressor
+ *   GenTCHeader::LoadFrom (codec/codec_base.h:9-20)  gst_parse_header
+ *
+ * Device buffers replace cl_mem, a CUDA stream (passed as void*, a
+ * cudaStream_t) replaces the cl_command_queue, and completion is stream order
+ * (record an event on the stream) instead of a returned cl_event.  The
+ * device-resident layout of the compressed data is the reference's
+ * (codec/decoder.cpp:430-476, demo/photos_sf.cpp:753-791): a page of
+ * 8*N u32 offsets padded to 512 bytes, then 4*N 512-byte frequency tables,
+ * then every image's four sections back to back.  Unlike the reference,
+ * a batch may mix image sizes.
+ *
+ * Every call returns a gst_status.  Malformed streams are rejected before any
+ * launch where the host holds the bytes; on the device-resident path the
+ * kernels check group offsets, table sums and palette indices themselves and
+ * report GST_E_FORMAT through gst_sync_status.  There is no CPU fallback: if
+ * the CUDA kernels cannot run, the calls fail with GST_E_CUDA.
+ */
+#ifndef GST_DECODER_H
+#define GST_DECODER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gst_status {
+  GST_OK = 0,
+  GST_E_ARG = 1,     /* bad argument (null pointer, short buffer, bad count) */
+  GST_E_FORMAT = 2,  /* malformed GST stream                                 */
+  GST_E_OOM = 3,     /* device or pinned memory could not be allocated       */
+  GST_E_CUDA = 4,    /* a CUDA call failed                                   */
+  GST_E_TIMEOUT = 5  /* a bounded wait on the device gave up                 */
+} gst_status;
+
+/* codec/codec_base.h:9-20: seven little-endian u32 words at the stream start. */
+typedef struct gst_header {
+  uint32_t width;
+  uint32_t height;
+  uint32_t palette_bytes;
+  uint32_t y_cmp_sz;
+  uint32_t chroma_cmp_sz;
+  uint32_t palette_sz;
+  uint32_t indices_sz;
+} gst_header;
+
+typedef struct gst_ctx gst_ctx;
+
+/* Creates a decoder context on CUDA device `device` (replaces
+ * gpu::GPUContext::InitializeOpenCL, gpu/gpu.cpp:394-529). */
+gst_status gst_init(int device, gst_ctx **ctx);
+void gst_destroy(gst_ctx *ctx);
+
+/* codec/decoder.cpp:558-591: loads the kernels and checks the device can run
+ * them (sm_103 and the shared memory they use).  Optional, as in the reference. */
+gst_status gst_initialize_decoder(gst_ctx *ctx);
+
+/* codec/codec_base.cpp:18-25 plus validation of the whole stream: dimensions
+ * (w, h multiples of 128, w*h a multiple of 131072), section sizes, the four
+ * frequency tables (each sums to 2048) and every group's end offset. */
+gst_status gst_parse_header(const uint8_t *gst, size_t len, gst_header *hdr);
+
+/* codec/decoder.cpp:41-47: device scratch one image of this header needs. */
+size_t gst_required_scratch(const gst_header *hdr);
+
+/* codec/decoder.cpp:478-485: reserve scratch once for later calls, or free it.
+ * Without it the context grows its scratch on demand. */
+gst_status gst_preallocate(gst_ctx *ctx, size_t bytes);
+gst_status gst_free_decompressor(gst_ctx *ctx);
+
+/* codec/decoder.cpp:487-532: host stream in, host DXT1 out (w*h/2 bytes),
+ * blocking. */
+gst_status gst_decompress_dxt(gst_ctx *ctx, const uint8_t *gst, size_t len, uint8_t *dxt_out,
+                              size_t out_cap);
+
+/* codec/decoder.cpp:534-544: device-resident decode of one image or a batch.
+ * d_cmp holds the reference's layout (see above); hdrs are the images'
+ * headers in order; outputs are written back to back from d_out (w*h/2 bytes
+ * per image).  Enqueued on `stream` (a cudaStream_t; NULL = legacy default). */
+gst_status gst_load_compressed_dxt(gst_ctx *ctx, const gst_header *hdr, const void *d_cmp,
+                                   void *d_out, void *stream);
+gst_status gst_load_compressed_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const void *d_cmp,
+                                    void *d_out, void *stream);
+
+/* Size of the reference's device layout for these headers (offsets page,
+ * frequency tables, sections), and a host-side packer that writes it from
+ * n complete GST streams (gst[i] of len[i] bytes) into `dst`. */
+size_t gst_batch_layout_bytes(const gst_header *hdrs, int n);
+gst_status gst_pack_batch(const uint8_t *const *gst, const size_t *len, int n, uint8_t *dst,
+                          size_t dst_cap);
+
+/* rANS stage alone (ans/ans_decode.cl:97-143 with the table of
+ * ans/build_table.cl), as the reference's ans::ocl::OpenCLDecoder::Decode
+ * (ans/ans_ocl.h:26-72) exposes it: d_freqs holds 256 u16 normalised
+ * frequencies (sum 2048), d_body a section body in the format of
+ * codec/entropy.cpp:174-265 (n_groups u32 end offsets, then the groups, each
+ * ending in streams_per_group u32 final states).  Writes n_groups *
+ * streams_per_group * 256 symbols to d_out, stream-major within a group
+ * (out[(g * streams + s) * 256 + i]).  d_out must be 16-byte aligned. */
+gst_status gst_decode_rans_groups(gst_ctx *ctx, const void *d_freqs, const void *d_body, uint32_t body_bytes,
+                                  uint32_t n_groups, uint32_t streams_per_group, void *d_out, void *stream);
+
+/* Waits for `stream` and returns the device-side status of the last decode
+ * enqueued through this context (GST_E_FORMAT if the kernels met a malformed
+ * stream), then clears it. */
+gst_status gst_sync_status(gst_ctx *ctx, void *stream);
+
+/* Number of kernel launches the last decode call made (for instrumentation). */
+int gst_last_launch_count(gst_ctx *ctx);
+
+/* Instrumentation (no counterpart in the reference, whose queues are created
+ * without profiling, gpu/gpu.cpp:483): with profiling on, each decode call
+ * records CUDA events on its stream around every kernel it launches;
+ * gst_kernel_times waits for the last call and writes the kernels' durations
+ * in milliseconds (and their names, if `names` is non-null); it returns the
+ * number written. */
+gst_status gst_set_profiling(gst_ctx *ctx, int enable);
+int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
+
+/* Human-readable name of a status code. */
+const char *gst_status_string(gst_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GST_DECODER_H */

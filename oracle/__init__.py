@@ -1,0 +1,145 @@
+"""CPU oracle for the GST decode path -- TEST INFRASTRUCTURE ONLY.
+
+``load()`` compiles and loads gst_oracle.c (a plain-C restatement of the
+reference's OpenCL decoder, see gst_oracle.h).  ``load_ref()`` loads the
+reference's own CPU code compiled from its sources by build_ref.sh, when it has
+been built on this machine (it needs the reference sources, which only exist
+where the reference is mounted).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
+this package, and only as the checker or the timed CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SRC = HERE / "gst_oracle.c"
+ORACLE_HDR = HERE / "gst_oracle.h"
+ORACLE_LIB = HERE / "libgst_oracle.so"
+REF_DIR = HERE / "_ref"
+REF_LIB = REF_DIR / "libgstref.so"
+
+SCAN_REFERENCE, SCAN_EXACT = 0, 1
+
+_lib = None
+_ref = None
+
+
+def build(force: bool = False) -> Path:
+    if force or not ORACLE_LIB.exists() or ORACLE_LIB.stat().st_mtime < max(
+            ORACLE_SRC.stat().st_mtime, ORACLE_HDR.stat().st_mtime):
+        subprocess.run([os.environ.get("CC", "gcc"), "-std=c11", "-O2", "-shared", "-fPIC", "-pthread",
+                        str(ORACLE_SRC), "-o", str(ORACLE_LIB)], check=True)
+    return ORACLE_LIB
+
+
+def build_ref() -> bool:
+    """Runs build_ref.sh (a no-op where the reference sources are absent)."""
+    subprocess.run(["bash", str(HERE / "build_ref.sh")], check=True)
+    return REF_LIB.exists()
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        lib = ctypes.CDLL(str(ORACLE_LIB))
+        P, S, I, U32 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint32
+        lib.gsto_parse_header.argtypes = [P, S, P]
+        lib.gsto_build_table.argtypes = [P, P, P, P]
+        lib.gsto_build_table_direct.argtypes = [P, P, P, P]
+        lib.gsto_rans_decode_group.argtypes = [P, S, U32, P, P, P, I, S, P]
+        lib.gsto_inverse_wavelet_block.argtypes = [P, P]
+        lib.gsto_inverse_wavelet_level.argtypes = [P, I, I]
+        lib.gsto_scan_indices.argtypes = [P, U32, P, I]
+        lib.gsto_ycocg_to_565.argtypes = [I, I, I]
+        lib.gsto_ycocg_to_565.restype = ctypes.c_uint16
+        lib.gsto_decode.argtypes = [P, S, P, S, I, I]
+        lib.gsto_decode_symbols.argtypes = [P, S, P, S, I]
+        lib.gsto_section_search.argtypes = [P, U32, U32]
+        lib.gsto_section_search.restype = U32
+        _lib = lib
+    return _lib
+
+
+def load_ref():
+    """The reference's CPU code (oracle/_ref/libgstref.so) or None if not built here."""
+    global _ref
+    if _ref is None and REF_LIB.exists():
+        lib = ctypes.CDLL(str(REF_LIB))
+        P, S, I = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
+        lib.gstref_compress_rgb.argtypes = [I, I, P, P, S, ctypes.POINTER(S), P]
+        lib.gstref_compress_file.argtypes = [ctypes.c_char_p, P, S, ctypes.POINTER(S), P, S,
+                                             ctypes.POINTER(I), ctypes.POINTER(I)]
+        lib.gstref_encode_bytes.argtypes = [P, S, P, S, ctypes.POINTER(S)]
+        lib.gstref_decode_interleaved.argtypes = [P, S, S, P, S, S, P]
+        lib.gstref_generate_histogram.argtypes = [P, S, I, P]
+        lib.gstref_inverse_wavelet2d.argtypes = [P, P, S]
+        lib.gstref_inverse_wavelet2d.restype = None
+        lib.gstref_rans_encode_single.argtypes = [P, S, P, S, P, S, ctypes.POINTER(S), ctypes.POINTER(ctypes.c_uint32)]
+        lib.gstref_encode_interleaved.argtypes = [P, S, P, S, S, P, S, ctypes.POINTER(S)]
+        _ref = lib
+    return _ref
+
+
+def decode(stream: bytes, scan_mode: int = SCAN_REFERENCE, nthreads: int = 1) -> tuple[int, np.ndarray]:
+    """Whole decode of one GST stream -> (status, DXT1 bytes)."""
+    lib = load()
+    w = int.from_bytes(stream[0:4], "little")
+    h = int.from_bytes(stream[4:8], "little")
+    out = np.zeros(max(w * h // 2, 8), dtype=np.uint8)
+    st = lib.gsto_decode(stream, len(stream), out.ctypes.data, out.nbytes, scan_mode, nthreads)
+    return int(st), out[: w * h // 2]
+
+
+def decode_symbols(stream: bytes, nthreads: int = 1) -> tuple[int, np.ndarray]:
+    """rANS stage only -> (status, the reference's decompressed-symbol buffer)."""
+    lib = load()
+    w = int.from_bytes(stream[0:4], "little")
+    h = int.from_bytes(stream[4:8], "little")
+    pal = int.from_bytes(stream[8:12], "little")
+    out = np.zeros(7 * (w * h // 16) + pal, dtype=np.uint8)
+    st = lib.gsto_decode_symbols(stream, len(stream), out.ctypes.data, out.nbytes, nthreads)
+    return int(st), out
+
+
+def build_table(freqs, direct: bool = False):
+    """Decode table from 256 u16 frequencies -> (freq, cum, sym) arrays of 2048."""
+    lib = load()
+    f = np.zeros(256, dtype=np.uint16)
+    src = np.asarray(freqs, dtype=np.uint16)
+    f[: src.size] = src
+    fr = np.zeros(2048, np.uint16)
+    cu = np.zeros(2048, np.uint16)
+    sy = np.zeros(2048, np.uint8)
+    (lib.gsto_build_table_direct if direct else lib.gsto_build_table)(
+        f.ctypes.data, fr.ctypes.data, cu.ctypes.data, sy.ctypes.data)
+    return fr, cu, sy
+
+
+def rans_decode_groups(body: bytes, freqs, n_groups: int, streams: int) -> tuple[int, np.ndarray]:
+    """ans_decode.cl over every group of a section body -> (status, symbols)."""
+    lib = load()
+    fr, cu, sy = build_table(freqs)
+    out = np.zeros(n_groups * streams * 256, dtype=np.uint8)
+    status = 0
+    for g in range(n_groups):
+        lo = 4 * n_groups if g == 0 else int.from_bytes(body[4 * (g - 1): 4 * g], "little")
+        st = lib.gsto_rans_decode_group(body, len(body), g, fr.ctypes.data, cu.ctypes.data, sy.ctypes.data,
+                                        streams, lo, out[g * streams * 256:].ctypes.data)
+        status = status or int(st)
+    return status, out
+
+
+def scan_indices(deltas: np.ndarray, mode: int) -> np.ndarray:
+    lib = load()
+    d = np.ascontiguousarray(deltas, dtype=np.uint8)
+    out = np.zeros(d.size, dtype=np.int32)
+    lib.gsto_scan_indices(d.ctypes.data, d.size, out.ctypes.data, mode)
+    return out

@@ -1,0 +1,556 @@
+/*
+ * gst_oracle.c -- CPU oracle for the GST decode path.  TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's OpenCL decoder (GammaUNC/GST).  It
+ * is the checker for the CUDA path and the timed CPU baseline; the product
+ * never links it.  Every function follows the reference lines named beside it,
+ * with the reference's integer semantics: uint32 state arithmetic, int32
+ * wavelet intermediates, C truncating division, char stores, ushort packing.
+ */
+#include "gst_oracle.h"
+
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+static uint32_t rd32(const uint8_t *p) {
+  return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+static uint16_t rd16(const uint8_t *p) { return (uint16_t)(p[0] | (p[1] << 8)); }
+static void wr16(uint8_t *p, uint16_t v) {
+  p[0] = (uint8_t)v;
+  p[1] = (uint8_t)(v >> 8);
+}
+static void wr32(uint8_t *p, uint32_t v) {
+  p[0] = (uint8_t)v;
+  p[1] = (uint8_t)(v >> 8);
+  p[2] = (uint8_t)(v >> 16);
+  p[3] = (uint8_t)(v >> 24);
+}
+static int popc32(uint32_t x) { return __builtin_popcount(x); }
+
+/* ------------------------------------------------------------------------- */
+/* Stream geometry: codec/decoder.cpp:430-461 (offsets), codec/encoder.cpp:122-144
+ * (header, four 512-byte frequency tables, then the sections Y, chroma,
+ * palette, indices), codec/entropy.cpp:174-265 (section body: u32 group end
+ * offsets, then groups). */
+typedef struct {
+  uint32_t in_off;  /* byte offset of the section body from the end of the freq tables */
+  uint32_t in_len;  /* section body bytes (header *_sz field) */
+  uint32_t nsyms;   /* decoded symbols */
+  uint32_t ngroups; /* nsyms / 8192 */
+  uint32_t out_off; /* offset in the decompressed-symbol buffer */
+} gsto_section;
+
+static void section_layout(const gsto_header *h, gsto_section s[4]) {
+  const uint32_t B = (h->width / 4) * (h->height / 4);
+  const uint32_t lens[4] = {h->y_cmp_sz, h->chroma_cmp_sz, h->palette_sz, h->indices_sz};
+  const uint32_t syms[4] = {2 * B, 4 * B, h->palette_bytes, B};
+  uint32_t in = 0, out = 0;
+  for (int i = 0; i < 4; ++i) {
+    s[i].in_off = in;
+    s[i].in_len = lens[i];
+    s[i].nsyms = syms[i];
+    s[i].ngroups = syms[i] / GSTO_SYMS_PER_GROUP;
+    s[i].out_off = out;
+    in += lens[i];
+    out += syms[i];
+  }
+}
+
+int gsto_parse_header(const uint8_t *gst, size_t n, gsto_header *hdr) {
+  if (!gst || !hdr) return GSTO_E_ARG;
+  if (n < GSTO_HEADER_BYTES + 4 * GSTO_FREQ_BYTES) return GSTO_E_FORMAT;
+  uint32_t w[7];
+  for (int i = 0; i < 7; ++i) w[i] = rd32(gst + 4 * i);
+  hdr->width = w[0];
+  hdr->height = w[1];
+  hdr->palette_bytes = w[2];
+  hdr->y_cmp_sz = w[3];
+  hdr->chroma_cmp_sz = w[4];
+  hdr->palette_sz = w[5];
+  hdr->indices_sz = w[6];
+  /* README.md:67-71 dimension rules; blocks < 2^28 keeps every offset in u32. */
+  if (hdr->width == 0 || hdr->height == 0) return GSTO_E_FORMAT;
+  if (hdr->width % 128 || hdr->height % 128) return GSTO_E_FORMAT;
+  const uint64_t px = (uint64_t)hdr->width * hdr->height;
+  if (px % (16u * 256u * 32u)) return GSTO_E_FORMAT;
+  const uint64_t B = px / 16;
+  if (B >= (1u << 28)) return GSTO_E_FORMAT;
+  if (hdr->palette_bytes == 0 || hdr->palette_bytes % GSTO_SYMS_PER_GROUP) return GSTO_E_FORMAT;
+  if (7 * B + hdr->palette_bytes >= (1ull << 32)) return GSTO_E_FORMAT;
+  gsto_section s[4];
+  section_layout(hdr, s);
+  uint64_t total = GSTO_HEADER_BYTES + 4 * GSTO_FREQ_BYTES;
+  for (int i = 0; i < 4; ++i) total += s[i].in_len;
+  if (total > n) return GSTO_E_FORMAT;
+  const uint8_t *freqs = gst + GSTO_HEADER_BYTES;
+  const uint8_t *body = freqs + 4 * GSTO_FREQ_BYTES;
+  for (int i = 0; i < 4; ++i) {
+    uint32_t sum = 0;
+    for (int k = 0; k < 256; ++k) sum += rd16(freqs + i * GSTO_FREQ_BYTES + 2 * k);
+    if (sum != GSTO_TABLE_SIZE) return GSTO_E_FORMAT;
+    const uint32_t G = s[i].ngroups;
+    if (s[i].in_len % 4) return GSTO_E_FORMAT;
+    if ((uint64_t)G * 4 + (uint64_t)G * 128 > s[i].in_len) return GSTO_E_FORMAT;
+    const uint8_t *sec = body + s[i].in_off;
+    uint32_t prev = 4 * G;
+    for (uint32_t g = 0; g < G; ++g) {
+      const uint32_t e = rd32(sec + 4 * g);
+      if (e % 4 || e < prev + 4 * GSTO_STREAMS_PER_GROUP || e > s[i].in_len) return GSTO_E_FORMAT;
+      prev = e;
+    }
+  }
+  return GSTO_OK;
+}
+
+/* ------------------------------------------------------------------------- */
+/* build_table.cl:12-83 */
+static void blelloch_exclusive_u16(uint16_t c[256]) {
+  uint32_t offset = 1;
+  for (uint32_t d = 256 >> 1; d > 0; d >>= 1) { /* :29-37 */
+    for (uint32_t lid = 0; lid < d; ++lid) {
+      const uint32_t ai = offset * (2 * lid + 1) - 1, bi = offset * (2 * lid + 2) - 1;
+      c[bi] = (uint16_t)(c[bi] + c[ai]);
+    }
+    offset *= 2;
+  }
+  c[255] = 0; /* :39-41 */
+  for (uint32_t d = 1; d < 256; d *= 2) { /* :43-54 */
+    offset >>= 1;
+    for (uint32_t lid = 0; lid < d; ++lid) {
+      const uint32_t ai = offset * (2 * lid + 1) - 1, bi = offset * (2 * lid + 2) - 1;
+      const uint32_t t = c[ai];
+      c[ai] = c[bi];
+      c[bi] = (uint16_t)(c[bi] + t);
+    }
+  }
+}
+
+void gsto_build_table(const uint16_t freqs[256], uint16_t freq[2048], uint16_t cum[2048],
+                      uint8_t sym[2048]) {
+  uint16_t c[256];
+  memcpy(c, freqs, sizeof(c));
+  blelloch_exclusive_u16(c);
+  for (uint32_t id = 0; id < GSTO_TABLE_SIZE; ++id) { /* :61-75, the kernel's 11-step search */
+    uint32_t low = 0, high = 255, x = (high + low) / 2;
+    for (int i = 0; i < GSTO_TABLE_LOG; ++i) {
+      const uint32_t too_high = (uint32_t)(id < c[x & 255]);
+      const uint32_t too_low = (uint32_t)(x < 255 && c[(x + 1) & 255] <= id);
+      const uint32_t lo1 = (low + 1 > x) ? low + 1 : x;
+      const uint32_t hi1 = (high - 1 < x) ? high - 1 : x;
+      low = too_low * lo1 + (1 - too_low) * low;
+      high = too_high * hi1 + (1 - too_high) * high;
+      x = (high + low) / 2;
+    }
+    x &= 255;
+    freq[id] = freqs[x]; /* :78-82 */
+    cum[id] = c[x];
+    sym[id] = (uint8_t)x;
+  }
+}
+
+void gsto_build_table_direct(const uint16_t freqs[256], uint16_t freq[2048], uint16_t cum[2048],
+                             uint8_t sym[2048]) {
+  uint32_t c = 0;
+  for (uint32_t x = 0; x < 256; ++x) {
+    for (uint32_t k = 0; k < freqs[x] && c + k < GSTO_TABLE_SIZE; ++k) {
+      freq[c + k] = freqs[x];
+      cum[c + k] = (uint16_t)c;
+      sym[c + k] = (uint8_t)x;
+    }
+    c += freqs[x];
+  }
+}
+
+/* ------------------------------------------------------------------------- */
+/* ans_decode.cl:25-74 (ans_decode_single); constants :3-8. */
+int gsto_rans_decode_group(const uint8_t *data, size_t data_len, uint32_t group,
+                           const uint16_t freq[2048], const uint16_t cum[2048],
+                           const uint8_t sym[2048], int num_streams, size_t lo_bytes,
+                           uint8_t *out) {
+  if (num_streams < 1 || num_streams > 32) return GSTO_E_ARG;
+  if ((size_t)group * 4 + 4 > data_len) return GSTO_E_FORMAT;
+  int status = GSTO_OK;
+  const uint32_t offset = rd32(data + 4 * group); /* :113 */
+  const uint32_t ns = (uint32_t)num_streams;
+  if (offset < 4 * ns || offset > data_len) return GSTO_E_FORMAT;
+  uint32_t st[32];
+  for (uint32_t l = 0; l < ns; ++l) st[l] = rd32(data + offset - 4 * ns + 4 * l); /* :114 */
+  uint32_t next = (offset - ns * 4) / 2;                                       /* :115 */
+  for (int i = 0; i < GSTO_SYMS_PER_STREAM; ++i) {
+    uint32_t mask = 0;
+    uint8_t s_out[32];
+    for (uint32_t l = 0; l < ns; ++l) { /* :121-129 */
+      const uint32_t slot = st[l] & (GSTO_TABLE_SIZE - 1);
+      st[l] = (st[l] >> GSTO_TABLE_LOG) * freq[slot] - cum[slot] + slot;
+      s_out[l] = sym[slot];
+      mask |= (uint32_t)(st[l] < GSTO_RANS_L) << l;
+    }
+    const uint32_t total = (uint32_t)popc32(mask); /* :134 */
+    for (uint32_t l = 0; l < ns; ++l) {            /* :135-140 */
+      if (!((mask >> l) & 1)) continue;
+      const uint32_t rank = (uint32_t)popc32(mask & ((1u << l) - 1));
+      const uint32_t idx = next - total + rank;
+      uint16_t v = 0;
+      /* Reads stay inside the group's word region [lo_bytes, offset - 4*ns);
+       * a valid stream never leaves it. */
+      if ((uint64_t)idx * 2 < lo_bytes || (uint64_t)idx * 2 + 2 > (uint64_t)offset - 4 * ns) {
+        status = GSTO_E_FORMAT;
+      } else {
+        v = rd16(data + 2 * (size_t)idx);
+      }
+      st[l] = (st[l] << 16) | v;
+    }
+    next -= total; /* :148 */
+    for (uint32_t l = 0; l < ns; ++l) out[l * GSTO_SYMS_PER_STREAM + GSTO_SYMS_PER_STREAM - 1 - i] = s_out[l];
+  }
+  return status;
+}
+
+/* ------------------------------------------------------------------------- */
+/* inverse_wavelet.cl:14-64 (NormalizeIndex, InverseWaveletEven/Odd) */
+static int normalize_index(int idx, int range) {
+  const int v = idx - (int)(idx >= range) * (idx - range + 2);
+  return v < 0 ? -v : v;
+}
+
+/* One level (len = dim): the row pass then the column pass, as the kernel's
+ * two transposing half-passes do (:117-172). */
+void gsto_inverse_wavelet_level(int32_t *blk, int stride, int dim) {
+  const int mid = dim / 2;
+  int32_t src[32], dst[32];
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int line = 0; line < dim; ++line) {
+      for (int k = 0; k < dim; ++k) src[k] = pass == 0 ? blk[line * stride + k] : blk[k * stride + line];
+      for (int x = 0; x < mid; ++x) { /* Even */
+        const int prev = mid + normalize_index(2 * x - 1, dim) / 2;
+        const int next = mid + normalize_index(2 * x + 1, dim) / 2;
+        dst[2 * x] = src[x] - (src[prev] + src[next] + 2) / 4;
+      }
+      for (int x = 0; x < mid; ++x) { /* Odd */
+        const int prev = normalize_index(2 * x, dim);
+        const int next = normalize_index(2 * x + 2, dim);
+        dst[2 * x + 1] = src[mid + x] + (dst[prev] + dst[next]) / 2;
+      }
+      for (int k = 0; k < dim; ++k) {
+        if (pass == 0) blk[line * stride + k] = dst[k];
+        else blk[k * stride + line] = dst[k];
+      }
+    }
+  }
+}
+
+void gsto_inverse_wavelet_block(const uint8_t *in, int8_t *out) {
+  int32_t b[1024];
+  for (int i = 0; i < 1024; ++i) b[i] = (int32_t)in[i] - 128; /* :93-104 */
+  for (int len = 2; len <= 32; len *= 2) gsto_inverse_wavelet_level(b, 32, len);
+  for (int i = 0; i < 1024; ++i) out[i] = (int8_t)(uint8_t)((uint32_t)b[i] & 0xFF); /* :188-190 */
+}
+
+/* ------------------------------------------------------------------------- */
+/* decode_indices.cl:6-84 driven by decoder.cpp:302-393. */
+static void local_scan128(uint32_t s[128], uint32_t lsize) {
+  uint32_t offset = 1; /* :225-236 */
+  for (uint32_t i = 128 >> 1; i > 0; i >>= 1) {
+    for (uint32_t tid = 0; tid < i && tid < lsize; ++tid) {
+      const uint32_t a = offset * (2 * tid + 1) - 1, b = offset * (2 * tid + 2) - 1;
+      s[b] += s[a];
+    }
+    offset *= 2;
+  }
+  offset >>= 1; /* :238-248 */
+  for (uint32_t d = 2; d < 128; d *= 2) {
+    offset >>= 1;
+    for (uint32_t tid = 1; tid < d && tid < lsize; ++tid) {
+      if (offset == 0) continue;
+      const uint32_t a = offset * (2 * tid) - 1, b = offset * (2 * tid + 1) - 1;
+      s[b] += s[a];
+    }
+  }
+}
+
+static void scan_reference(const uint8_t *deltas, uint32_t n, int32_t *out_i) {
+  uint32_t *out = (uint32_t *)out_i;
+  int stage = -1;
+  for (;;) { /* decoder.cpp:311-356 */
+    stage++;
+    const uint32_t num = n >> (stage * 7);
+    if (num == 0) break;
+    const uint32_t gsize = num < 128 ? num : ((num + 127) / 128) * 128;
+    const uint32_t lsize = num < 128 ? num : 128;
+    const uint32_t idx_offset = 1u << (stage * 7);
+    /* Work-groups run one after another in id order (one legal interleaving;
+     * for the sizes where the kernel's writes alias, decode_indices.cl:217-255
+     * gives no ordering guarantee). */
+    for (uint32_t g0 = 0; g0 < gsize; g0 += lsize) {
+      uint32_t s[128];
+      for (uint32_t k = 0; k < 128; ++k) s[k] = 0xA5A5A5A5u; /* local memory not written by the kernel */
+      for (uint32_t lid = 0; lid < lsize; ++lid) {
+        const uint32_t gid = g0 + lid;
+        const uint32_t gidx = idx_offset * (gid + 1) - 1, pgidx = idx_offset * gid - 1;
+        if (stage == 0) s[lid] = (uint32_t)((int32_t)deltas[gid] - 128);
+        else if (gidx < n) s[lid] = out[gidx];
+        else if (pgidx < n) s[lid] = out[n - 1];
+        else s[lid] = 0;
+      }
+      local_scan128(s, lsize);
+      for (uint32_t lid = 0; lid < lsize; ++lid) {
+        const uint32_t gid = g0 + lid;
+        const uint32_t gidx = idx_offset * (gid + 1) - 1, pgidx = idx_offset * gid - 1;
+        if (stage == 0 || gidx < n) out[gidx] = s[lid];
+        else if (pgidx < n && gidx >= n) out[n - 1] = s[lid];
+      }
+    }
+  }
+  while (stage > 0) { /* decoder.cpp:358-393, collect_indices :66-84 */
+    const int sh = (stage - 1) * 7;
+    const uint32_t num = n >> (sh > 0 ? sh : 0);
+    const uint32_t gsize = ((num + 127) / 128) * 128;
+    const uint32_t offset = 1u << (stage * 7), next_offset = 1u << ((stage - 1) * 7);
+    for (uint32_t gid = 0; gid < gsize; ++gid) {
+      const uint32_t group = gid / 128, lid = gid % 128;
+      const uint32_t gidx = offset * group - 1, tidx = next_offset * (gid + 1) - 1;
+      if (tidx < n - 1 && gidx < n - 1 && group > 0 && lid != 127) out[tidx] += out[gidx];
+    }
+    stage--;
+  }
+}
+
+void gsto_scan_indices(const uint8_t *deltas, uint32_t n, int32_t *out, int mode) {
+  if (n == 0) return;
+  if (mode == GSTO_SCAN_REFERENCE && n % 128 == 0) {
+    scan_reference(deltas, n, out);
+    return;
+  }
+  uint32_t acc = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    acc += (uint32_t)((int32_t)deltas[i] - 128);
+    out[i] = (int32_t)acc;
+  }
+}
+
+/* ------------------------------------------------------------------------- */
+/* assemble.cl:39-62 */
+uint16_t gsto_ycocg_to_565(int y, int co, int cg) {
+  const int t = y - (cg / 2);
+  const int g = cg + t;
+  const int b = (t - co) / 2;
+  const int r = b + co;
+  const uint32_t p = ((uint32_t)r << 11) | ((uint32_t)g << 5) | (uint32_t)b;
+  return (uint16_t)p;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Parallel-for over [0, count) with a static split (pthreads). */
+typedef void (*range_fn)(void *ctx, uint32_t lo, uint32_t hi, int *status);
+typedef struct {
+  range_fn fn;
+  void *ctx;
+  uint32_t lo, hi;
+  int status;
+} pf_job;
+
+static void *pf_thread(void *arg) {
+  pf_job *j = (pf_job *)arg;
+  j->fn(j->ctx, j->lo, j->hi, &j->status);
+  return NULL;
+}
+
+static int parallel_for(uint32_t count, int nthreads, range_fn fn, void *ctx) {
+  if (nthreads < 1) nthreads = 1;
+  if ((uint32_t)nthreads > count) nthreads = count ? (int)count : 1;
+  if (nthreads == 1) {
+    int st = GSTO_OK;
+    fn(ctx, 0, count, &st);
+    return st;
+  }
+  pthread_t th[256];
+  pf_job jobs[256];
+  if (nthreads > 256) nthreads = 256;
+  for (int t = 0; t < nthreads; ++t) {
+    jobs[t].fn = fn;
+    jobs[t].ctx = ctx;
+    jobs[t].lo = (uint32_t)((uint64_t)count * t / nthreads);
+    jobs[t].hi = (uint32_t)((uint64_t)count * (t + 1) / nthreads);
+    jobs[t].status = GSTO_OK;
+    pthread_create(&th[t], NULL, pf_thread, &jobs[t]);
+  }
+  int st = GSTO_OK;
+  for (int t = 0; t < nthreads; ++t) {
+    pthread_join(th[t], NULL);
+    if (jobs[t].status != GSTO_OK) st = jobs[t].status;
+  }
+  return st;
+}
+
+typedef struct {
+  const uint8_t *gst;
+  gsto_header hdr;
+  gsto_section sec[4];
+  uint16_t freq[4][2048], cum[4][2048];
+  uint8_t sym[4][2048];
+  uint32_t group_base[5]; /* first flat group id per section */
+  uint8_t *symbols;       /* 7B + palette_bytes */
+  int8_t *planes;         /* 6 x B raster */
+  int32_t *indices;       /* B */
+  uint8_t *dxt;
+  uint32_t B, bx, by;
+} decode_ctx;
+
+static void rans_range(void *vctx, uint32_t lo, uint32_t hi, int *status) {
+  decode_ctx *c = (decode_ctx *)vctx;
+  const uint8_t *body = c->gst + GSTO_HEADER_BYTES + 4 * GSTO_FREQ_BYTES;
+  for (uint32_t fg = lo; fg < hi; ++fg) {
+    int s = 0;
+    while (fg >= c->group_base[s + 1]) ++s;
+    const uint32_t g = fg - c->group_base[s];
+    const uint8_t *sec = body + c->sec[s].in_off;
+    const size_t lo_bytes = g == 0 ? 4u * c->sec[s].ngroups : rd32(sec + 4 * (g - 1));
+    const int st = gsto_rans_decode_group(sec, c->sec[s].in_len, g, c->freq[s], c->cum[s], c->sym[s],
+                                          GSTO_STREAMS_PER_GROUP, lo_bytes,
+                                          c->symbols + c->sec[s].out_off + (size_t)g * GSTO_SYMS_PER_GROUP);
+    if (st != GSTO_OK) *status = st;
+  }
+}
+
+/* inverse_wavelet.cl:69-192 over all planes and 32x32 tiles; the block of tile
+ * (tx, ty) is the (ty * tiles_x + tx)-th 1024-byte run of the plane (:94-95)
+ * and lands at rows ty*32.., columns tx*32.. of the raster plane (:175-191). */
+static void wavelet_range(void *vctx, uint32_t lo, uint32_t hi, int *status) {
+  (void)status;
+  decode_ctx *c = (decode_ctx *)vctx;
+  const uint32_t tiles_x = c->bx / 32, tiles = (c->bx / 32) * (c->by / 32);
+  int8_t blk[1024];
+  for (uint32_t item = lo; item < hi; ++item) {
+    const uint32_t p = item / tiles, t = item % tiles;
+    const uint32_t tx = t % tiles_x, ty = t / tiles_x;
+    gsto_inverse_wavelet_block(c->symbols + (size_t)p * c->B + (size_t)t * 1024, blk);
+    int8_t *plane = c->planes + (size_t)p * c->B;
+    for (uint32_t r = 0; r < 32; ++r)
+      memcpy(plane + (size_t)(ty * 32 + r) * c->bx + tx * 32, blk + r * 32, 32);
+  }
+}
+
+/* assemble.cl:64-81 (assemble_dxt), rows [lo, hi) of blocks. */
+static void assemble_range(void *vctx, uint32_t lo, uint32_t hi, int *status) {
+  decode_ctx *c = (decode_ctx *)vctx;
+  const uint8_t *palette = c->symbols + c->sec[2].out_off;
+  const uint32_t nwords = c->hdr.palette_bytes / 4;
+  const int8_t *Y1 = c->planes, *Y2 = c->planes + c->B, *Co1 = c->planes + 2 * (size_t)c->B,
+               *Cg1 = c->planes + 3 * (size_t)c->B, *Co2 = c->planes + 4 * (size_t)c->B,
+               *Cg2 = c->planes + 5 * (size_t)c->B;
+  for (uint32_t i = lo * c->bx; i < hi * c->bx; ++i) {
+    const uint16_t ep1 = gsto_ycocg_to_565(Y1[i], Co1[i], Cg1[i]);
+    const uint16_t ep2 = gsto_ycocg_to_565(Y2[i], Co2[i], Cg2[i]);
+    const uint32_t idx = (uint32_t)c->indices[i];
+    uint32_t word = 0;
+    if (idx < nwords) word = rd32(palette + 4 * (size_t)idx);
+    else *status = GSTO_E_FORMAT;
+    wr16(c->dxt + 8 * (size_t)i, ep1);
+    wr16(c->dxt + 8 * (size_t)i + 2, ep2);
+    wr32(c->dxt + 8 * (size_t)i + 4, word);
+  }
+}
+
+static int setup_ctx(decode_ctx *c, const uint8_t *gst, size_t n) {
+  int st = gsto_parse_header(gst, n, &c->hdr);
+  if (st != GSTO_OK) return st;
+  c->gst = gst;
+  section_layout(&c->hdr, c->sec);
+  c->bx = c->hdr.width / 4;
+  c->by = c->hdr.height / 4;
+  c->B = c->bx * c->by;
+  c->group_base[0] = 0;
+  for (int s = 0; s < 4; ++s) {
+    uint16_t f[256];
+    for (int k = 0; k < 256; ++k) f[k] = rd16(gst + GSTO_HEADER_BYTES + s * GSTO_FREQ_BYTES + 2 * k);
+    gsto_build_table(f, c->freq[s], c->cum[s], c->sym[s]);
+    c->group_base[s + 1] = c->group_base[s] + c->sec[s].ngroups;
+  }
+  return GSTO_OK;
+}
+
+int gsto_decode_symbols(const uint8_t *gst, size_t n, uint8_t *symbols, size_t cap, int nthreads) {
+  decode_ctx *c = (decode_ctx *)calloc(1, sizeof(decode_ctx));
+  if (!c) return GSTO_E_ARG;
+  int st = setup_ctx(c, gst, n);
+  if (st == GSTO_OK) {
+    const size_t need = 7 * (size_t)c->B + c->hdr.palette_bytes;
+    if (!symbols || cap < need) st = GSTO_E_ARG;
+    else {
+      c->symbols = symbols;
+      st = parallel_for(c->group_base[4], nthreads, rans_range, c);
+    }
+  }
+  free(c);
+  return st;
+}
+
+int gsto_decode(const uint8_t *gst, size_t n, uint8_t *dxt_out, size_t out_cap, int scan_mode,
+                int nthreads) {
+  decode_ctx *c = (decode_ctx *)calloc(1, sizeof(decode_ctx));
+  if (!c) return GSTO_E_ARG;
+  int st = setup_ctx(c, gst, n);
+  if (st != GSTO_OK) {
+    free(c);
+    return st;
+  }
+  if (!dxt_out || out_cap < 8 * (size_t)c->B) {
+    free(c);
+    return GSTO_E_ARG;
+  }
+  c->dxt = dxt_out;
+  c->symbols = (uint8_t *)malloc(7 * (size_t)c->B + c->hdr.palette_bytes);
+  c->planes = (int8_t *)malloc(6 * (size_t)c->B);
+  c->indices = (int32_t *)malloc(4 * (size_t)c->B);
+  if (!c->symbols || !c->planes || !c->indices) {
+    st = GSTO_E_ARG;
+  } else {
+    int s1 = parallel_for(c->group_base[4], nthreads, rans_range, c);
+    parallel_for(6 * (c->bx / 32) * (c->by / 32), nthreads, wavelet_range, c);
+    gsto_scan_indices(c->symbols + c->sec[3].out_off, c->B, c->indices, scan_mode);
+    int s2 = parallel_for(c->by, nthreads, assemble_range, c);
+    st = s1 != GSTO_OK ? s1 : s2;
+  }
+  free(c->symbols);
+  free(c->planes);
+  free(c->indices);
+  free(c);
+  return st;
+}
+
+int gsto_decode_batch(const uint8_t *const *gst, const size_t *lens, int n_streams,
+                      uint8_t *dxt_out, size_t out_cap, int scan_mode, int nthreads) {
+  size_t off = 0;
+  int status = GSTO_OK;
+  for (int i = 0; i < n_streams; ++i) {
+    gsto_header h;
+    int st = gsto_parse_header(gst[i], lens[i], &h);
+    if (st != GSTO_OK) return st;
+    const size_t sz = (size_t)h.width * h.height / 2;
+    if (off + sz > out_cap) return GSTO_E_ARG;
+    st = gsto_decode(gst[i], lens[i], dxt_out + off, sz, scan_mode, nthreads);
+    if (st == GSTO_E_ARG) return st;
+    if (st != GSTO_OK) status = st;
+    off += sz;
+  }
+  return status;
+}
+
+/* ans_decode.cl:185-204 */
+uint32_t gsto_section_search(const uint32_t *oo, uint32_t num_offsets, uint32_t wg) {
+  const uint32_t id = wg * GSTO_STREAMS_PER_GROUP * GSTO_SYMS_PER_STREAM;
+  uint32_t low = 0, high = num_offsets - 1, x = (high + low) / 2;
+  const uint32_t iters = 32 - (uint32_t)__builtin_clz(high - low + 1);
+  for (uint32_t i = 0; i < iters; ++i) {
+    const uint32_t too_high = (uint32_t)(id < oo[x]);
+    const uint32_t too_low = (uint32_t)(x < (num_offsets - 1) && oo[x + 1] <= id);
+    const uint32_t lo1 = (low + 1 > x) ? low + 1 : x;
+    const uint32_t hi1 = (high - 1 < x) ? high - 1 : x;
+    low = too_low * lo1 + (1 - too_low) * low;
+    high = too_high * hi1 + (1 - too_high) * high;
+    x = (high + low) >> 1;
+  }
+  return x;
+}

@@ -1,0 +1,224 @@
+"""CUDA decode path vs the oracle and the golden fixtures, through the C ABI.
+
+Bit-exact everywhere (integer and byte work).  Small cases compare against the
+CPU oracle directly; full-size cases (8192x8192, the 2^26-symbol rANS section)
+check the size-independent property that decoding returns exactly what the
+encoder encoded, plus the oracle where it finishes in seconds."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import as_blocks, golden_stream
+from gst_gb300 import decoder, encoder, workloads
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+SHA = lambda b: hashlib.sha256(bytes(b)).hexdigest()  # noqa: E731
+
+
+def to_dev(a) -> "torch.Tensor":
+    return torch.from_numpy(np.ascontiguousarray(np.frombuffer(bytes(a), dtype=np.uint8)).copy()).cuda()
+
+
+def batch_decode(ctx, streams, stream=None):
+    hdrs, packed = decoder.pack_batch(streams)
+    d_cmp = torch.from_numpy(packed).cuda()
+    total = sum(h.dxt_bytes for h in hdrs)
+    d_out = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    decoder.load_compressed_dxts(ctx, hdrs, d_cmp, d_out, stream)
+    st = decoder.sync_status(ctx, stream)
+    out = d_out.cpu().numpy()
+    res, off = [], 0
+    for h in hdrs:
+        res.append(out[off:off + h.dxt_bytes])
+        off += h.dxt_bytes
+    return st, res
+
+
+@pytest.mark.parametrize("name", ["test1.gst", "synth512_s0.gst"])
+def test_decompress_dxt_golden(gpu_ctx, golden, name):
+    # codec/test/codec_test.cpp:36-48 on the GPU: DecompressDXT == PhysicalBlocks().
+    out = decoder.decompress_dxt(gpu_ctx, golden_stream(name))
+    assert SHA(out) == golden["streams"][name]["blocks_sha256"]
+    st, ref = oracle.decode(golden_stream(name))
+    assert np.array_equal(out, ref)
+
+
+def test_non_power_of_two_block_count_matches_encoder(gpu_ctx, golden):
+    # The GPU computes the exact index prefix sum: it reproduces the encoder's
+    # blocks, where the reference's staged scan differs in the last block.
+    g = golden["streams"]["synth768x512_s3.gst"]
+    out = decoder.decompress_dxt(gpu_ctx, golden_stream("synth768x512_s3.gst"))
+    assert SHA(out) == g["blocks_sha256"]
+    st, ref_scan = oracle.decode(golden_stream("synth768x512_s3.gst"), oracle.SCAN_REFERENCE)
+    assert np.nonzero(as_blocks(out) != as_blocks(ref_scan))[0].tolist() == g["reference_scan_mismatch"]
+
+
+@pytest.mark.parametrize("idx", range(4))
+def test_rans_vectors(gpu_ctx, golden, rans_blob, idx):
+    # ans/ans_ocl_test.cpp:157-345 (1, 24 and 32 interleaved streams).
+    c = golden["rans"][idx]
+    body = rans_blob[c["body_off"]: c["body_off"] + c["body_len"]]
+    want = np.frombuffer(rans_blob[c["sym_off"]: c["sym_off"] + c["sym_len"]], dtype=np.uint8)
+    freqs = np.zeros(256, np.uint16)
+    freqs[: len(c["freqs"])] = c["freqs"]
+    d_f = to_dev(freqs.tobytes())
+    d_b = to_dev(body)
+    d_o = torch.zeros(want.size, dtype=torch.uint8, device="cuda")
+    decoder.decode_rans_groups(gpu_ctx, d_f, d_b, len(body), c["n_groups"], c["streams"], d_o)
+    assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
+    assert np.array_equal(d_o.cpu().numpy(), want)
+
+
+def test_batch_of_mixed_sizes_matches_oracle_and_encoder(gpu_ctx):
+    imgs = [workloads.encode_image(w, h, 300 + i) for i, (w, h) in enumerate(
+        [(512, 512), (1024, 512), (512, 1024), (1024, 1024), (2048, 512), (512, 2048), (512, 512)])]
+    streams = [im.stream for im in imgs] + [golden_stream("test1.gst")]
+    st, outs = batch_decode(gpu_ctx, streams)
+    assert st == decoder.GST_OK
+    for im, out in zip(imgs, outs):
+        assert np.array_equal(as_blocks(out), im.blocks)
+    for s, out in zip(streams, outs):
+        st_o, ref = oracle.decode(s, oracle.SCAN_EXACT, nthreads=4)
+        assert st_o == 0 and np.array_equal(out, ref)
+
+
+def test_same_result_alone_and_in_batch(gpu_ctx):
+    imgs = [workloads.encode_image(w, h, 400 + i) for i, (w, h) in enumerate([(1024, 512), (512, 512), (1024, 1024)])]
+    st, together = batch_decode(gpu_ctx, [im.stream for im in imgs])
+    assert st == 0
+    for im, t in zip(imgs, together):
+        alone = decoder.decompress_dxt(gpu_ctx, im.stream)
+        assert np.array_equal(alone, t)
+
+
+def test_device_resident_single_image(gpu_ctx):
+    s = golden_stream("synth512_s0.gst")
+    st, outs = batch_decode(gpu_ctx, [s])
+    assert st == 0
+    assert np.array_equal(outs[0], oracle.decode(s)[1])
+
+
+def test_repeated_decodes_are_identical(gpu_ctx):
+    s = workloads.encode_image(2048, 1024, 17).stream
+    a = decoder.decompress_dxt(gpu_ctx, s)
+    b = decoder.decompress_dxt(gpu_ctx, s)
+    assert np.array_equal(a, b)
+
+
+def test_single_symbol_sections(gpu_ctx):
+    # A flat image: every section but the chroma/luma ones has one symbol, whose
+    # frequency is 2048 (no renormalisation words at all).
+    rgb = np.full((512, 512, 3), 77, np.uint8)
+    stream, blocks, clips = encoder.encode_rgb(rgb)
+    out = decoder.decompress_dxt(gpu_ctx, stream)
+    assert np.array_equal(as_blocks(out), blocks)
+
+
+def test_large_8192_round_trip(gpu_ctx):
+    im = workloads.large()
+    out = decoder.decompress_dxt(gpu_ctx, im.stream)
+    assert np.array_equal(as_blocks(out), im.blocks)
+    st, ref = oracle.decode(im.stream, oracle.SCAN_EXACT, nthreads=16)
+    assert st == 0 and np.array_equal(out, ref)
+
+
+def test_rans_micro_full_size(gpu_ctx):
+    sec = workloads.rans_section()
+    d_f = to_dev(sec.section[:512])
+    d_b = to_dev(sec.section[512:])
+    d_o = torch.zeros(sec.symbols.size, dtype=torch.uint8, device="cuda")
+    decoder.decode_rans_groups(gpu_ctx, d_f, d_b, len(sec.section) - 512, sec.n_groups, 32, d_o)
+    assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
+    assert np.array_equal(d_o.cpu().numpy(), sec.symbols)
+
+
+def test_corrupted_payloads_match_oracle_and_are_flagged(gpu_ctx):
+    # Byte flips inside group payloads pass header validation; the kernels keep
+    # every read inside its group and the palette, and report GST_E_FORMAT when
+    # a read would leave them -- exactly as the oracle does.
+    base = bytearray(golden_stream("synth512_s0.gst"))
+    rng = np.random.default_rng(9)
+    hdr = decoder.parse_header(bytes(base))
+    body = 28 + 2048
+    flagged = 0
+    for trial in range(12):
+        s = bytearray(base)
+        lo = body + 4 * 64  # past the Y section's offset table
+        hi = body + hdr.compressed_bytes
+        for pos in rng.integers(lo, hi, size=8):
+            s[int(pos)] ^= int(rng.integers(1, 256))
+        s = bytes(s)
+        try:
+            decoder.parse_header(s)
+        except decoder.GstError:
+            continue  # a flip hit an offset table: rejected on the host
+        st_g, outs = batch_decode(gpu_ctx, [s])
+        st_o, ref = oracle.decode(s, oracle.SCAN_EXACT)
+        assert st_g == st_o, trial
+        assert np.array_equal(outs[0], ref), trial
+        flagged += st_g != 0
+    # The context stays usable afterwards.
+    out = decoder.decompress_dxt(gpu_ctx, golden_stream("test1.gst"))
+    assert np.array_equal(out, oracle.decode(golden_stream("test1.gst"))[1])
+
+
+def test_device_checks_tables_and_group_offsets(gpu_ctx):
+    # On the device-resident path the host holds only headers: a bad table sum
+    # or group end offset is caught by the kernels, not by a fault.
+    s = bytearray(golden_stream("synth512_s0.gst"))
+    s[28:30] = (int.from_bytes(s[28:30], "little") + 1).to_bytes(2, "little")
+    hdrs = [decoder.GenTCHeader.load_from(bytes(s))]
+    packed = np.zeros(decoder.batch_layout_bytes(hdrs), np.uint8)
+    packed[512:512 + 2048] = np.frombuffer(bytes(s[28:28 + 2048]), np.uint8)
+    packed[512 + 2048:] = np.frombuffer(bytes(s[28 + 2048:]), np.uint8)
+    d_cmp = torch.from_numpy(packed).cuda()
+    d_out = torch.zeros(hdrs[0].dxt_bytes, dtype=torch.uint8, device="cuda")
+    decoder.load_compressed_dxts(gpu_ctx, hdrs, d_cmp, d_out)
+    assert decoder.sync_status(gpu_ctx) == decoder.GST_E_FORMAT
+    s2 = bytearray(golden_stream("synth512_s0.gst"))
+    body = 28 + 2048
+    s2[body + 4: body + 8] = (1 << 30).to_bytes(4, "little")
+    packed[512:512 + 2048] = np.frombuffer(bytes(s2[28:28 + 2048]), np.uint8)
+    packed[512 + 2048:] = np.frombuffer(bytes(s2[28 + 2048:]), np.uint8)
+    d_cmp = torch.from_numpy(packed).cuda()
+    decoder.load_compressed_dxts(gpu_ctx, hdrs, d_cmp, d_out)
+    assert decoder.sync_status(gpu_ctx) == decoder.GST_E_FORMAT
+    assert decoder.sync_status(gpu_ctx) == decoder.GST_OK  # cleared
+
+
+def test_preallocated_scratch():
+    ctx = decoder.GPUContext(0)
+    try:
+        s = golden_stream("test1.gst")
+        h = decoder.parse_header(s)
+        decoder.preallocate_decompressor(ctx, decoder.required_scratch_mem(h))
+        out = decoder.decompress_dxt(ctx, s)
+        assert np.array_equal(out, oracle.decode(s)[1])
+        big = workloads.encode_image(1024, 1024, 3).stream
+        with pytest.raises(decoder.GstError) as e:
+            decoder.decompress_dxt(ctx, big)
+        assert e.value.status == decoder.GST_E_OOM
+        decoder.free_decompressor(ctx)
+        out = decoder.decompress_dxt(ctx, big)
+        assert np.array_equal(out, oracle.decode(big, oracle.SCAN_EXACT)[1])
+    finally:
+        ctx.close()
+
+
+def test_host_validation_before_launch(gpu_ctx):
+    s = golden_stream("test1.gst")
+    with pytest.raises(decoder.GstError) as e:
+        decoder.decompress_dxt(gpu_ctx, s[:-100])
+    assert e.value.status == decoder.GST_E_FORMAT
+
+
+def test_stream_argument_and_launch_count(gpu_ctx):
+    s = golden_stream("synth512_s0.gst")
+    side = torch.cuda.Stream()
+    st, outs = batch_decode(gpu_ctx, [s, s], stream=side)
+    assert st == 0 and np.array_equal(outs[0], outs[1])
+    assert gpu_ctx.last_launch_count() == 2

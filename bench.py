@@ -54,6 +54,8 @@ def parse_args():
     p.add_argument("--impl", choices=("gst", "reference"), default="gst")
     p.add_argument("--skip-extra", action="store_true", help="headline workload only")
     p.add_argument("--cpu-sample", type=int, default=16, help="images of the batch the CPU baseline decodes")
+    p.add_argument("--only", choices=("batched", "large", "plain", "rans"),
+                   help="time one workload's decode call only (a small command for profilers)")
     return p.parse_args()
 
 
@@ -101,18 +103,30 @@ class ClockSampler:
         self.proc = None
         self.path = Path(tempfile.mkstemp(prefix="gst_clocks_", suffix=".csv")[1])
 
+    def _lines(self) -> int:
+        try:
+            return len(self.path.read_text().splitlines())
+        except OSError:
+            return 0
+
     def __enter__(self):
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
+            t0 = time.time()
+            while self._lines() < 1 and time.time() - t0 < 5 and self.proc.poll() is None:
+                time.sleep(0.02)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
 
     def __exit__(self, *exc):
         if self.proc is not None:
+            t0 = time.time()
+            while self._lines() < 3 and time.time() - t0 < 3 and self.proc.poll() is None:
+                time.sleep(0.05)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -211,6 +225,37 @@ def kernel_summary(kern_steps):
     total = sum(sum(v) for v in agg.values()) or 1.0
     return {name: {"avg_ms": statistics.mean(v), "launches": len(v), "share": sum(v) / total}
             for name, v in agg.items()}
+
+
+def run_only(args, local):
+    """One workload's decode call, timed; for profiler command lines."""
+    import torch
+    from gst_gb300 import decoder, workloads
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    ctx = decoder.GPUContext(local)
+    stream = torch.cuda.Stream(device)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=device)
+    if args.only == "rans":
+        sec = workloads.rans_section()
+        d_f = torch.from_numpy(np.frombuffer(sec.section[:512], np.uint8).copy()).to(device)
+        d_b = torch.from_numpy(np.frombuffer(sec.section[512:], np.uint8).copy()).to(device)
+        d_o = torch.empty(sec.symbols.size, dtype=torch.uint8, device=device)
+        fn = lambda: decoder.decode_rans_groups(ctx, d_f, d_b, len(sec.section) - 512, sec.n_groups, 32, d_o, stream)  # noqa: E731
+        t, _ = time_steps(fn, args.steps, args.warmup, stream, flush)
+        ok = bool(np.array_equal(d_o.cpu().numpy(), sec.symbols))
+        units = sec.symbols.size
+    else:
+        imgs = {"batched": lambda: workloads.batched(64), "large": lambda: [workloads.large()],
+                "plain": lambda: [workloads.plain(0)]}[args.only]()
+        b = Batch(imgs, device)
+        fn = lambda: decoder.load_compressed_dxts(ctx, b.hdrs, b.d_cmp, b.d_out, stream)  # noqa: E731
+        t, _ = time_steps(fn, args.steps, args.warmup, stream, flush)
+        ok = bool(np.array_equal(b.d_out.cpu().numpy().view(np.uint64), b.expected()))
+        units = b.pixels
+    ctx.close()
+    return {"only": args.only, "ms_per_call": round(statistics.mean(t), 4), "units_per_call": units,
+            "bit_exact": ok, "steps": args.steps, "warmup": args.warmup}
 
 
 def run_gst(args, rank, world, local):
@@ -432,6 +477,8 @@ def main():
     rank, world, local = dist_init(args.gpus)
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.only:
+        line = run_only(args, local)
     else:
         line = run_gst(args, rank, world, local)
     if rank == 0 and line is not None:

@@ -42,9 +42,10 @@ __device__ __forceinline__ void flag_error(uint32_t *err, uint32_t bits) { atomi
 // ---------------------------------------------------------------------------
 // Decode table (ans/build_table.cl:12-83).  Slot s in [0, 2048) belongs to the
 // symbol x with cum[x] <= s < cum[x] + freq[x]; the table stores
-// freq | (s - cum) << 12 | x << 23 so that one lookup gives the next state,
+// (s - cum) | freq << 11 | x << 24 so that one lookup gives the next state,
 // x' = (x >> 11) * freq + (s - cum), equal to the reference's
-// (x >> 11) * freq - cum + s in u32 arithmetic.  Requires blockDim.x == 256.
+// (x >> 11) * freq - cum + s in u32 arithmetic, and the symbol is the top
+// byte.  Requires blockDim.x == 256.
 // Returns false (block-uniformly) if the frequencies do not sum to 2048.
 __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t *tbl, uint32_t *cum_s,
                                    uint32_t *f_s, uint32_t *wsum) {
@@ -72,25 +73,165 @@ __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t 
 #pragma unroll
     for (uint32_t step = 128; step >= 1; step >>= 1)
       if (cum_s[x + step] <= s) x += step;
-    tbl[s] = f_s[x] | ((s - cum_s[x]) << 12) | (x << 23);
+    tbl[s] = (s - cum_s[x]) | (f_s[x] << 11) | (x << 24);
   }
   __syncthreads();
   return true;
 }
 
 // ---------------------------------------------------------------------------
+// rANS kernel shared memory: the decode table, the table-build scratch, and one
+// staging buffer per warp holding (the top of) its group's renormalisation
+// words, so that the serial decode chain reads shared memory, not HBM.
+constexpr int kStageWords = 2816;               // 16-bit words staged per group (5.5 KB)
+constexpr int kStagePitch = kStageWords + 8;    // + slack for the 16-byte alignment of the copy
+struct alignas(16) RansSmem {
+  uint32_t tbl[kTableSize];
+  uint32_t cum[257];
+  uint32_t f[256];
+  uint32_t wsum[8];
+  alignas(16) uint16_t stage[kGroupsPerRansCta][kStagePitch];
+};
+constexpr size_t kRansSmemBytes = sizeof(RansSmem);
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Warp-cooperative copy of the 4-aligned byte range [a, b) into `buf`, where
+// buf[0] corresponds to the 16-byte-aligned address at or below a.  The bulk
+// goes as 16-byte cp.async copies, the unaligned ends as 4-byte ones; nothing
+// outside [a, b) is read.
+__device__ __forceinline__ void stage_range(uint8_t *buf, const uint8_t *a, const uint8_t *b, int lane) {
+  const uintptr_t ua = reinterpret_cast<uintptr_t>(a), ub = reinterpret_cast<uintptr_t>(b);
+  const uintptr_t origin = ua & ~uintptr_t(15);
+  uintptr_t m0 = (ua + 15) & ~uintptr_t(15), m1 = ub & ~uintptr_t(15);
+  if (m0 >= m1) m0 = m1 = ub;  // no whole 16-byte chunk: all 4-byte copies
+  const int head = static_cast<int>((m0 - ua) >> 2), tail = static_cast<int>((ub - m1) >> 2);
+  if (lane < head) cp_async4(buf + (ua + 4 * lane - origin), reinterpret_cast<const void *>(ua + 4 * lane));
+  if (lane < tail) cp_async4(buf + (m1 + 4 * lane - origin), reinterpret_cast<const void *>(m1 + 4 * lane));
+  const int chunks = static_cast<int>((m1 - m0) >> 4);
+  for (int c = lane; c < chunks; c += 32)
+    cp_async16(buf + (m0 + 16 * c - origin), reinterpret_cast<const void *>(m0 + 16 * c));
+  cp_async_wait_all();
+  __syncwarp();
+}
+
+// One rANS step for every lane (ans_decode.cl:120-148).  Returns the new
+// state's renormalisation need; `e` receives the table entry (symbol in its top
+// byte).
+__device__ __forceinline__ uint32_t rans_advance(uint32_t x, const uint32_t *__restrict__ tbl, uint32_t *e_out) {
+  const uint32_t e = tbl[x & (kTableSize - 1)];
+  *e_out = e;
+  return (x >> 11) * ((e >> 11) & 0xFFFu) + (e & 0x7FFu);
+}
+
+// Decodes one group: ns <= 32 interleaved streams of 256 symbols whose final
+// states sit at [top, hi) and whose renormalisation words fill [lo, top) of
+// the section `sec` (ans_decode.cl:25-74).  Lane l is stream l.  When INDEX,
+// also returns the lane's suffix sums of (symbol - 128) after 32, 64, ..., 256
+// steps in suf[] (the palette-index deltas).
+//
+// FAST: the whole word region is staged in shared memory.  Every lane then
+// reads the stage each step (a clamped, always in-bounds read; only lanes that
+// renormalise keep the word), with no per-step branch; a valid stream never
+// reads below the region, and the final read pointer tells if a malformed one
+// did.  Otherwise the top kStageWords words are staged and reads below them go
+// to global memory with per-read checks.
+template <bool INDEX, bool FAST>
+__device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, uint32_t lo, uint32_t top,
+                                             const uint32_t *__restrict__ tbl, uint16_t *stage, int lane, bool active,
+                                             uint8_t *__restrict__ out, int32_t suf[8]) {
+  const uint32_t stage_lo = FAST ? lo : top - 2u * kStageWords;
+  stage_range(reinterpret_cast<uint8_t *>(stage), sec + stage_lo, sec + top, lane);
+  // stage[0] holds the word at sec + stage_lo rounded down to 16 bytes, so
+  // word idx of the section is stage[idx - sbase16].
+  const int sbase16 = static_cast<int>(stage_lo >> 1) -
+                      static_cast<int>((reinterpret_cast<uintptr_t>(sec + stage_lo) & 15) >> 1);
+  const int lo16 = static_cast<int>(lo >> 1), fast_lo = static_cast<int>(stage_lo >> 1);
+  const uint16_t *words = reinterpret_cast<const uint16_t *>(sec);
+  uint32_t x = active ? reinterpret_cast<const uint32_t *>(sec + top)[lane] : kRansL;
+  int ptr = static_cast<int>(top >> 1);
+  bool bad = false;
+  const uint32_t lt = lanemask_lt();
+  uint32_t total_sym = 0;
+  int32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0;
+#pragma unroll 2
+  for (int k = 0; k < 16; ++k) {
+    uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      uint32_t e;
+      x = rans_advance(x, tbl, &e);
+      const bool need = active && x < kRansL;
+      const uint32_t m = __ballot_sync(0xFFFFFFFFu, need);
+      const int total = __popc(m);
+      // ans_decode.cl:133-140: renormalising lanes read consecutive 16-bit
+      // words below the read pointer, the lowest lane the lowest address.
+      const int idx = ptr - total + __popc(m & lt);
+      if (FAST) {
+        const uint32_t si = min(static_cast<uint32_t>(idx - sbase16), static_cast<uint32_t>(kStagePitch - 1));
+        const uint32_t v = stage[si];
+        x = need ? __byte_perm(x, v, 0x1054) : x;
+      } else if (ptr - total >= fast_lo) {  // warp-uniform: every read is staged
+        if (need) x = __byte_perm(x, stage[idx - sbase16], 0x1054);
+      } else if (need) {
+        uint32_t v = 0;
+        if (idx >= fast_lo) v = stage[idx - sbase16];
+        else if (idx >= lo16) v = __ldg(words + idx);
+        else bad = true;
+        x = __byte_perm(x, v, 0x1054);
+      }
+      ptr -= total;
+      if (j < 4) w3 = __byte_perm(w3, e, 0x2107);
+      else if (j < 8) w2 = __byte_perm(w2, e, 0x2107);
+      else if (j < 12) w1 = __byte_perm(w1, e, 0x2107);
+      else w0 = __byte_perm(w0, e, 0x2107);
+      if (INDEX) total_sym += e >> 24;
+    }
+    // Steps 16k..16k+15 are positions 255-16k .. 240-16k of this stream
+    // (ans_decode.cl:154-155 stores the symbols in reverse).
+    if (active) *reinterpret_cast<uint4 *>(out + 240 - 16 * k) = make_uint4(w0, w1, w2, w3);
+    if (INDEX && (k & 1)) {
+      const int mm = k >> 1;
+      const int32_t v = static_cast<int32_t>(total_sym) - 4096 * (mm + 1);
+      s0 = mm == 0 ? v : s0;
+      s1 = mm == 1 ? v : s1;
+      s2 = mm == 2 ? v : s2;
+      s3 = mm == 3 ? v : s3;
+      s4 = mm == 4 ? v : s4;
+      s5 = mm == 5 ? v : s5;
+      s6 = mm == 6 ? v : s6;
+      s7 = mm == 7 ? v : s7;
+    }
+  }
+  if (INDEX) {
+    suf[0] = s0; suf[1] = s1; suf[2] = s2; suf[3] = s3;
+    suf[4] = s4; suf[5] = s5; suf[6] = s6; suf[7] = s7;
+  }
+  // In FAST mode the lowest word read is the final pointer.
+  if (FAST) bad = ptr < lo16;
+  return __any_sync(0xFFFFFFFFu, bad);
+}
+
 __global__ void __launch_bounds__(256) gst_rans_kernel(const uint8_t *__restrict__ cmp,
                                                        uint8_t *__restrict__ scratch, GstPlanView plan) {
-  __shared__ uint32_t tbl[kTableSize];
-  __shared__ uint32_t cum_s[257];
-  __shared__ uint32_t f_s[256];
-  __shared__ uint32_t wsum[8];
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  RansSmem &sm = *reinterpret_cast<RansSmem *>(smem_raw);
 
   const GstRansItem it = plan.rans[blockIdx.x];
   const GstImageDesc &im = plan.images[it.image];
   uint32_t *err = &plan.head->err;
   const uint16_t *freqs = reinterpret_cast<const uint16_t *>(cmp + im.freq_off + kFreqTableBytes * it.section);
-  const bool table_ok = build_decode_table(freqs, tbl, cum_s, f_s, wsum);
+  const bool table_ok = build_decode_table(freqs, sm.tbl, sm.cum, sm.f, sm.wsum);
   if (!table_ok && threadIdx.x == 0) flag_error(err, kErrTable);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -104,51 +245,24 @@ __global__ void __launch_bounds__(256) gst_rans_kernel(const uint8_t *__restrict
   const uint32_t lo = g == 0 ? 4u * G : ends[g - 1];
   const uint32_t ns = it.streams;
   const bool active = static_cast<uint32_t>(lane) < ns;
-  const bool group_ok = table_ok && (hi & 3u) == 0 && hi <= len && lo <= len && hi >= lo + 4u * ns;
+  const bool group_ok = table_ok && (hi & 3u) == 0 && (lo & 3u) == 0 && hi <= len && lo <= len &&
+                        hi >= lo + 4u * ns;
   const bool is_index = it.section == 3;
+  uint8_t *out = scratch + im.sym_off + im.sec_out[it.section] + static_cast<size_t>(g) * ns * kSymsPerStream +
+                 static_cast<size_t>(lane) * kSymsPerStream;
 
   int32_t suf[8];
-  uint32_t total_sym = 0;
   if (group_ok) {
     const uint32_t top = hi - 4u * ns;  // the group's final states sit at [top, hi)
-    uint32_t x = active ? reinterpret_cast<const uint32_t *>(sec + top)[lane] : kRansL;
-    const uint16_t *words = reinterpret_cast<const uint16_t *>(sec);
-    const uint32_t lo16 = lo >> 1, top16 = top >> 1;
-    uint32_t ptr = top16;
-    uint32_t bad = 0;
-    const uint32_t lt = lanemask_lt();
-    uint8_t *out = scratch + im.sym_off + im.sec_out[it.section] + static_cast<size_t>(g) * ns * kSymsPerStream +
-                   static_cast<size_t>(lane) * kSymsPerStream;
-#pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      uint32_t w[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const uint32_t e = tbl[x & (kTableSize - 1)];
-        x = (x >> 11) * (e & 0xFFFu) + ((e >> 12) & 0x7FFu);
-        const uint32_t sym = e >> 23;
-        const bool need = active && x < kRansL;
-        const uint32_t m = __ballot_sync(0xFFFFFFFFu, need);
-        const uint32_t total = __popc(m);
-        if (need) {
-          // ans_decode.cl:133-140: lanes that renormalise read consecutive
-          // 16-bit words below the read pointer, lowest lane lowest address.
-          const uint32_t idx = ptr - total + __popc(m & lt);
-          uint32_t v = 0;
-          if (idx - lo16 < top16 - lo16) v = __ldg(words + idx);
-          else bad = 1;
-          x = (x << 16) | v;
-        }
-        ptr -= total;
-        w[3 - j / 4] = (w[3 - j / 4] << 8) | sym;
-        total_sym += sym;
-      }
-      // Steps 16k..16k+15 are positions 255-16k .. 240-16k of this stream
-      // (ans_decode.cl:154-155 writes the symbols in reverse).
-      if (active) *reinterpret_cast<uint4 *>(out + 240 - 16 * k) = make_uint4(w[0], w[1], w[2], w[3]);
-      if (is_index && (k & 1)) suf[k >> 1] = static_cast<int32_t>(total_sym) - 128 * 32 * ((k >> 1) + 1);
-    }
-    if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(err, kErrStream);
+    const bool fits = top - lo <= 2u * kStageWords;  // warp-uniform
+    bool bad;
+    if (is_index)
+      bad = fits ? decode_group<true, true>(sec, lo, top, sm.tbl, sm.stage[warp], lane, active, out, suf)
+                 : decode_group<true, false>(sec, lo, top, sm.tbl, sm.stage[warp], lane, active, out, suf);
+    else
+      bad = fits ? decode_group<false, true>(sec, lo, top, sm.tbl, sm.stage[warp], lane, active, out, suf)
+                 : decode_group<false, false>(sec, lo, top, sm.tbl, sm.stage[warp], lane, active, out, suf);
+    if (bad && lane == 0) flag_error(err, kErrStream);
   } else if (lane == 0 && table_ok) {
     flag_error(err, kErrGroup);
   }
@@ -317,7 +431,14 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
   *launches = 0;
   if (ev) cudaEventRecord(ev[0], stream);
   if (plan.n_rans) {
-    gst_rans_kernel<<<plan.n_rans, 256, 0, stream>>>(d_cmp, d_scratch, plan);
+    static bool configured = false;  // per process; the attribute applies to every device context
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(gst_rans_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(kRansSmemBytes));
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    gst_rans_kernel<<<plan.n_rans, 256, kRansSmemBytes, stream>>>(d_cmp, d_scratch, plan);
     ++*launches;
     if (ev) cudaEventRecord(ev[*launches], stream);
   }

@@ -139,7 +139,9 @@ def test_rans_micro_full_size(gpu_ctx):
 def test_corrupted_payloads_match_oracle_and_are_flagged(gpu_ctx):
     # Byte flips inside group payloads pass header validation; the kernels keep
     # every read inside its group and the palette, and report GST_E_FORMAT when
-    # a read would leave them -- exactly as the oracle does.
+    # a read would leave them -- exactly when the oracle does.  With GST_OK the
+    # output is bit-exact; with GST_E_FORMAT it is unspecified (the reference's
+    # decoder reads out of bounds there).
     base = bytearray(golden_stream("synth512_s0.gst"))
     rng = np.random.default_rng(9)
     hdr = decoder.parse_header(bytes(base))
@@ -159,7 +161,8 @@ def test_corrupted_payloads_match_oracle_and_are_flagged(gpu_ctx):
         st_g, outs = batch_decode(gpu_ctx, [s])
         st_o, ref = oracle.decode(s, oracle.SCAN_EXACT)
         assert st_g == st_o, trial
-        assert np.array_equal(outs[0], ref), trial
+        if st_g == decoder.GST_OK:
+            assert np.array_equal(outs[0], ref), trial
         flagged += st_g != 0
     # The context stays usable afterwards.
     out = decoder.decompress_dxt(gpu_ctx, golden_stream("test1.gst"))

@@ -249,10 +249,12 @@ def run_only(args, local):
         imgs = {"batched": lambda: workloads.batched(64), "large": lambda: [workloads.large()],
                 "plain": lambda: [workloads.plain(0)]}[args.only]()
         b = Batch(imgs, device)
-        fn = lambda: decoder.load_compressed_dxts(ctx, b.hdrs, b.d_cmp, b.d_out, stream)  # noqa: E731
+        rb = decoder.ResidentBatch(ctx, b.hdrs)
+        fn = lambda: rb.launch(b.d_cmp, b.d_out, stream, graph=True)  # noqa: E731
         t, _ = time_steps(fn, args.steps, args.warmup, stream, flush)
         ok = bool(np.array_equal(b.d_out.cpu().numpy().view(np.uint64), b.expected()))
         units = b.pixels
+        rb.close()
     ctx.close()
     return {"only": args.only, "ms_per_call": round(statistics.mean(t), 4), "units_per_call": units,
             "bit_exact": ok, "steps": args.steps, "warmup": args.warmup}
@@ -269,45 +271,51 @@ def run_gst(args, rank, world, local):
     encode_s = time.time() - t0
     batch = Batch(images, device)
     ctx = decoder.GPUContext(local)
-    ctx.set_profiling(True)
     stream = torch.cuda.Stream(device)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=device)
+    rb = decoder.ResidentBatch(ctx, batch.hdrs)
 
-    def step_batched():
-        decoder.load_compressed_dxts(ctx, batch.hdrs, batch.d_cmp, batch.d_out, stream)
+    def step_batched():  # the resident batch, replayed as a captured CUDA graph
+        rb.launch(batch.d_cmp, batch.d_out, stream, graph=True)
 
-    def step_per_image():
+    def step_profiled():  # the same launch sequence, direct, with events between kernels
+        rb.launch(batch.d_cmp, batch.d_out, stream)
+
+    def step_per_image():  # the plain per-image path: one gst_load_compressed_dxt call per image
         base = batch.d_out.data_ptr()
         for h, d_one, off in batch.views:
             decoder.load_compressed_dxt(ctx, h, d_one, base + off, stream)
 
-    def step_e2e():
+    def step_e2e():  # host buffers: pinned H2D, decode, D2H of the DXT1 blocks
         with torch.cuda.stream(stream):
             batch.d_cmp.copy_(batch.h_cmp, non_blocking=True)
-        decoder.load_compressed_dxts(ctx, batch.hdrs, batch.d_cmp, batch.d_out, stream)
+        rb.launch(batch.d_cmp, batch.d_out, stream, graph=True)
         with torch.cuda.stream(stream):
             batch.h_out.copy_(batch.d_out, non_blocking=True)
 
     peak, peak_kind = measured_peak_hbm()
     barrier(world)
     with ClockSampler(local) as clocks:
-        times, kern = time_steps(step_batched, args.steps, args.warmup, stream, flush, ctx)
+        times, _ = time_steps(step_batched, args.steps, args.warmup, stream, flush)
     clock = clocks.summary()
-    launches_per_step = ctx.last_launch_count()
     stream.synchronize()
     got = batch.d_out.cpu().numpy().view(np.uint64)
     bit_exact = bool(np.array_equal(got, batch.expected()))
     status = decoder.sync_status(ctx, stream)
 
+    ctx.set_profiling(True)
+    _, kern = time_steps(step_profiled, args.steps, 2, stream, flush, ctx)
+    ctx.set_profiling(False)
+    launches_per_step = ctx.last_launch_count()
+
     total_ms = max_over_ranks(sum(times), world)
     ms_per_step = total_ms / args.steps
     value = world * batch.pixels * args.steps / (total_ms / 1e3) / 1e6
     ksum = kernel_summary(kern)
-    kernel_ms = sum(k["avg_ms"] for k in ksum.values())
     dominant = max(ksum.items(), key=lambda kv: kv[1]["share"])[0] if ksum else None
 
     # per-image path
-    t_img, k_img = time_steps(step_per_image, max(3, args.steps // 4), 2, stream, flush, ctx)
+    t_img, _ = time_steps(step_per_image, max(3, args.steps // 4), 2, stream, flush)
     per_image_ms = statistics.mean(t_img)
     got_pi = batch.d_out.cpu().numpy().view(np.uint64)
     per_image_exact = bool(np.array_equal(got_pi, batch.expected()))
@@ -332,7 +340,8 @@ def run_gst(args, rank, world, local):
         "dtype": "u8",
         "data": "synthetic",
         "config": {
-            "workload": "batched: 64 synthetic images, w,h in {512,1024,2048}, seeds 1000+i, one call per step",
+            "workload": "batched: 64 synthetic images, w,h in {512,1024,2048}, seeds 1000+i, one resident-batch "
+                        "graph launch per step",
             "images": len(images),
             "pixels_per_step": batch.pixels,
             "gst_bytes_per_step": batch.gst_bytes,
@@ -341,16 +350,18 @@ def run_gst(args, rank, world, local):
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
         },
         "dxt1_gbs": round(batch.out_bytes * args.steps / (total_ms / 1e3) / 1e9 * world, 2),
+        "p50_ms": round(float(np.percentile(times, 50)), 4),
+        "p99_ms": round(float(np.percentile(times, 99)), 4),
         "bit_exact": bit_exact and status == 0,
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clock,
         "roofline": {
             "bound": "hbm",
-            "kernel": "one decode call (" + " + ".join(ksum) + ")",
-            "achieved": round(batch.alg_bytes / (kernel_ms / 1e3) / 1e9, 1),
+            "kernel": "one batch decode (graph of " + " + ".join(ksum) + ")",
+            "achieved": round(batch.alg_bytes / (ms_per_step / 1e3) / 1e9, 1),
             "peak": peak,
             "unit": "GB/s",
-            "frac": round(batch.alg_bytes / (kernel_ms / 1e3) / 1e9 / peak, 4),
+            "frac": round(batch.alg_bytes / (ms_per_step / 1e3) / 1e9 / peak, 4),
             "peak_source": f"{peak_kind} hbm_gbs",
             "traffic": None,
             "algorithmic_bytes_per_launch": batch.alg_bytes,
@@ -378,6 +389,7 @@ def run_gst(args, rank, world, local):
         line["workloads"] = extra_workloads(ctx, stream, flush, device, peak, args)
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(images[: args.cpu_sample])
+    rb.close()
     ctx.close()
     return line
 
@@ -389,26 +401,31 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
     steps = max(5, args.steps // 2)
     for name, imgs in (("large_8192", [workloads.large()]), ("plain_512", [workloads.plain(0)])):
         b = Batch(imgs, device)
-        fn = lambda b=b: decoder.load_compressed_dxts(ctx, b.hdrs, b.d_cmp, b.d_out, stream)  # noqa: E731
-        t, k = time_steps(fn, steps, 3, stream, flush, ctx)
-        ks = kernel_summary(k)
-        kms = sum(v["avg_ms"] for v in ks.values())
+        rb = decoder.ResidentBatch(ctx, b.hdrs)
+        fn = lambda b=b, rb=rb: rb.launch(b.d_cmp, b.d_out, stream, graph=True)  # noqa: E731
+        t, _ = time_steps(fn, steps, 3, stream, flush)
         ok = bool(np.array_equal(b.d_out.cpu().numpy().view(np.uint64), b.expected()))
+        ctx.set_profiling(True)
+        _, k = time_steps(lambda b=b, rb=rb: rb.launch(b.d_cmp, b.d_out, stream), 3, 1, stream, flush, ctx)
+        ctx.set_profiling(False)
+        ks = kernel_summary(k)
+        ms = statistics.mean(t)
         out[name] = {
-            "value": round(b.pixels / (statistics.mean(t) / 1e3) / 1e6, 2), "unit": "Mpix/s",
-            "ms_per_call": round(statistics.mean(t), 4),
+            "value": round(b.pixels / (ms / 1e3) / 1e6, 2), "unit": "Mpix/s",
+            "ms_per_call": round(ms, 4),
             "p50_ms": round(float(np.percentile(t, 50)), 4), "p99_ms": round(float(np.percentile(t, 99)), 4),
-            "dxt1_gbs": round(b.out_bytes / (statistics.mean(t) / 1e3) / 1e9, 2),
-            "hbm_frac_of_kernels": round(b.alg_bytes / (kms / 1e3) / 1e9 / peak, 4),
+            "dxt1_gbs": round(b.out_bytes / (ms / 1e3) / 1e9, 2),
+            "hbm_frac": round(b.alg_bytes / (ms / 1e3) / 1e9 / peak, 4),
             "kernels": {kk: round(v["avg_ms"], 4) for kk, v in ks.items()},
             "gst_bytes": b.gst_bytes, "bit_exact": ok,
         }
+        rb.close()
     sec = workloads.rans_section()
     d_f = torch.from_numpy(np.frombuffer(sec.section[:512], np.uint8).copy()).to(device)
     d_b = torch.from_numpy(np.frombuffer(sec.section[512:], np.uint8).copy()).to(device)
     d_o = torch.empty(sec.symbols.size, dtype=torch.uint8, device=device)
     fn = lambda: decoder.decode_rans_groups(ctx, d_f, d_b, len(sec.section) - 512, sec.n_groups, 32, d_o, stream)  # noqa: E731
-    t, _ = time_steps(fn, steps, 3, stream, flush, ctx)
+    t, _ = time_steps(fn, steps, 3, stream, flush)
     ok = bool(np.array_equal(d_o.cpu().numpy(), sec.symbols))
     alg = len(sec.section) + sec.symbols.size
     out["rans_2^26"] = {

@@ -75,15 +75,18 @@ ScratchLayout scratch_layout(const gst_header &h) {
 
 size_t offsets_page_bytes(int n) { return align_up(size_t(n) * 8 * 4, 512); }
 
-struct Slot {
-  uint8_t *scratch = nullptr;
-  size_t scratch_cap = 0;
-  uint8_t *plan_d = nullptr;
-  size_t plan_cap = 0;
-  uint8_t *plan_h = nullptr;  // pinned
-  size_t plan_h_cap = 0;
-  cudaEvent_t plan_copied = nullptr;  // the pinned plan may be rewritten once this fires
-  cudaEvent_t done = nullptr;         // scratch and plan_d are free once this fires
+// Each decode call uploads its plan from one of kPlanRing pinned host buffers
+// into the matching device buffer, so the host can prepare up to kPlanRing
+// calls ahead of the GPU before it waits.
+constexpr int kPlanRing = 8;
+struct PlanBuf {
+  uint8_t *d = nullptr;  // device copy read by the kernels
+  size_t d_cap = 0;
+  uint8_t *h = nullptr;  // pinned host staging
+  size_t h_cap = 0;
+  cudaEvent_t copied = nullptr;  // the pinned staging may be rewritten once this fires
+  cudaEvent_t done = nullptr;    // the device copy may be rewritten once this fires
+  cudaStream_t stream = nullptr;
   bool used = false;
 };
 
@@ -92,8 +95,17 @@ struct Slot {
 struct gst_ctx {
   int device = 0;
   std::mutex mu;
-  Slot slot;
+  // Scratch for decoded symbols and index prefixes, shared by all calls;
+  // calls on different streams are ordered through scratch_done.
+  uint8_t *scratch = nullptr;
+  size_t scratch_cap = 0;
   bool preallocated = false;
+  cudaEvent_t scratch_done = nullptr;
+  cudaStream_t scratch_stream = nullptr;
+  bool scratch_used = false;
+  PlanBuf plans[kPlanRing];
+  int next_plan = 0;
+  uint32_t *status_d = nullptr;  // device error bits of the calls since the last status read
   cudaStream_t own_stream = nullptr;
   // Staging for the host-buffer path (gst_decompress_dxt).
   uint8_t *cmp_d = nullptr;
@@ -155,63 +167,109 @@ bool capturing(cudaStream_t s) {
   return st != cudaStreamCaptureStatusNone;
 }
 
-// Builds the plan for n images whose compressed data sit in the reference's
-// layout at d_cmp, then launches.  hdrs have passed check_header.
-gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8_t *d_cmp, uint8_t *d_out,
-                        cudaStream_t stream) {
-  Slot &sl = ctx->slot;
-  const bool cap = capturing(stream);
-  // Per-image scratch and plan sizes.
-  std::vector<ScratchLayout> lay(n);
-  size_t scratch_need = 0;
-  uint32_t n_rans = 0, n_tiles = 0;
+// Takes the next plan buffer of the ring with room for `bytes`; on return
+// its pinned staging may be written and the device copy may be overwritten by
+// work enqueued on `stream`.
+gst_status acquire_plan(gst_ctx *ctx, size_t bytes, cudaStream_t stream, bool cap, PlanBuf **out) {
+  PlanBuf &pb = ctx->plans[ctx->next_plan];
+  ctx->next_plan = (ctx->next_plan + 1) % kPlanRing;
+  if (pb.used && !cap) {
+    cudaEventSynchronize(pb.copied);
+    if (pb.stream != stream) cudaStreamWaitEvent(stream, pb.done, 0);
+  }
+  if (pb.d_cap < bytes || pb.h_cap < bytes) {
+    if (cap) return GST_E_ARG;  // buffers cannot be reallocated during stream capture
+    if (pb.used) cudaEventSynchronize(pb.done);
+    gst_status st = grow_device(&pb.d, &pb.d_cap, bytes);
+    if (st != GST_OK) return st;
+    st = grow_pinned(&pb.h, &pb.h_cap, bytes);
+    if (st != GST_OK) return st;
+  }
+  *out = &pb;
+  return GST_OK;
+}
+
+// Makes ctx->scratch at least `bytes` and orders its use on `stream` after
+// the previous call that used it.
+gst_status acquire_scratch(gst_ctx *ctx, size_t bytes, cudaStream_t stream, bool cap) {
+  if (ctx->scratch_used && !cap && ctx->scratch_stream != stream) cudaStreamWaitEvent(stream, ctx->scratch_done, 0);
+  if (ctx->scratch_cap >= bytes) return GST_OK;
+  if (ctx->preallocated) return GST_E_OOM;
+  if (cap) return GST_E_ARG;
+  if (ctx->scratch_used) cudaEventSynchronize(ctx->scratch_done);
+  return grow_device(&ctx->scratch, &ctx->scratch_cap, bytes);
+}
+
+// Uploads the plan staged in pb->h and launches the kernels on it.
+gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, size_t off_images, size_t off_rans,
+                             size_t off_tiles, size_t off_counters, uint32_t n_rans, uint32_t n_tiles,
+                             const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, cudaStream_t stream,
+                             bool cap) {
+  cudaError_t e = cudaMemcpyAsync(pb->d, pb->h, plan_bytes, cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (!cap) cudaEventRecord(pb->copied, stream);
+  GstPlanView view;
+  view.err = ctx->status_d;
+  view.images = reinterpret_cast<const GstImageDesc *>(pb->d + off_images);
+  view.rans = reinterpret_cast<const GstRansItem *>(pb->d + off_rans);
+  view.tiles = n_tiles ? reinterpret_cast<const GstTileItem *>(pb->d + off_tiles) : nullptr;
+  view.counters = reinterpret_cast<uint32_t *>(pb->d + off_counters);
+  view.n_rans = n_rans;
+  view.n_tiles = n_tiles;
+  cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
+  e = launch_decode(d_cmp, d_scratch, d_out, view, stream, &ctx->last_launches, ev);
+  ctx->timed_kernels = ev ? ctx->last_launches : 0;
+  if (e != cudaSuccess) return cuda_status(e);
+  if (!cap) {
+    cudaEventRecord(pb->done, stream);
+    pb->stream = stream;
+    pb->used = true;
+  }
+  return GST_OK;
+}
+
+// Where everything of a plan for these headers goes.
+struct PlanLayout {
+  size_t off_images, off_rans, off_tiles, off_counters, bytes;
+  uint32_t n_rans, n_tiles;
+  size_t scratch_bytes;
+  std::vector<ScratchLayout> lay;
+};
+
+PlanLayout plan_layout(const gst_header *hdrs, int n) {
+  PlanLayout L;
+  L.lay.resize(n);
+  L.scratch_bytes = 0;
+  L.n_rans = L.n_tiles = 0;
   for (int i = 0; i < n; ++i) {
-    lay[i] = scratch_layout(hdrs[i]);
-    scratch_need += lay[i].total;
+    L.lay[i] = scratch_layout(hdrs[i]);
+    L.scratch_bytes += L.lay[i].total;
     const uint64_t B = image_blocks(hdrs[i]);
     const uint64_t groups[4] = {2 * B / kSymsPerGroup, 4 * B / kSymsPerGroup, hdrs[i].palette_bytes / kSymsPerGroup,
                                 B / kSymsPerGroup};
-    for (uint64_t G : groups) n_rans += uint32_t((G + kGroupsPerRansCta - 1) / kGroupsPerRansCta);
-    n_tiles += uint32_t(B / 1024);
+    for (uint64_t G : groups) L.n_rans += uint32_t((G + kGroupsPerRansCta - 1) / kGroupsPerRansCta);
+    L.n_tiles += uint32_t(B / 1024);
   }
-  const size_t off_images = align_up(sizeof(GstPlanHead), 128);
-  const size_t off_rans = off_images + sizeof(GstImageDesc) * n;
-  const size_t off_tiles = align_up(off_rans + sizeof(GstRansItem) * n_rans, 16);
-  const size_t off_counters = align_up(off_tiles + sizeof(GstTileItem) * n_tiles, 16);
-  const size_t plan_bytes = align_up(off_counters + 4 * size_t(n), 16);
+  L.off_images = align_up(sizeof(GstPlanHead), 128);
+  L.off_rans = L.off_images + sizeof(GstImageDesc) * n;
+  L.off_tiles = align_up(L.off_rans + sizeof(GstRansItem) * L.n_rans, 16);
+  L.off_counters = align_up(L.off_tiles + sizeof(GstTileItem) * L.n_tiles, 16);
+  L.bytes = align_up(L.off_counters + 4 * size_t(n), 16);
+  return L;
+}
 
-  // The previous call may still be using this slot's buffers: wait on the
-  // device for its completion, and on the host for its plan upload.
-  if (sl.used && !cap) {
-    cudaEventSynchronize(sl.plan_copied);
-    cudaStreamWaitEvent(stream, sl.done, 0);
-  }
-  if (sl.scratch_cap < scratch_need || sl.plan_cap < plan_bytes) {
-    if (ctx->preallocated && sl.scratch_cap < scratch_need) return GST_E_OOM;
-    if (cap) return GST_E_ARG;  // buffers cannot be reallocated during stream capture
-    if (sl.used) cudaEventSynchronize(sl.done);
-    gst_status st = grow_device(&sl.scratch, &sl.scratch_cap, scratch_need);
-    if (st != GST_OK) return st;
-    st = grow_device(&sl.plan_d, &sl.plan_cap, plan_bytes);
-    if (st != GST_OK) return st;
-  }
-  if (sl.plan_h_cap < plan_bytes) {
-    if (cap) return GST_E_ARG;
-    gst_status st = grow_pinned(&sl.plan_h, &sl.plan_h_cap, plan_bytes);
-    if (st != GST_OK) return st;
-  }
-
-  uint8_t *ph = sl.plan_h;
-  memset(ph, 0, plan_bytes);
+// Writes the plan (L.bytes) for n images whose compressed data sit in the
+// reference's layout: codec/decoder.cpp:132-149 and demo/photos_sf.cpp:753-791
+// (offsets page, then 4n frequency tables, then each image's four sections).
+void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph) {
+  memset(ph, 0, L.bytes);
   GstPlanHead *head = reinterpret_cast<GstPlanHead *>(ph);
   head->n_images = uint32_t(n);
-  head->n_rans = n_rans;
-  head->n_tiles = n_tiles;
-  GstImageDesc *imgs = reinterpret_cast<GstImageDesc *>(ph + off_images);
-  GstRansItem *rans = reinterpret_cast<GstRansItem *>(ph + off_rans);
-  GstTileItem *tiles = reinterpret_cast<GstTileItem *>(ph + off_tiles);
-  // codec/decoder.cpp:132-149 and demo/photos_sf.cpp:753-791: offsets page,
-  // then 4n frequency tables, then each image's four sections.
+  head->n_rans = L.n_rans;
+  head->n_tiles = L.n_tiles;
+  GstImageDesc *imgs = reinterpret_cast<GstImageDesc *>(ph + L.off_images);
+  GstRansItem *rans = reinterpret_cast<GstRansItem *>(ph + L.off_rans);
+  GstTileItem *tiles = reinterpret_cast<GstTileItem *>(ph + L.off_tiles);
   const size_t page = offsets_page_bytes(n);
   uint64_t body = page + size_t(n) * 4 * kFreqTableBytes;
   uint64_t scratch_off = 0, out_off = 0;
@@ -222,9 +280,9 @@ gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8
     const uint32_t B = uint32_t(image_blocks(h));
     d.freq_off = page + size_t(i) * 4 * kFreqTableBytes;
     d.body_off = body;
-    d.sym_off = scratch_off + lay[i].sym;
-    d.chunk_off = scratch_off + lay[i].chunk;
-    d.gsum_off = scratch_off + lay[i].gsum;
+    d.sym_off = scratch_off + L.lay[i].sym;
+    d.chunk_off = scratch_off + L.lay[i].chunk;
+    d.gsum_off = scratch_off + L.lay[i].gsum;
     d.out_off = out_off;
     const uint32_t lens[4] = {h.y_cmp_sz, h.chroma_cmp_sz, h.palette_sz, h.indices_sz};
     const uint32_t syms[4] = {2 * B, 4 * B, h.palette_bytes, B};
@@ -246,46 +304,76 @@ gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8
     d.tiles_x = d.bx / kWaveletDim;
     for (uint32_t t = 0; t < B / 1024; ++t) tiles[ti++] = {uint32_t(i), t};
     body += section_bytes(h);
-    scratch_off += lay[i].total;
+    scratch_off += L.lay[i].total;
     out_off += 8ull * B;
   }
+}
 
-  cudaError_t e = cudaMemcpyAsync(sl.plan_d, ph, plan_bytes, cudaMemcpyHostToDevice, stream);
-  if (e != cudaSuccess) return cuda_status(e);
-  if (!cap) cudaEventRecord(sl.plan_copied, stream);
+GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) {
   GstPlanView view;
-  view.head = reinterpret_cast<GstPlanHead *>(sl.plan_d);
-  view.images = reinterpret_cast<const GstImageDesc *>(sl.plan_d + off_images);
-  view.rans = reinterpret_cast<const GstRansItem *>(sl.plan_d + off_rans);
-  view.tiles = reinterpret_cast<const GstTileItem *>(sl.plan_d + off_tiles);
-  view.counters = reinterpret_cast<uint32_t *>(sl.plan_d + off_counters);
-  view.n_rans = n_rans;
-  view.n_tiles = n_tiles;
-  cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
-  e = launch_decode(d_cmp, sl.scratch, d_out, view, stream, &ctx->last_launches, ev);
-  ctx->timed_kernels = ev ? ctx->last_launches : 0;
-  if (e != cudaSuccess) return cuda_status(e);
-  if (!cap) cudaEventRecord(sl.done, stream);
-  sl.used = true;
+  view.err = status_d;
+  view.images = reinterpret_cast<const GstImageDesc *>(plan_d + L.off_images);
+  view.rans = reinterpret_cast<const GstRansItem *>(plan_d + L.off_rans);
+  view.tiles = L.n_tiles ? reinterpret_cast<const GstTileItem *>(plan_d + L.off_tiles) : nullptr;
+  view.counters = reinterpret_cast<uint32_t *>(plan_d + L.off_counters);
+  view.n_rans = L.n_rans;
+  view.n_tiles = L.n_tiles;
+  return view;
+}
+
+// Builds the plan for n images whose compressed data sit in the reference's
+// layout at d_cmp, uploads it through the plan ring and launches.  hdrs have
+// passed check_header.
+gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8_t *d_cmp, uint8_t *d_out,
+                        cudaStream_t stream) {
+  const bool cap = capturing(stream);
+  const PlanLayout L = plan_layout(hdrs, n);
+  gst_status st = acquire_scratch(ctx, L.scratch_bytes, stream, cap);
+  if (st != GST_OK) return st;
+  PlanBuf *pb = nullptr;
+  st = acquire_plan(ctx, L.bytes, stream, cap, &pb);
+  if (st != GST_OK) return st;
+  write_plan(L, hdrs, n, pb->h);
+  st = upload_and_launch(ctx, pb, L.bytes, L.off_images, L.off_rans, L.off_tiles, L.off_counters, L.n_rans, L.n_tiles,
+                         d_cmp, ctx->scratch, d_out, stream, cap);
+  if (st != GST_OK) return st;
+  if (!cap) {
+    cudaEventRecord(ctx->scratch_done, stream);
+    ctx->scratch_stream = stream;
+    ctx->scratch_used = true;
+  }
   return GST_OK;
 }
 
 gst_status read_device_status(gst_ctx *ctx, cudaStream_t stream) {
   cudaError_t e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return cuda_status(e);
-  if (!ctx->slot.used) return GST_OK;
-  GstPlanHead head;
-  e = cudaMemcpy(&head, ctx->slot.plan_d, sizeof(head), cudaMemcpyDeviceToHost);
+  uint32_t bits = 0;
+  e = cudaMemcpy(&bits, ctx->status_d, sizeof(bits), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_status(e);
-  if (head.err) {
-    const uint32_t zero = 0;
-    cudaMemcpy(ctx->slot.plan_d + offsetof(GstPlanHead, err), &zero, 4, cudaMemcpyHostToDevice);
+  if (bits) {
+    e = cudaMemset(ctx->status_d, 0, sizeof(uint32_t));
+    if (e != cudaSuccess) return cuda_status(e);
     return GST_E_FORMAT;
   }
   return GST_OK;
 }
 
 }  // namespace
+
+// A resident batch: its plan is uploaded once and it owns its scratch, so a
+// launch enqueues kernels only (and can be captured in a CUDA graph).
+struct gst_batch {
+  gst_ctx *ctx = nullptr;
+  PlanLayout layout;
+  size_t compressed_bytes = 0;
+  size_t out_bytes = 0;
+  uint8_t *plan_d = nullptr;
+  uint8_t *scratch = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  const void *graph_cmp = nullptr;
+  void *graph_out = nullptr;
+};
 
 extern "C" {
 
@@ -311,9 +399,15 @@ gst_status gst_init(int device, gst_ctx **out) {
   if (e != cudaSuccess) return cuda_status(e);
   gst_ctx *ctx = new gst_ctx();
   ctx->device = device;
-  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->slot.plan_copied, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&ctx->slot.done, cudaEventDisableTiming) != cudaSuccess) {
+  bool ok = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&ctx->scratch_done, cudaEventDisableTiming) == cudaSuccess &&
+            cudaMalloc(reinterpret_cast<void **>(&ctx->status_d), sizeof(uint32_t)) == cudaSuccess &&
+            cudaMemset(ctx->status_d, 0, sizeof(uint32_t)) == cudaSuccess;
+  for (auto &pb : ctx->plans) {
+    ok = ok && cudaEventCreateWithFlags(&pb.copied, cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&pb.done, cudaEventDisableTiming) == cudaSuccess;
+  }
+  if (!ok) {
     gst_destroy(ctx);
     return GST_E_CUDA;
   }
@@ -324,17 +418,20 @@ gst_status gst_init(int device, gst_ctx **out) {
 void gst_destroy(gst_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
-  if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
-  if (ctx->slot.used) cudaEventSynchronize(ctx->slot.done);
-  cudaFree(ctx->slot.scratch);
-  cudaFree(ctx->slot.plan_d);
-  cudaFreeHost(ctx->slot.plan_h);
+  cudaDeviceSynchronize();
+  cudaFree(ctx->scratch);
+  cudaFree(ctx->status_d);
+  for (auto &pb : ctx->plans) {
+    cudaFree(pb.d);
+    cudaFreeHost(pb.h);
+    if (pb.copied) cudaEventDestroy(pb.copied);
+    if (pb.done) cudaEventDestroy(pb.done);
+  }
   cudaFree(ctx->cmp_d);
   cudaFree(ctx->out_d);
   cudaFreeHost(ctx->cmp_h);
   cudaFreeHost(ctx->out_h);
-  if (ctx->slot.plan_copied) cudaEventDestroy(ctx->slot.plan_copied);
-  if (ctx->slot.done) cudaEventDestroy(ctx->slot.done);
+  if (ctx->scratch_done) cudaEventDestroy(ctx->scratch_done);
   for (auto &e : ctx->ev)
     if (e) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -389,14 +486,17 @@ gst_status gst_preallocate(gst_ctx *ctx, size_t bytes) {
   if (!ctx) return GST_E_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   cudaSetDevice(ctx->device);
-  Slot &sl = ctx->slot;
-  if (sl.used) cudaEventSynchronize(sl.done);
-  if (sl.scratch) cudaFree(sl.scratch);
-  sl.scratch = nullptr;
-  sl.scratch_cap = 0;
-  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&sl.scratch), std::max<size_t>(bytes, 256));
-  if (e != cudaSuccess) return cuda_status(e);
-  sl.scratch_cap = std::max<size_t>(bytes, 256);
+  if (ctx->scratch_used) cudaEventSynchronize(ctx->scratch_done);
+  cudaFree(ctx->scratch);
+  ctx->scratch = nullptr;
+  ctx->scratch_cap = 0;
+  const size_t sz = std::max<size_t>(bytes, 256);
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&ctx->scratch), sz);
+  if (e != cudaSuccess) {
+    ctx->scratch = nullptr;
+    return cuda_status(e);
+  }
+  ctx->scratch_cap = sz;
   ctx->preallocated = true;
   return GST_OK;
 }
@@ -405,11 +505,10 @@ gst_status gst_free_decompressor(gst_ctx *ctx) {
   if (!ctx) return GST_E_ARG;
   std::lock_guard<std::mutex> lock(ctx->mu);
   cudaSetDevice(ctx->device);
-  Slot &sl = ctx->slot;
-  if (sl.used) cudaEventSynchronize(sl.done);
-  cudaFree(sl.scratch);
-  sl.scratch = nullptr;
-  sl.scratch_cap = 0;
+  if (ctx->scratch_used) cudaEventSynchronize(ctx->scratch_done);
+  cudaFree(ctx->scratch);
+  ctx->scratch = nullptr;
+  ctx->scratch_cap = 0;
   ctx->preallocated = false;
   return GST_OK;
 }
@@ -516,7 +615,6 @@ gst_status gst_decode_rans_groups(gst_ctx *ctx, const void *d_freqs, const void 
   if (uint64_t(n_groups) * 4 > body_bytes) return GST_E_FORMAT;
   std::lock_guard<std::mutex> lock(ctx->mu);
   cudaSetDevice(ctx->device);
-  Slot &sl = ctx->slot;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const bool cap = capturing(st);
   const uint32_t n_rans = (n_groups + kGroupsPerRansCta - 1) / kGroupsPerRansCta;
@@ -524,22 +622,10 @@ gst_status gst_decode_rans_groups(gst_ctx *ctx, const void *d_freqs, const void 
   const size_t off_rans = off_images + sizeof(GstImageDesc);
   const size_t off_counters = align_up(off_rans + sizeof(GstRansItem) * n_rans, 16);
   const size_t plan_bytes = align_up(off_counters + 4, 16);
-  if (sl.used && !cap) {
-    cudaEventSynchronize(sl.plan_copied);
-    cudaStreamWaitEvent(st, sl.done, 0);
-  }
-  if (sl.plan_cap < plan_bytes) {
-    if (cap) return GST_E_ARG;
-    if (sl.used) cudaEventSynchronize(sl.done);
-    gst_status s2 = grow_device(&sl.plan_d, &sl.plan_cap, plan_bytes);
-    if (s2 != GST_OK) return s2;
-  }
-  if (sl.plan_h_cap < plan_bytes) {
-    if (cap) return GST_E_ARG;
-    gst_status s2 = grow_pinned(&sl.plan_h, &sl.plan_h_cap, plan_bytes);
-    if (s2 != GST_OK) return s2;
-  }
-  uint8_t *ph = sl.plan_h;
+  PlanBuf *pb = nullptr;
+  gst_status s2 = acquire_plan(ctx, plan_bytes, st, cap, &pb);
+  if (s2 != GST_OK) return s2;
+  uint8_t *ph = pb->h;
   memset(ph, 0, plan_bytes);
   GstPlanHead *head = reinterpret_cast<GstPlanHead *>(ph);
   head->n_images = 1;
@@ -554,24 +640,102 @@ gst_status gst_decode_rans_groups(gst_ctx *ctx, const void *d_freqs, const void 
   GstRansItem *rans = reinterpret_cast<GstRansItem *>(ph + off_rans);
   for (uint32_t g = 0, r = 0; g < n_groups; g += kGroupsPerRansCta, ++r)
     rans[r] = {0u, 0u, g, uint16_t(std::min(kGroupsPerRansCta, n_groups - g)), uint16_t(streams_per_group)};
-  cudaError_t e = cudaMemcpyAsync(sl.plan_d, ph, plan_bytes, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_status(e);
-  if (!cap) cudaEventRecord(sl.plan_copied, st);
-  GstPlanView view;
-  view.head = reinterpret_cast<GstPlanHead *>(sl.plan_d);
-  view.images = reinterpret_cast<const GstImageDesc *>(sl.plan_d + off_images);
-  view.rans = reinterpret_cast<const GstRansItem *>(sl.plan_d + off_rans);
-  view.tiles = nullptr;
-  view.counters = reinterpret_cast<uint32_t *>(sl.plan_d + off_counters);
-  view.n_rans = n_rans;
-  view.n_tiles = 0;
-  cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
-  e = launch_decode(nullptr, nullptr, nullptr, view, st, &ctx->last_launches, ev);
-  ctx->timed_kernels = ev ? ctx->last_launches : 0;
-  if (e != cudaSuccess) return cuda_status(e);
-  if (!cap) cudaEventRecord(sl.done, st);
-  sl.used = true;
+  return upload_and_launch(ctx, pb, plan_bytes, off_images, off_rans, 0, off_counters, n_rans, 0, nullptr, nullptr,
+                           nullptr, st, cap);
+}
+
+gst_status gst_batch_create(gst_ctx *ctx, const gst_header *hdrs, int n, gst_batch **out) {
+  if (!ctx || !hdrs || n <= 0 || !out) return GST_E_ARG;
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    gst_status st = check_header(hdrs[i]);
+    if (st != GST_OK) return st;
+  }
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  gst_batch *b = new gst_batch();
+  b->ctx = ctx;
+  b->layout = plan_layout(hdrs, n);
+  b->compressed_bytes = gst_batch_layout_bytes(hdrs, n);
+  for (int i = 0; i < n; ++i) b->out_bytes += size_t(image_blocks(hdrs[i])) * 8;
+  std::vector<uint8_t> plan(b->layout.bytes);
+  write_plan(b->layout, hdrs, n, plan.data());
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&b->plan_d), b->layout.bytes);
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(&b->scratch), std::max<size_t>(b->layout.scratch_bytes, 256));
+  if (e == cudaSuccess) e = cudaMemcpy(b->plan_d, plan.data(), b->layout.bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    gst_batch_destroy(b);
+    return cuda_status(e);
+  }
+  *out = b;
   return GST_OK;
+}
+
+void gst_batch_destroy(gst_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->ctx->device);
+  cudaDeviceSynchronize();
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->plan_d);
+  cudaFree(b->scratch);
+  delete b;
+}
+
+size_t gst_batch_device_bytes(const gst_batch *b) {
+  return b ? b->layout.bytes + b->layout.scratch_bytes : 0;
+}
+
+gst_status gst_batch_launch(gst_batch *b, const void *d_cmp, void *d_out, void *stream) {
+  if (!b || !d_cmp || !d_out) return GST_E_ARG;
+  if ((reinterpret_cast<uintptr_t>(d_cmp) & 15) || (reinterpret_cast<uintptr_t>(d_out) & 7)) return GST_E_ARG;
+  gst_ctx *ctx = b->ctx;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool cap = capturing(st);
+  cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
+  cudaError_t e = launch_decode(static_cast<const uint8_t *>(d_cmp), b->scratch, static_cast<uint8_t *>(d_out),
+                                plan_view(b->layout, b->plan_d, ctx->status_d), st, &ctx->last_launches, ev);
+  ctx->timed_kernels = ev ? ctx->last_launches : 0;
+  return cuda_status(e);
+}
+
+gst_status gst_batch_graph_launch(gst_batch *b, const void *d_cmp, void *d_out, void *stream) {
+  if (!b || !d_cmp || !d_out) return GST_E_ARG;
+  gst_ctx *ctx = b->ctx;
+  cudaSetDevice(ctx->device);
+  if (!b->graph || b->graph_cmp != d_cmp || b->graph_out != d_out) {
+    // Capture the launch sequence once per (input, output) pair.
+    cudaStream_t cs = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e);
+    {
+      std::lock_guard<std::mutex> lock(ctx->mu);
+      launch_decode(nullptr, nullptr, nullptr, GstPlanView{}, nullptr, &ctx->last_launches, nullptr);  // configure attributes
+    }
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    gst_status st = GST_OK;
+    if (e == cudaSuccess) st = gst_batch_launch(b, d_cmp, d_out, cs);
+    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return cuda_status(e != cudaSuccess ? e : e2);
+    }
+    if (st != GST_OK) {
+      cudaGraphDestroy(g);
+      return st;
+    }
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_status(e);
+    b->graph_cmp = d_cmp;
+    b->graph_out = d_out;
+  }
+  return cuda_status(cudaGraphLaunch(b->graph, static_cast<cudaStream_t>(stream)));
 }
 
 gst_status gst_sync_status(gst_ctx *ctx, void *stream) {

@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(256) gst_rans_kernel(const uint8_t *__restrict
 
   const GstRansItem it = plan.rans[blockIdx.x];
   const GstImageDesc &im = plan.images[it.image];
-  uint32_t *err = &plan.head->err;
+  uint32_t *err = plan.err;
   const uint16_t *freqs = reinterpret_cast<const uint16_t *>(cmp + im.freq_off + kFreqTableBytes * it.section);
   const bool table_ok = build_decode_table(freqs, sm.tbl, sm.cum, sm.f, sm.wsum);
   if (!table_ok && threadIdx.x == 0) flag_error(err, kErrTable);
@@ -297,6 +297,9 @@ __global__ void __launch_bounds__(256) gst_rans_kernel(const uint8_t *__restrict
   last = __shfl_sync(0xFFFFFFFFu, last, 31);
   if (!last) return;
   __threadfence();
+  // Every index group of this image is done: re-arm its counter so a resident
+  // plan can be launched again without a re-upload.
+  if (lane == 0) plan.counters[it.image] = 0;
   // Exclusive prefix of the G group sums, one warp, 32 at a time.
   int32_t carry = 0;
   for (uint32_t base = 0; base < G; base += 32) {
@@ -373,55 +376,79 @@ __global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict
   const size_t B = static_cast<size_t>(im.bx) * im.by;
   const uint32_t tx = it.tile % im.tiles_x, ty = it.tile / im.tiles_x;
   const uint8_t *sym = scratch + im.sym_off;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
 
-  // The tile's 1024 coefficients of plane p are the tile-th 1024-byte run of
-  // the plane (inverse_wavelet.cl:79-104); planes Y1 Y2 Co1 Cg1 Co2 Cg2 are
-  // consecutive B-byte runs of the decoded Y and chroma sections.
-  for (int i = threadIdx.x; i < 6 * 256; i += 256) {
-    const int p = i >> 8, wi = i & 255;
-    const uint32_t v = __ldg(reinterpret_cast<const uint32_t *>(sym + p * B + static_cast<size_t>(it.tile) * 1024) + wi);
-    int32_t *dst = pl + p * kPlaneWords + (wi >> 3) * kPlanePitch + (wi & 7) * 4;
-    dst[0] = static_cast<int32_t>(v & 0xFFu) - 128;
-    dst[1] = static_cast<int32_t>((v >> 8) & 0xFFu) - 128;
-    dst[2] = static_cast<int32_t>((v >> 16) & 0xFFu) - 128;
-    dst[3] = static_cast<int32_t>(v >> 24) - 128;
+  // 1. The tile's 1024 coefficients of plane p are the tile-th 1024-byte run of
+  //    the plane (inverse_wavelet.cl:79-104); planes Y1 Y2 Co1 Cg1 Co2 Cg2 are
+  //    consecutive B-byte runs of the decoded Y and chroma sections.  384
+  //    16-byte chunks, one or two per thread.
+  const uint8_t *tile_base = sym + static_cast<size_t>(it.tile) * 1024;
+  const uint4 c0 = __ldg(reinterpret_cast<const uint4 *>(tile_base + (t >> 6) * B) + (t & 63));
+  uint4 c1 = make_uint4(0, 0, 0, 0);
+  if (t < 128) c1 = __ldg(reinterpret_cast<const uint4 *>(tile_base + ((t + 256) >> 6) * B) + ((t + 256) & 63));
+
+  // 2. Palette indices of the four rows this thread assembles (rows warp+8i,
+  //    column lane): loads first, so that they overlap the wavelet.
+  const int32_t *chunk_pref = reinterpret_cast<const int32_t *>(scratch + im.chunk_off);
+  const int32_t *gpref = reinterpret_cast<const int32_t *>(scratch + im.gsum_off) + im.sec_groups[3];
+  const uint8_t *deltas = sym + im.sec_out[3];
+  uint32_t d[4], base[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const uint32_t p0 = (ty * 32 + warp + 8 * i) * im.bx + tx * 32;  // first block of the row segment
+    d[i] = static_cast<uint32_t>(__ldg(deltas + p0 + lane)) - 128u;
+    base[i] = static_cast<uint32_t>(__ldg(gpref + (p0 >> 13))) + static_cast<uint32_t>(__ldg(chunk_pref + (p0 >> 5)));
+  }
+
+  // 3. Coefficients to int32 (byte - 128), rows of pitch kPlanePitch.
+  auto unpack = [&](uint4 c, int chunk) {
+    const int p = chunk >> 6, q = chunk & 63;          // plane, 16-byte chunk in the plane's block
+    int32_t *dst = pl + p * kPlaneWords + (q >> 1) * kPlanePitch + (q & 1) * 16;
+    const uint32_t w[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int k = 0; k < 16; ++k) dst[k] = static_cast<int32_t>((w[k >> 2] >> (8 * (k & 3))) & 0xFFu) - 128;
+  };
+  unpack(c0, t);
+  if (t < 128) unpack(c1, t + 256);
+
+  // 4. Finish the index prefix sums (warp scans) and start the palette gathers.
+  const uint32_t *pal = reinterpret_cast<const uint32_t *>(sym + im.sec_out[2]);
+  uint32_t word[4];
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, d[i], o);
+      if (lane >= o) d[i] += n;
+    }
+    const uint32_t idx = base[i] + d[i];
+    word[i] = 0;
+    if (idx < im.palette_words) word[i] = __ldg(pal + idx);
+    else bad = true;
   }
   __syncthreads();
+
+  // 5. Five levels of the inverse 5/3 wavelet.
   inv53_level<2>(pl);
   inv53_level<4>(pl);
   inv53_level<8>(pl);
   inv53_level<16>(pl);
   inv53_level<32>(pl);
 
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int32_t *chunk_pref = reinterpret_cast<const int32_t *>(scratch + im.chunk_off);
-  const int32_t *gpref = reinterpret_cast<const int32_t *>(scratch + im.gsum_off) + im.sec_groups[3];
-  const uint8_t *deltas = sym + im.sec_out[3];
-  const uint32_t *pal = reinterpret_cast<const uint32_t *>(sym + im.sec_out[2]);
-  bool bad = false;
+  // 6. YCoCg667 -> RGB565 endpoints and whole 8-byte DXT1 blocks.
 #pragma unroll
-  for (int rr = 0; rr < 4; ++rr) {
-    const int r = warp + 8 * rr;
-    const uint32_t p0 = (ty * 32 + r) * im.bx + tx * 32;  // first block of this row segment
-    const uint32_t p = p0 + lane;
-    uint32_t d = static_cast<uint32_t>(__ldg(deltas + p)) - 128u;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, d, o);
-      if (lane >= o) d += n;
-    }
-    const uint32_t idx = static_cast<uint32_t>(gpref[p0 >> 13]) + static_cast<uint32_t>(chunk_pref[p0 >> 5]) + d;
-    uint32_t word = 0;
-    if (idx < im.palette_words) word = __ldg(pal + idx);
-    else bad = true;
+  for (int i = 0; i < 4; ++i) {
+    const int r = warp + 8 * i;
+    const uint32_t p = (ty * 32 + r) * im.bx + tx * 32 + lane;
     const int32_t *row = pl + r * kPlanePitch + lane;
     const int y1 = static_cast<int8_t>(row[0]), y2 = static_cast<int8_t>(row[kPlaneWords]);
     const int co1 = static_cast<int8_t>(row[2 * kPlaneWords]), cg1 = static_cast<int8_t>(row[3 * kPlaneWords]);
     const int co2 = static_cast<int8_t>(row[4 * kPlaneWords]), cg2 = static_cast<int8_t>(row[5 * kPlaneWords]);
     const uint32_t ep1 = ycocg_to_565(y1, co1, cg1), ep2 = ycocg_to_565(y2, co2, cg2);
-    *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) = make_uint2(ep1 | (ep2 << 16), word);
+    *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) = make_uint2(ep1 | (ep2 << 16), word[i]);
   }
-  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(&plan.head->err, kErrPalette);
+  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(plan.err, kErrPalette);
 }
 
 // Enqueues the decode of one plan.  With `ev` non-null, records ev[0] before
@@ -429,15 +456,15 @@ __global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict
 cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, const GstPlanView &plan,
                           cudaStream_t stream, int *launches, cudaEvent_t *ev) {
   *launches = 0;
+  static bool configured = false;  // per process; the attribute applies to every device context
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(gst_rans_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(kRansSmemBytes));
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
   if (ev) cudaEventRecord(ev[0], stream);
   if (plan.n_rans) {
-    static bool configured = false;  // per process; the attribute applies to every device context
-    if (!configured) {
-      cudaError_t e = cudaFuncSetAttribute(gst_rans_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           static_cast<int>(kRansSmemBytes));
-      if (e != cudaSuccess) return e;
-      configured = true;
-    }
     gst_rans_kernel<<<plan.n_rans, 256, kRansSmemBytes, stream>>>(d_cmp, d_scratch, plan);
     ++*launches;
     if (ev) cudaEventRecord(ev[*launches], stream);

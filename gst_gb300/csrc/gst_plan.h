@@ -10,9 +10,8 @@
 //   * the rANS work list: one item per (image, section, run of <= 8 groups of
 //     32 x 256 symbols) -- a CTA of 8 warps, one warp per group;
 //   * the tile work list: one item per (image, 32x32-block wavelet tile).
-// The plan is copied to the device in one cudaMemcpyAsync; its head also
-// carries the device-side error word and per-image counters, so the copy
-// resets them for every call.
+// The plan is copied to the device in one cudaMemcpyAsync; it also carries the
+// per-image counters, so the copy resets them for every call.
 #pragma once
 
 #include <stdint.h>
@@ -28,7 +27,7 @@ constexpr uint32_t kRansL = 1u << 15;         // k * M, k = 2^4      ans/ans_ocl
 constexpr uint32_t kFreqTableBytes = 512;
 constexpr uint32_t kWaveletDim = 32;          //                    codec/codec_base.h:22
 
-// Device error bits (GstPlanHead::err).
+// Device error bits (GstPlanView::err).
 constexpr uint32_t kErrTable = 1u;       // a frequency table does not sum to 2048
 constexpr uint32_t kErrGroup = 2u;       // a group end offset is out of order or range
 constexpr uint32_t kErrStream = 4u;      // a renormalisation read left its group
@@ -68,12 +67,12 @@ struct alignas(16) GstPlanHead {
   uint32_t n_images;
   uint32_t n_rans;
   uint32_t n_tiles;
-  uint32_t err;
+  uint32_t reserved;
 };
 
 // Device-side view of an uploaded plan.
 struct GstPlanView {
-  GstPlanHead *head;
+  uint32_t *err;  // the context's device status word (error bits, OR-ed)
   const GstImageDesc *images;
   const GstRansItem *rans;
   const GstTileItem *tiles;

@@ -42,6 +42,8 @@ EXPORTED_SYMBOLS = (
     "gst_required_scratch", "gst_preallocate", "gst_free_decompressor",
     "gst_decompress_dxt", "gst_load_compressed_dxt", "gst_load_compressed_dxts",
     "gst_batch_layout_bytes", "gst_pack_batch", "gst_decode_rans_groups",
+    "gst_batch_create", "gst_batch_destroy", "gst_batch_device_bytes", "gst_batch_launch",
+    "gst_batch_graph_launch",
     "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times",
     "gst_status_string",
 )
@@ -113,6 +115,11 @@ def load_library() -> ctypes.CDLL:
         "gst_batch_layout_bytes": (S, [HP, I]),
         "gst_pack_batch": (I, [ctypes.POINTER(P), ctypes.POINTER(S), I, P, S]),
         "gst_decode_rans_groups": (I, [P, P, P, U32, U32, U32, P, P]),
+        "gst_batch_create": (I, [P, HP, I, ctypes.POINTER(P)]),
+        "gst_batch_destroy": (None, [P]),
+        "gst_batch_device_bytes": (S, [P]),
+        "gst_batch_launch": (I, [P, P, P, P]),
+        "gst_batch_graph_launch": (I, [P, P, P, P]),
         "gst_sync_status": (I, [P, P]),
         "gst_last_launch_count": (I, [P]),
         "gst_set_profiling": (I, [P, I]),
@@ -205,6 +212,38 @@ class GPUContext:
         names = (ctypes.c_char_p * 8)()
         n = load_library().gst_kernel_times(self.handle, ms, names, 8)
         return [(names[i].decode(), float(ms[i])) for i in range(n)]
+
+
+class ResidentBatch:
+    """A resident batch (gst_batch_*): plan uploaded once, own scratch; each
+    launch enqueues kernels only.  ``graph=True`` replays a captured CUDA graph."""
+
+    def __init__(self, ctx: GPUContext, hdrs: Sequence[GenTCHeader]):
+        arr = (GenTCHeader * len(hdrs))(*hdrs)
+        h = ctypes.c_void_p()
+        _check(load_library().gst_batch_create(ctx.handle, arr, len(hdrs), ctypes.byref(h)), "gst_batch_create")
+        self._h = h
+        self.ctx = ctx
+        self.hdrs = list(hdrs)
+
+    @property
+    def device_bytes(self) -> int:
+        return int(load_library().gst_batch_device_bytes(self._h))
+
+    def launch(self, cmp_data, output, stream=None, graph: bool = False) -> None:
+        fn = load_library().gst_batch_graph_launch if graph else load_library().gst_batch_launch
+        _check(fn(self._h, _ptr(cmp_data), _ptr(output), _stream(stream)), "gst_batch_launch")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            load_library().gst_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def parse_header(data) -> GenTCHeader:

@@ -102,6 +102,23 @@ gst_status gst_load_compressed_dxt(gst_ctx *ctx, const gst_header *hdr, const vo
 gst_status gst_load_compressed_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const void *d_cmp,
                                     void *d_out, void *stream);
 
+/* Resident batches (the serving and benchmark form of LoadCompressedDXTs):
+ * gst_batch_create builds the batch's work plan once, uploads it and reserves
+ * the batch's own scratch (gst_batch_device_bytes in total), so that
+ * gst_batch_launch enqueues only kernels -- no host work, no copies -- and may
+ * be captured in a CUDA graph; gst_batch_graph_launch captures it once per
+ * (d_cmp, d_out) pair and replays the graph.  Batches are independent of each
+ * other and of the context's own scratch, so different batches may run
+ * concurrently on different streams; one batch must not run concurrently with
+ * itself.  No counterpart in the reference, whose every call rebuilds its
+ * sub-buffers and re-enqueues its kernels (codec/decoder.cpp:98-428). */
+typedef struct gst_batch gst_batch;
+gst_status gst_batch_create(gst_ctx *ctx, const gst_header *hdrs, int n, gst_batch **batch);
+void gst_batch_destroy(gst_batch *batch);
+size_t gst_batch_device_bytes(const gst_batch *batch);
+gst_status gst_batch_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
+gst_status gst_batch_graph_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
+
 /* Size of the reference's device layout for these headers (offsets page,
  * frequency tables, sections), and a host-side packer that writes it from
  * n complete GST streams (gst[i] of len[i] bytes) into `dst`. */

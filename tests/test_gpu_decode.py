@@ -225,3 +225,23 @@ def test_stream_argument_and_launch_count(gpu_ctx):
     st, outs = batch_decode(gpu_ctx, [s, s], stream=side)
     assert st == 0 and np.array_equal(outs[0], outs[1])
     assert gpu_ctx.last_launch_count() == 2
+
+
+def test_resident_batch_launch_and_graph_replay(gpu_ctx):
+    # A resident batch launched directly and through its captured graph, twice
+    # each, gives the encoder's blocks every time (the plan re-arms itself).
+    imgs = [workloads.encode_image(w, h, 600 + i) for i, (w, h) in enumerate([(1024, 512), (512, 512), (2048, 1024)])]
+    hdrs, packed = decoder.pack_batch([im.stream for im in imgs])
+    want = np.concatenate([im.blocks for im in imgs])
+    d_cmp = torch.from_numpy(packed).cuda()
+    d_out = torch.zeros(sum(h.dxt_bytes for h in hdrs), dtype=torch.uint8, device="cuda")
+    b = decoder.ResidentBatch(gpu_ctx, hdrs)
+    assert b.device_bytes > 0
+    side = torch.cuda.Stream()
+    for graph in (False, False, True, True):
+        d_out.zero_()
+        torch.cuda.synchronize()
+        b.launch(d_cmp, d_out, side, graph=graph)
+        assert decoder.sync_status(gpu_ctx, side) == decoder.GST_OK
+        assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want), graph
+    b.close()

@@ -480,3 +480,312 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
 const char *kernel_name(int i) { return i == 0 ? "gst_rans_kernel" : "gst_tile_kernel"; }
 
 }  // namespace gst
+
+namespace gst {
+
+// ===========================================================================
+// One-image decode that allocates nothing: gst_load_compressed_dxt_static.
+//
+// Who needs it: callers that must not allocate device memory at decode time.
+// cudaMalloc and cudaFree can synchronise the whole device, which a render or
+// texture-streaming thread with a per-frame time budget cannot afford; neither
+// call may be made while the caller's stream is being captured into a CUDA
+// graph; and some engines hand out all device memory from their own fixed pools
+// and forbid anyone else to allocate.  Such callers cannot create a gst_ctx
+// (it allocates its scratch, plan buffers and events), so this entry point
+// needs no context: its scratch is g_static_scratch below, a file-scope device
+// array that is part of this library's image and is held by every GPU that
+// loads the library until the process exits.
+//
+// Limits and rules (also stated in include/gst_decoder.h):
+//  * kStaticScratchBytes (4 MiB) bounds the image: 256 + 7*B + palette_bytes
+//    + B/8 + 8*B/8192 bytes must fit (B = w*h/16); that is at most 2048x2048
+//    with a typical palette.  Larger images are rejected with GST_E_ARG before
+//    anything is enqueued.
+//  * Every call uses the same array and leaves its contents behind.  Each call
+//    clears, on its stream, the words that must start at zero (the device
+//    status word and the index-group counter); the rest is fully rewritten
+//    before it is read.  Calls whose work overlaps on the GPU (different
+//    streams without ordering between them, or several host threads) race on
+//    the array: serialise them, e.g. by using one stream.
+//  * The first call on each device looks up the array's device address
+//    (cudaGetSymbolAddress, with that device current) and sets the rANS
+//    kernel's shared-memory attribute; make that first call before any stream
+//    capture on that device.
+//  * It calls no cudaMalloc, cudaFree or other allocating routine.
+// No counterpart in the reference, whose decoder allocates its scratch per call
+// or from PreallocateDecompressor (codec/decoder.cpp:98-130, 478-485).
+constexpr size_t kStaticScratchBytes = size_t(4) << 20;
+constexpr size_t kStaticHeaderBytes = 256;  // [status word][index-group counter], then image scratch
+static __device__ __align__(256) uint8_t g_static_scratch[kStaticScratchBytes];
+
+// gst_rans_kernel for a single image whose descriptor arrives by value; the
+// work item is derived from blockIdx (ceil(G/8) CTAs per section, in section
+// order).  `base` is g_static_scratch: [status][counter] then the image scratch.
+__global__ void __launch_bounds__(256) gst_rans_static_kernel(const uint8_t *__restrict__ cmp, uint8_t *base,
+                                                              GstImageDesc im) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  RansSmem &sm = *reinterpret_cast<RansSmem *>(smem_raw);
+  uint32_t *err = reinterpret_cast<uint32_t *>(base);
+  uint32_t *counter = err + 1;
+  uint8_t *scratch = base + kStaticHeaderBytes;
+
+  uint32_t b = blockIdx.x, section = 0;
+  for (; section < 3; ++section) {
+    const uint32_t c = (im.sec_groups[section] + kGroupsPerRansCta - 1) / kGroupsPerRansCta;
+    if (b < c) break;
+    b -= c;
+  }
+  const uint32_t first = b * kGroupsPerRansCta;
+  const uint32_t ngroups = min(kGroupsPerRansCta, im.sec_groups[section] - first);
+
+  const uint16_t *freqs = reinterpret_cast<const uint16_t *>(cmp + im.freq_off + kFreqTableBytes * section);
+  const bool table_ok = build_decode_table(freqs, sm.tbl, sm.cum, sm.f, sm.wsum);
+  if (!table_ok && threadIdx.x == 0) flag_error(err, kErrTable);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (static_cast<uint32_t>(warp) >= ngroups) return;
+  const uint32_t g = first + warp;
+  const uint32_t G = im.sec_groups[section];
+  const uint32_t len = im.sec_len[section];
+  const uint8_t *sec = cmp + im.body_off + im.sec_in[section];
+  const uint32_t *ends = reinterpret_cast<const uint32_t *>(sec);
+  const uint32_t hi = ends[g];
+  const uint32_t lo = g == 0 ? 4u * G : ends[g - 1];
+  const bool group_ok = table_ok && (hi & 3u) == 0 && (lo & 3u) == 0 && hi <= len && lo <= len &&
+                        hi >= lo + 4u * kStreamsPerGroup;
+  const bool is_index = section == 3;
+  uint8_t *out = scratch + im.sym_off + im.sec_out[section] + static_cast<size_t>(g) * kSymsPerGroup +
+                 static_cast<size_t>(lane) * kSymsPerStream;
+
+  int32_t suf[8];
+  if (group_ok) {
+    const uint32_t top = hi - 4u * kStreamsPerGroup;
+    const bool fits = top - lo <= 2u * kStageWords;
+    bool bad;
+    if (is_index)
+      bad = fits ? decode_group<true, true>(sec, lo, top, sm.tbl, sm.stage[warp], lane, true, out, suf)
+                 : decode_group<true, false>(sec, lo, top, sm.tbl, sm.stage[warp], lane, true, out, suf);
+    else
+      bad = fits ? decode_group<false, true>(sec, lo, top, sm.tbl, sm.stage[warp], lane, true, out, suf)
+                 : decode_group<false, false>(sec, lo, top, sm.tbl, sm.stage[warp], lane, true, out, suf);
+    if (bad && lane == 0) flag_error(err, kErrStream);
+  } else if (lane == 0 && table_ok) {
+    flag_error(err, kErrGroup);
+  }
+  if (!is_index) return;
+
+  const int32_t T = group_ok ? suf[7] : 0;
+  int32_t incl = T;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+    if (lane >= d) incl += n;
+  }
+  if (group_ok) {
+    const int32_t lane_off = incl - T;
+    int32_t pre[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) pre[c] = lane_off + T - suf[7 - c];
+    int32_t *chunk = reinterpret_cast<int32_t *>(scratch + im.chunk_off) + static_cast<size_t>(g) * 256 + lane * 8;
+    reinterpret_cast<int4 *>(chunk)[0] = make_int4(pre[0], pre[1], pre[2], pre[3]);
+    reinterpret_cast<int4 *>(chunk)[1] = make_int4(pre[4], pre[5], pre[6], pre[7]);
+  }
+  int32_t *gsum = reinterpret_cast<int32_t *>(scratch + im.gsum_off);
+  uint32_t last = 0;
+  if (lane == 31) {
+    gsum[g] = incl;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == G - 1;
+  }
+  last = __shfl_sync(0xFFFFFFFFu, last, 31);
+  if (!last) return;
+  __threadfence();
+  int32_t carry = 0;
+  for (uint32_t i0 = 0; i0 < G; i0 += 32) {
+    const uint32_t i = i0 + lane;
+    const int32_t s = i < G ? __ldcg(gsum + i) : 0;
+    int32_t v = s;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int32_t n = __shfl_up_sync(0xFFFFFFFFu, v, d);
+      if (lane >= d) v += n;
+    }
+    if (i < G) gsum[G + i] = carry + v - s;
+    carry += __shfl_sync(0xFFFFFFFFu, v, 31);
+  }
+}
+
+// gst_tile_kernel for a single image whose descriptor arrives by value; the
+// tile is blockIdx.x.
+__global__ void __launch_bounds__(256) gst_tile_static_kernel(const uint8_t *base, uint8_t *__restrict__ out,
+                                                              GstImageDesc im) {
+  __shared__ int32_t pl[6 * kPlaneWords];
+  uint32_t *err = reinterpret_cast<uint32_t *>(const_cast<uint8_t *>(base));
+  const uint8_t *scratch = base + kStaticHeaderBytes;
+  const uint32_t tile = blockIdx.x;
+  const size_t B = static_cast<size_t>(im.bx) * im.by;
+  const uint32_t tx = tile % im.tiles_x, ty = tile / im.tiles_x;
+  const uint8_t *sym = scratch + im.sym_off;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+
+  const uint8_t *tile_base = sym + static_cast<size_t>(tile) * 1024;
+  const uint4 c0 = *(reinterpret_cast<const uint4 *>(tile_base + (t >> 6) * B) + (t & 63));
+  uint4 c1 = make_uint4(0, 0, 0, 0);
+  if (t < 128) c1 = *(reinterpret_cast<const uint4 *>(tile_base + ((t + 256) >> 6) * B) + ((t + 256) & 63));
+
+  const int32_t *chunk_pref = reinterpret_cast<const int32_t *>(scratch + im.chunk_off);
+  const int32_t *gpref = reinterpret_cast<const int32_t *>(scratch + im.gsum_off) + im.sec_groups[3];
+  const uint8_t *deltas = sym + im.sec_out[3];
+  uint32_t d[4], basev[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const uint32_t p0 = (ty * 32 + warp + 8 * i) * im.bx + tx * 32;
+    d[i] = static_cast<uint32_t>(deltas[p0 + lane]) - 128u;
+    basev[i] = static_cast<uint32_t>(gpref[p0 >> 13]) + static_cast<uint32_t>(chunk_pref[p0 >> 5]);
+  }
+  auto unpack = [&](uint4 c, int chunk) {
+    const int p = chunk >> 6, q = chunk & 63;
+    int32_t *dst = pl + p * kPlaneWords + (q >> 1) * kPlanePitch + (q & 1) * 16;
+    const uint32_t w[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int k = 0; k < 16; ++k) dst[k] = static_cast<int32_t>((w[k >> 2] >> (8 * (k & 3))) & 0xFFu) - 128;
+  };
+  unpack(c0, t);
+  if (t < 128) unpack(c1, t + 256);
+
+  const uint32_t *pal = reinterpret_cast<const uint32_t *>(sym + im.sec_out[2]);
+  uint32_t word[4];
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, d[i], o);
+      if (lane >= o) d[i] += n;
+    }
+    const uint32_t idx = basev[i] + d[i];
+    word[i] = 0;
+    if (idx < im.palette_words) word[i] = pal[idx];
+    else bad = true;
+  }
+  __syncthreads();
+  inv53_level<2>(pl);
+  inv53_level<4>(pl);
+  inv53_level<8>(pl);
+  inv53_level<16>(pl);
+  inv53_level<32>(pl);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = warp + 8 * i;
+    const uint32_t p = (ty * 32 + r) * im.bx + tx * 32 + lane;
+    const int32_t *row = pl + r * kPlanePitch + lane;
+    const int y1 = static_cast<int8_t>(row[0]), y2 = static_cast<int8_t>(row[kPlaneWords]);
+    const int co1 = static_cast<int8_t>(row[2 * kPlaneWords]), cg1 = static_cast<int8_t>(row[3 * kPlaneWords]);
+    const int co2 = static_cast<int8_t>(row[4 * kPlaneWords]), cg2 = static_cast<int8_t>(row[5 * kPlaneWords]);
+    const uint32_t ep1 = ycocg_to_565(y1, co1, cg1), ep2 = ycocg_to_565(y2, co2, cg2);
+    *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) = make_uint2(ep1 | (ep2 << 16), word[i]);
+  }
+  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(err, kErrPalette);
+}
+
+}  // namespace gst
+
+// Host side of the static-scratch decode.
+#include <mutex>
+
+#include "gst_decoder.h"
+
+namespace {
+
+constexpr int kMaxStaticDevices = 64;
+std::mutex g_static_mu;
+void *g_static_ptr[kMaxStaticDevices] = {};  // device address of g_static_scratch, per device
+
+// Once per device, with it current: the array's device address and the rANS
+// kernel's shared-memory attribute.  The array's name is only a host-side
+// stand-in; kernels must be given this address.
+gst_status static_setup(int device, uint8_t **base) {
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (device < 0 || device >= kMaxStaticDevices) return GST_E_ARG;
+  if (!g_static_ptr[device]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, gst::g_static_scratch);
+    if (e != cudaSuccess || !p) return GST_E_CUDA;
+    e = cudaFuncSetAttribute(gst::gst_rans_static_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(gst::kRansSmemBytes));
+    if (e != cudaSuccess) return GST_E_CUDA;
+    g_static_ptr[device] = p;
+  }
+  *base = static_cast<uint8_t *>(g_static_ptr[device]);
+  return GST_OK;
+}
+
+}  // namespace
+
+extern "C" gst_status gst_load_compressed_dxt_static(const gst_header *hdr, const void *d_cmp, void *d_out,
+                                                     void *stream, uint32_t *device_status) {
+  using namespace gst;
+  if (!hdr || !d_cmp || !d_out) return GST_E_ARG;
+  if ((reinterpret_cast<uintptr_t>(d_cmp) & 15) || (reinterpret_cast<uintptr_t>(d_out) & 7)) return GST_E_ARG;
+  const gst_header &h = *hdr;
+  // The header rules of gst_parse_header (README.md:67-71 of the reference).
+  if (h.width == 0 || h.height == 0 || h.width % 128 || h.height % 128) return GST_E_FORMAT;
+  const uint64_t px = uint64_t(h.width) * h.height;
+  if (px % (16u * 256u * 32u)) return GST_E_FORMAT;
+  const uint64_t B = px / 16;
+  if (h.palette_bytes == 0 || h.palette_bytes % kSymsPerGroup) return GST_E_FORMAT;
+  const uint32_t lens[4] = {h.y_cmp_sz, h.chroma_cmp_sz, h.palette_sz, h.indices_sz};
+  const uint64_t syms[4] = {2 * B, 4 * B, h.palette_bytes, B};
+  for (int s = 0; s < 4; ++s) {
+    const uint64_t G = syms[s] / kSymsPerGroup;
+    if (lens[s] % 4 || G * (4 + 4 * kStreamsPerGroup) > lens[s]) return GST_E_FORMAT;
+  }
+  // Scratch inside the static array: symbols, chunk prefixes, group sums.
+  auto up = [](uint64_t x) { return (x + 255) / 256 * 256; };
+  const uint64_t sym_bytes = up(7 * B + h.palette_bytes), chunk_bytes = up(B / 32 * 4);
+  const uint64_t gsum_bytes = up(2 * (B / kSymsPerGroup) * 4);
+  if (kStaticHeaderBytes + sym_bytes + chunk_bytes + gsum_bytes > kStaticScratchBytes) return GST_E_ARG;
+
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return GST_E_CUDA;
+  uint8_t *base = nullptr;
+  gst_status st = static_setup(device, &base);
+  if (st != GST_OK) return st;
+
+  GstImageDesc im = {};
+  im.freq_off = 512;  // the reference's layout for one image: offsets page, tables, sections
+  im.body_off = 512 + 4 * kFreqTableBytes;
+  im.sym_off = 0;
+  im.chunk_off = sym_bytes;
+  im.gsum_off = sym_bytes + chunk_bytes;
+  im.out_off = 0;
+  uint32_t in = 0, o = 0, rans_ctas = 0;
+  for (int s = 0; s < 4; ++s) {
+    im.sec_in[s] = in;
+    im.sec_len[s] = lens[s];
+    im.sec_groups[s] = uint32_t(syms[s] / kSymsPerGroup);
+    im.sec_out[s] = o;
+    in += lens[s];
+    o += uint32_t(syms[s]);
+    rans_ctas += (im.sec_groups[s] + kGroupsPerRansCta - 1) / kGroupsPerRansCta;
+  }
+  im.bx = h.width / 4;
+  im.by = h.height / 4;
+  im.palette_words = h.palette_bytes / 4;
+  im.tiles_x = im.bx / kWaveletDim;
+
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // Words that must start at zero: the status word and the index-group counter.
+  if (cudaMemsetAsync(base, 0, 8, s) != cudaSuccess) return GST_E_CUDA;
+  gst_rans_static_kernel<<<rans_ctas, 256, kRansSmemBytes, s>>>(static_cast<const uint8_t *>(d_cmp), base, im);
+  gst_tile_static_kernel<<<uint32_t(B / 1024), 256, 0, s>>>(base, static_cast<uint8_t *>(d_out), im);
+  if (cudaGetLastError() != cudaSuccess) return GST_E_CUDA;
+  if (device_status) {
+    if (cudaStreamSynchronize(s) != cudaSuccess) return GST_E_CUDA;
+    uint32_t bits = 0;
+    if (cudaMemcpy(&bits, base, sizeof(bits), cudaMemcpyDeviceToHost) != cudaSuccess) return GST_E_CUDA;
+    *device_status = bits;
+  }
+  return GST_OK;
+}

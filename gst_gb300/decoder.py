@@ -43,7 +43,7 @@ EXPORTED_SYMBOLS = (
     "gst_decompress_dxt", "gst_load_compressed_dxt", "gst_load_compressed_dxts",
     "gst_batch_layout_bytes", "gst_pack_batch", "gst_decode_rans_groups",
     "gst_batch_create", "gst_batch_destroy", "gst_batch_device_bytes", "gst_batch_launch",
-    "gst_batch_graph_launch",
+    "gst_batch_graph_launch", "gst_load_compressed_dxt_static",
     "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times",
     "gst_status_string",
 )
@@ -120,6 +120,7 @@ def load_library() -> ctypes.CDLL:
         "gst_batch_device_bytes": (S, [P]),
         "gst_batch_launch": (I, [P, P, P, P]),
         "gst_batch_graph_launch": (I, [P, P, P, P]),
+        "gst_load_compressed_dxt_static": (I, [HP, P, P, P, ctypes.POINTER(U32)]),
         "gst_sync_status": (I, [P, P]),
         "gst_last_launch_count": (I, [P]),
         "gst_set_profiling": (I, [P, I]),

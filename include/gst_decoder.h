@@ -119,6 +119,29 @@ size_t gst_batch_device_bytes(const gst_batch *batch);
 gst_status gst_batch_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
 gst_status gst_batch_graph_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
 
+/* One-image device-resident decode that allocates nothing -- no counterpart in
+ * the reference, which allocates its decoder scratch per call or through
+ * PreallocateDecompressor.  For callers that must not allocate device memory
+ * while they decode: a render or streaming thread that cannot absorb the
+ * device-wide synchronisation cudaMalloc/cudaFree may cause, code running while
+ * its stream is being captured into a CUDA graph, or an engine that owns all
+ * device memory through its own pools.  It needs no gst_ctx (creating one
+ * allocates).  Input and output are the caller's, as for
+ * gst_load_compressed_dxt; the scratch is a 4 MiB array built into the library,
+ * held by every GPU that loads the library until the process exits.
+ *   - Limit: the image's scratch (256 + 7*B + palette_bytes + B/8 + B/1024
+ *     bytes, B = width*height/16) must fit in 4 MiB -- about 2048x2048;
+ *     larger images return GST_E_ARG and nothing is enqueued.
+ *   - All calls share that array and leave their data in it: each call clears
+ *     the words that must start at zero; calls whose GPU work overlaps (other
+ *     streams without ordering, other host threads) race -- serialise them.
+ *   - The first call on a device looks up the array's address on that device;
+ *     make it before any stream capture there.
+ *   - With device_status non-null the call waits for `stream` and stores the
+ *     kernels' error bits there (0 when the stream was well formed). */
+gst_status gst_load_compressed_dxt_static(const gst_header *hdr, const void *d_cmp, void *d_out, void *stream,
+                                          uint32_t *device_status);
+
 /* Size of the reference's device layout for these headers (offsets page,
  * frequency tables, sections), and a host-side packer that writes it from
  * n complete GST streams (gst[i] of len[i] bytes) into `dst`. */

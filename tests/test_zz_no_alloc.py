@@ -1,0 +1,69 @@
+"""gst_load_compressed_dxt_static: the one-image decode that allocates nothing.
+
+It exists for callers that may not allocate device memory while they decode
+(a frame-budgeted render or streaming thread, code whose stream is being
+captured into a CUDA graph, an engine that owns all device memory), so its
+scratch is an array built into the library instead of cudaMalloc'd memory.
+These tests call it through the C ABI and check it against the allocating
+entry point, gst_load_compressed_dxt, on two calls in a row.  This file is
+collected last so that a run stopping at the first failure has already run
+every other test."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import golden_stream
+from gst_gb300 import decoder, workloads
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _device_layout(stream: bytes):
+    hdrs, packed = decoder.pack_batch([stream])
+    return hdrs[0], torch.from_numpy(packed).cuda()
+
+
+def _static_decode(hdr, d_cmp, d_out, side):
+    status = ctypes.c_uint32(0xFFFFFFFF)
+    rc = decoder.load_library().gst_load_compressed_dxt_static(
+        ctypes.byref(hdr), d_cmp.data_ptr(), d_out.data_ptr(), side.cuda_stream, ctypes.byref(status))
+    return rc, status.value
+
+
+def test_static_decode_matches_allocating_entry_point_twice_in_a_row():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    side = torch.cuda.Stream()
+    streams = [golden_stream("test1.gst"), workloads.encode_image(2048, 1024, 77).stream]
+    ctx = decoder.GPUContext(0)
+    try:
+        for s in streams:
+            hdr, d_cmp = _device_layout(s)
+            want = torch.zeros(hdr.dxt_bytes, dtype=torch.uint8, device="cuda")
+            decoder.load_compressed_dxt(ctx, hdr, d_cmp, want)
+            assert decoder.sync_status(ctx) == decoder.GST_OK
+            want = want.cpu().numpy()
+            for call in range(2):
+                got = torch.full((hdr.dxt_bytes,), 0xA5, dtype=torch.uint8, device="cuda")
+                torch.cuda.synchronize()
+                rc, bits = _static_decode(hdr, d_cmp, got, side)
+                assert rc == decoder.GST_OK, call
+                assert bits == 0, call
+                assert np.array_equal(got.cpu().numpy(), want), call
+    finally:
+        ctx.close()
+
+
+def test_static_decode_rejects_images_beyond_its_scratch():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    hdr = decoder.parse_header(golden_stream("test1.gst"))
+    big = decoder.GenTCHeader(*hdr.as_tuple())
+    big.width = big.height = 4096  # a well-formed 4096x4096 header needs ~7.4 MB of scratch
+    big.y_cmp_sz, big.chroma_cmp_sz, big.indices_sz = 256 * 264, 512 * 264, 128 * 264
+    d = torch.zeros(1024, dtype=torch.uint8, device="cuda")
+    rc = decoder.load_library().gst_load_compressed_dxt_static(
+        ctypes.byref(big), d.data_ptr(), d.data_ptr(), None, None)
+    assert rc == decoder.GST_E_ARG

@@ -56,7 +56,22 @@ def parse_args():
     p.add_argument("--cpu-sample", type=int, default=16, help="images of the batch the CPU baseline decodes")
     p.add_argument("--only", choices=("batched", "large", "plain", "rans"),
                    help="time one workload's decode call only (a small command for profilers)")
+    p.add_argument("--rans-blocks-per-sm", type=int, default=0,
+                   help="fix the rANS kernel's CTAs per SM (4, 6 or 8) instead of autotuning")
+    p.add_argument("--rans-stage-words", type=int, default=1016,
+                   help="staging depth with --rans-blocks-per-sm (a multiple of 8 in [520, 2816])")
     return p.parse_args()
+
+
+def tune(rb, b, stream, args) -> dict:
+    """The resident batch's rANS launch configuration: fixed by the command
+    line, or chosen by gst_batch_autotune (outside any timed region)."""
+    if args.rans_blocks_per_sm:
+        rb.set_tuning(args.rans_blocks_per_sm, args.rans_stage_words)
+        return {"blocks_per_sm": args.rans_blocks_per_sm, "stage_words": args.rans_stage_words,
+                "chosen_by": "command line"}
+    bps, words = rb.autotune(b.d_cmp, b.d_out, stream, iterations=3)
+    return {"blocks_per_sm": bps, "stage_words": words, "chosen_by": "gst_batch_autotune"}
 
 
 # ---------------------------------------------------------------------------
@@ -234,6 +249,9 @@ def run_only(args, local):
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
     ctx = decoder.GPUContext(local)
+    if args.rans_blocks_per_sm:
+        ctx.set_option("rans_blocks_per_sm", args.rans_blocks_per_sm)
+        ctx.set_option("rans_stage_words", args.rans_stage_words)
     stream = torch.cuda.Stream(device)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=device)
     if args.only == "rans":
@@ -242,7 +260,10 @@ def run_only(args, local):
         d_b = torch.from_numpy(np.frombuffer(sec.section[512:], np.uint8).copy()).to(device)
         d_o = torch.empty(sec.symbols.size, dtype=torch.uint8, device=device)
         fn = lambda: decoder.decode_rans_groups(ctx, d_f, d_b, len(sec.section) - 512, sec.n_groups, 32, d_o, stream)  # noqa: E731
-        t, _ = time_steps(fn, args.steps, args.warmup, stream, flush)
+        ctx.set_profiling(True)  # device time of the kernel (the call also uploads a plan from the host)
+        _, k = time_steps(fn, args.steps, args.warmup, stream, flush, ctx)
+        ctx.set_profiling(False)
+        t = [sum(ms for _, ms in step) for step in k]
         ok = bool(np.array_equal(d_o.cpu().numpy(), sec.symbols))
         units = sec.symbols.size
     else:
@@ -250,14 +271,18 @@ def run_only(args, local):
                 "plain": lambda: [workloads.plain(0)]}[args.only]()
         b = Batch(imgs, device)
         rb = decoder.ResidentBatch(ctx, b.hdrs)
+        tuning = tune(rb, b, stream, args)
         fn = lambda: rb.launch(b.d_cmp, b.d_out, stream, graph=True)  # noqa: E731
         t, _ = time_steps(fn, args.steps, args.warmup, stream, flush)
         ok = bool(np.array_equal(b.d_out.cpu().numpy().view(np.uint64), b.expected()))
         units = b.pixels
         rb.close()
     ctx.close()
-    return {"only": args.only, "ms_per_call": round(statistics.mean(t), 4), "units_per_call": units,
+    line = {"only": args.only, "ms_per_call": round(statistics.mean(t), 4), "units_per_call": units,
             "bit_exact": ok, "steps": args.steps, "warmup": args.warmup}
+    if args.only != "rans":
+        line["rans_tuning"] = tuning
+    return line
 
 
 def run_gst(args, rank, world, local):
@@ -274,6 +299,7 @@ def run_gst(args, rank, world, local):
     stream = torch.cuda.Stream(device)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=device)
     rb = decoder.ResidentBatch(ctx, batch.hdrs)
+    tuning = tune(rb, batch, stream, args)
 
     def step_batched():  # the resident batch, replayed as a captured CUDA graph
         rb.launch(batch.d_cmp, batch.d_out, stream, graph=True)
@@ -348,6 +374,7 @@ def run_gst(args, rank, world, local):
             "dxt1_bytes_per_step": batch.out_bytes,
             "l2": "flushed by a 256 MiB write before each timed step (outside the timed events)",
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "rans_tuning": tuning,
         },
         "dxt1_gbs": round(batch.out_bytes * args.steps / (total_ms / 1e3) / 1e9 * world, 2),
         "p50_ms": round(float(np.percentile(times, 50)), 4),
@@ -402,6 +429,7 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
     for name, imgs in (("large_8192", [workloads.large()]), ("plain_512", [workloads.plain(0)])):
         b = Batch(imgs, device)
         rb = decoder.ResidentBatch(ctx, b.hdrs)
+        tuning = tune(rb, b, stream, args)
         fn = lambda b=b, rb=rb: rb.launch(b.d_cmp, b.d_out, stream, graph=True)  # noqa: E731
         t, _ = time_steps(fn, steps, 3, stream, flush)
         ok = bool(np.array_equal(b.d_out.cpu().numpy().view(np.uint64), b.expected()))
@@ -417,7 +445,7 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
             "dxt1_gbs": round(b.out_bytes / (ms / 1e3) / 1e9, 2),
             "hbm_frac": round(b.alg_bytes / (ms / 1e3) / 1e9 / peak, 4),
             "kernels": {kk: round(v["avg_ms"], 4) for kk, v in ks.items()},
-            "gst_bytes": b.gst_bytes, "bit_exact": ok,
+            "gst_bytes": b.gst_bytes, "bit_exact": ok, "rans_tuning": tuning,
         }
         rb.close()
     sec = workloads.rans_section()
@@ -425,7 +453,10 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
     d_b = torch.from_numpy(np.frombuffer(sec.section[512:], np.uint8).copy()).to(device)
     d_o = torch.empty(sec.symbols.size, dtype=torch.uint8, device=device)
     fn = lambda: decoder.decode_rans_groups(ctx, d_f, d_b, len(sec.section) - 512, sec.n_groups, 32, d_o, stream)  # noqa: E731
-    t, _ = time_steps(fn, steps, 3, stream, flush)
+    ctx.set_profiling(True)  # device time of table build + decode (the call also uploads a plan from the host)
+    _, k = time_steps(fn, steps, 3, stream, flush, ctx)
+    ctx.set_profiling(False)
+    t = [sum(ms for _, ms in step) for step in k]
     ok = bool(np.array_equal(d_o.cpu().numpy(), sec.symbols))
     alg = len(sec.section) + sec.symbols.size
     out["rans_2^26"] = {

@@ -18,8 +18,8 @@
 
 namespace gst {
 const char *kernel_name(int i);
-cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, const GstPlanView &plan,
-                          cudaStream_t stream, int *launches, cudaEvent_t *ev);
+cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, GstPlanView plan,
+                          cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning);
 }
 
 constexpr int kMaxTimedKernels = 4;
@@ -117,6 +117,7 @@ struct gst_ctx {
   uint8_t *out_h = nullptr;  // pinned
   size_t out_h_cap = 0;
   int last_launches = 0;
+  GstTuning tuning;  // rANS launch configuration of the context's calls and untuned batches
   // Instrumentation: events around each kernel of the last decode call.
   bool profiling = false;
   cudaEvent_t ev[kMaxTimedKernels + 1] = {};
@@ -217,7 +218,7 @@ gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, size_
   view.n_rans = n_rans;
   view.n_tiles = n_tiles;
   cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
-  e = launch_decode(d_cmp, d_scratch, d_out, view, stream, &ctx->last_launches, ev);
+  e = launch_decode(d_cmp, d_scratch, d_out, view, stream, &ctx->last_launches, ev, ctx->tuning);
   ctx->timed_kernels = ev ? ctx->last_launches : 0;
   if (e != cudaSuccess) return cuda_status(e);
   if (!cap) {
@@ -370,10 +371,32 @@ struct gst_batch {
   size_t out_bytes = 0;
   uint8_t *plan_d = nullptr;
   uint8_t *scratch = nullptr;
+  bool tuned = false;  // tuning set by gst_batch_autotune / gst_batch_set_tuning
+  GstTuning tuning;
   cudaGraphExec_t graph = nullptr;
   const void *graph_cmp = nullptr;
   void *graph_out = nullptr;
+  GstTuning graph_tuning;
 };
+
+namespace {
+
+GstTuning batch_tuning(const gst_batch *b) { return b->tuned ? b->tuning : b->ctx->tuning; }
+
+bool valid_tuning(int blocks_per_sm, int stage_words) {
+  return blocks_per_sm >= 1 && blocks_per_sm <= 8 && stage_words >= int(kMinStageWords) &&
+         stage_words <= int(kMaxStageWords) && (stage_words & 7) == 0;
+}
+
+// Launches the batch's kernels under `t`; the caller holds ctx->mu.
+cudaError_t batch_launch_locked(gst_batch *b, const void *d_cmp, void *d_out, cudaStream_t st, const GstTuning &t,
+                                cudaEvent_t *ev) {
+  gst_ctx *ctx = b->ctx;
+  return launch_decode(static_cast<const uint8_t *>(d_cmp), b->scratch, static_cast<uint8_t *>(d_out),
+                       plan_view(b->layout, b->plan_d, ctx->status_d), st, &ctx->last_launches, ev, t);
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -694,8 +717,7 @@ gst_status gst_batch_launch(gst_batch *b, const void *d_cmp, void *d_out, void *
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const bool cap = capturing(st);
   cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
-  cudaError_t e = launch_decode(static_cast<const uint8_t *>(d_cmp), b->scratch, static_cast<uint8_t *>(d_out),
-                                plan_view(b->layout, b->plan_d, ctx->status_d), st, &ctx->last_launches, ev);
+  cudaError_t e = batch_launch_locked(b, d_cmp, d_out, st, batch_tuning(b), ev);
   ctx->timed_kernels = ev ? ctx->last_launches : 0;
   return cuda_status(e);
 }
@@ -704,14 +726,15 @@ gst_status gst_batch_graph_launch(gst_batch *b, const void *d_cmp, void *d_out, 
   if (!b || !d_cmp || !d_out) return GST_E_ARG;
   gst_ctx *ctx = b->ctx;
   cudaSetDevice(ctx->device);
-  if (!b->graph || b->graph_cmp != d_cmp || b->graph_out != d_out) {
+  if (!b->graph || b->graph_cmp != d_cmp || b->graph_out != d_out || b->graph_tuning != batch_tuning(b)) {
     // Capture the launch sequence once per (input, output) pair.
     cudaStream_t cs = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_status(e);
     {
       std::lock_guard<std::mutex> lock(ctx->mu);
-      launch_decode(nullptr, nullptr, nullptr, GstPlanView{}, nullptr, &ctx->last_launches, nullptr);  // configure attributes
+      launch_decode(nullptr, nullptr, nullptr, GstPlanView{}, nullptr, &ctx->last_launches, nullptr,
+                    GstTuning{});  // configure attributes
     }
     cudaGraph_t g = nullptr;
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
@@ -734,8 +757,84 @@ gst_status gst_batch_graph_launch(gst_batch *b, const void *d_cmp, void *d_out, 
     if (e != cudaSuccess) return cuda_status(e);
     b->graph_cmp = d_cmp;
     b->graph_out = d_out;
+    b->graph_tuning = batch_tuning(b);
   }
   return cuda_status(cudaGraphLaunch(b->graph, static_cast<cudaStream_t>(stream)));
+}
+
+gst_status gst_set_option(gst_ctx *ctx, const char *name, int value) {
+  if (!ctx || !name) return GST_E_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if (strcmp(name, "rans_blocks_per_sm") == 0) {
+    if (!valid_tuning(value, int(ctx->tuning.stage_words))) return GST_E_ARG;
+    ctx->tuning.blocks_per_sm = value;
+    return GST_OK;
+  }
+  if (strcmp(name, "rans_stage_words") == 0) {
+    if (!valid_tuning(ctx->tuning.blocks_per_sm, value)) return GST_E_ARG;
+    ctx->tuning.stage_words = uint32_t(value);
+    return GST_OK;
+  }
+  return GST_E_ARG;
+}
+
+gst_status gst_batch_set_tuning(gst_batch *b, int blocks_per_sm, int stage_words) {
+  if (!b) return GST_E_ARG;
+  if (blocks_per_sm == 0 && stage_words == 0) {  // back to the context's configuration
+    b->tuned = false;
+    return GST_OK;
+  }
+  if (!valid_tuning(blocks_per_sm, stage_words)) return GST_E_ARG;
+  std::lock_guard<std::mutex> lock(b->ctx->mu);
+  b->tuning.blocks_per_sm = blocks_per_sm;
+  b->tuning.stage_words = uint32_t(stage_words);
+  b->tuned = true;
+  return GST_OK;
+}
+
+gst_status gst_batch_autotune(gst_batch *b, const void *d_cmp, void *d_out, void *stream, int iterations,
+                              int *blocks_per_sm, int *stage_words) {
+  if (!b || !d_cmp || !d_out || iterations < 1) return GST_E_ARG;
+  if ((reinterpret_cast<uintptr_t>(d_cmp) & 15) || (reinterpret_cast<uintptr_t>(d_out) & 7)) return GST_E_ARG;
+  gst_ctx *ctx = b->ctx;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (capturing(st)) return GST_E_ARG;
+  // CTAs per SM x staging depth; each staging depth is the largest (or half
+  // the largest) that the shared memory of that many CTAs per SM holds.
+  static const GstTuning kCandidates[] = {
+      {8, 520}, {8, 1016}, {6, 1016}, {6, 1528}, {4, 2040}, {4, 2816},
+  };
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  GstTuning best = batch_tuning(b);
+  float best_ms = 0.f;
+  bool found = false;
+  for (const GstTuning &t : kCandidates) {
+    if (e != cudaSuccess) break;
+    e = batch_launch_locked(b, d_cmp, d_out, st, t, nullptr);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    for (int i = 0; i < iterations && e == cudaSuccess; ++i) e = batch_launch_locked(b, d_cmp, d_out, st, t, nullptr);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && (!found || ms < best_ms)) {
+      best = t;
+      best_ms = ms;
+      found = true;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e != cudaSuccess) return cuda_status(e);
+  b->tuning = best;
+  b->tuned = true;
+  if (blocks_per_sm) *blocks_per_sm = best.blocks_per_sm;
+  if (stage_words) *stage_words = int(best.stage_words);
+  return GST_OK;
 }
 
 gst_status gst_sync_status(gst_ctx *ctx, void *stream) {

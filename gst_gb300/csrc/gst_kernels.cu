@@ -42,10 +42,10 @@ __device__ __forceinline__ void flag_error(uint32_t *err, uint32_t bits) { atomi
 // ---------------------------------------------------------------------------
 // Decode table (ans/build_table.cl:12-83).  Slot s in [0, 2048) belongs to the
 // symbol x with cum[x] <= s < cum[x] + freq[x]; the table stores
-// (s - cum) | freq << 11 | x << 24 so that one lookup gives the next state,
+// freq << 20 | x << 12 | (s - cum) so that one lookup gives the next state,
 // x' = (x >> 11) * freq + (s - cum), equal to the reference's
-// (x >> 11) * freq - cum + s in u32 arithmetic, and the symbol is the top
-// byte.  Requires blockDim.x == 256.
+// (x >> 11) * freq - cum + s in u32 arithmetic; freq (at most 2048) is the
+// top 12 bits.  Requires blockDim.x == 256.
 // Returns false (block-uniformly) if the frequencies do not sum to 2048.
 __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t *tbl, uint32_t *cum_s,
                                    uint32_t *f_s, uint32_t *wsum) {
@@ -73,7 +73,7 @@ __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t 
 #pragma unroll
     for (uint32_t step = 128; step >= 1; step >>= 1)
       if (cum_s[x + step] <= s) x += step;
-    tbl[s] = (s - cum_s[x]) | (f_s[x] << 11) | (x << 24);
+    tbl[s] = (f_s[x] << 20) | (x << 12) | (s - cum_s[x]);
   }
   __syncthreads();
   return true;
@@ -81,18 +81,21 @@ __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t 
 
 // ---------------------------------------------------------------------------
 // rANS kernel shared memory: the decode table, the table-build scratch, and one
-// staging buffer per warp holding (the top of) its group's renormalisation
-// words, so that the serial decode chain reads shared memory, not HBM.
-constexpr int kStageWords = 2816;               // 16-bit words staged per group (5.5 KB)
-constexpr int kStagePitch = kStageWords + 8;    // + slack for the 16-byte alignment of the copy
-struct alignas(16) RansSmem {
+// staging buffer per warp holding the renormalisation words the warp is about
+// to read, so that the serial decode chain reads shared memory, not HBM.
+// The stage holds `stage_words` 16-bit words per warp (a launch parameter, the
+// "staging depth" tuning knob), each warp's stage padded by 8 words of slack
+// for the 16-byte alignment of the copy.
+struct alignas(16) RansHead {
   uint32_t tbl[kTableSize];
   uint32_t cum[257];
   uint32_t f[256];
   uint32_t wsum[8];
-  alignas(16) uint16_t stage[kGroupsPerRansCta][kStagePitch];
 };
-constexpr size_t kRansSmemBytes = sizeof(RansSmem);
+constexpr size_t kStageOffset = (sizeof(RansHead) + 15) & ~size_t(15);
+__host__ __device__ constexpr size_t rans_smem_bytes(uint32_t stage_words) {
+  return kStageOffset + size_t(kGroupsPerRansCta) * (stage_words + 8) * 2;
+}
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
   const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
@@ -125,13 +128,13 @@ __device__ __forceinline__ void stage_range(uint8_t *buf, const uint8_t *a, cons
   __syncwarp();
 }
 
-// One rANS step for every lane (ans_decode.cl:120-148).  Returns the new
-// state's renormalisation need; `e` receives the table entry (symbol in its top
-// byte).
-__device__ __forceinline__ uint32_t rans_advance(uint32_t x, const uint32_t *__restrict__ tbl, uint32_t *e_out) {
-  const uint32_t e = tbl[x & (kTableSize - 1)];
-  *e_out = e;
-  return (x >> 11) * ((e >> 11) & 0xFFFu) + (e & 0x7FFu);
+// Byte offset of table slot (x mod 2048) computed on the FMA pipe as
+// 4x - 8192 (x >> 11), sparing the integer ALU pipe the mask and shift.
+__device__ __forceinline__ uint32_t slot_offset(uint32_t x, uint32_t q) {
+  uint32_t x4, off;
+  asm("mul.lo.u32 %0, %1, 4;" : "=r"(x4) : "r"(x));
+  asm("mad.lo.u32 %0, %1, 4294959104, %2;" : "=r"(off) : "r"(q), "r"(x4));  // 4294959104 = -8192 mod 2^32
+  return off;
 }
 
 // Decodes one group: ns <= 32 interleaved streams of 256 symbols whose final
@@ -140,63 +143,70 @@ __device__ __forceinline__ uint32_t rans_advance(uint32_t x, const uint32_t *__r
 // also returns the lane's suffix sums of (symbol - 128) after 32, 64, ..., 256
 // steps in suf[] (the palette-index deltas).
 //
-// FAST: the whole word region is staged in shared memory.  Every lane then
-// reads the stage each step (a clamped, always in-bounds read; only lanes that
-// renormalise keep the word), with no per-step branch; a valid stream never
-// reads below the region, and the final read pointer tells if a malformed one
-// did.  Otherwise the top kStageWords words are staged and reads below them go
-// to global memory with per-read checks.
-template <bool INDEX, bool FAST>
+// The top stage_words words of [lo, top) are staged in shared memory; every 16
+// steps, if the next 16 steps could read below the staged words, the warp
+// re-stages the stage_words words below its read pointer (a warp-uniform test;
+// groups that fit never re-stage).  Every lane reads the stage each step at a
+// clamped, always in-bounds index and keeps the word only if it renormalises;
+// a valid stream never reads below its group, and the final read pointer tells
+// if a malformed one did.
+template <bool INDEX>
 __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, uint32_t lo, uint32_t top,
-                                             const uint32_t *__restrict__ tbl, uint16_t *stage, int lane, bool active,
-                                             uint8_t *__restrict__ out, int32_t suf[8]) {
-  const uint32_t stage_lo = FAST ? lo : top - 2u * kStageWords;
+                                             const uint32_t *__restrict__ tbl, uint16_t *stage, uint32_t stage_words,
+                                             int lane, bool active, uint8_t *__restrict__ out, int32_t suf[8]) {
+  const uint32_t pitch = stage_words + 8;
+  const uint8_t *tbl_bytes = reinterpret_cast<const uint8_t *>(tbl);
+  const int lo16 = static_cast<int>(lo >> 1);
+  uint32_t stage_lo = (top - lo > 2u * stage_words) ? top - 2u * stage_words : lo;
   stage_range(reinterpret_cast<uint8_t *>(stage), sec + stage_lo, sec + top, lane);
   // stage[0] holds the word at sec + stage_lo rounded down to 16 bytes, so
   // word idx of the section is stage[idx - sbase16].
-  const int sbase16 = static_cast<int>(stage_lo >> 1) -
-                      static_cast<int>((reinterpret_cast<uintptr_t>(sec + stage_lo) & 15) >> 1);
-  const int lo16 = static_cast<int>(lo >> 1), fast_lo = static_cast<int>(stage_lo >> 1);
-  const uint16_t *words = reinterpret_cast<const uint16_t *>(sec);
+  int sbase16 = static_cast<int>(stage_lo >> 1) -
+                static_cast<int>((reinterpret_cast<uintptr_t>(sec + stage_lo) & 15) >> 1);
   uint32_t x = active ? reinterpret_cast<const uint32_t *>(sec + top)[lane] : kRansL;
-  int ptr = static_cast<int>(top >> 1);
-  bool bad = false;
+  int ptr = static_cast<int>(top >> 1);  // word index of the section
+  int sptr = ptr - sbase16;              // the same, relative to the stage
   const uint32_t lt = lanemask_lt();
   uint32_t total_sym = 0;
   int32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0;
-#pragma unroll 2
+#pragma unroll 1
   for (int k = 0; k < 16; ++k) {
+    if (ptr - 16 * 32 < static_cast<int>(stage_lo >> 1) && static_cast<int>(stage_lo) > static_cast<int>(lo) &&
+        ptr > lo16) {
+      // Every later read is below ptr: stage the words just below it.
+      const uint32_t new_top = (2u * static_cast<uint32_t>(ptr) + 3u) & ~3u;
+      stage_lo = (new_top - lo > 2u * stage_words) ? new_top - 2u * stage_words : lo;
+      stage_range(reinterpret_cast<uint8_t *>(stage), sec + stage_lo, sec + new_top, lane);
+      sbase16 = static_cast<int>(stage_lo >> 1) -
+                static_cast<int>((reinterpret_cast<uintptr_t>(sec + stage_lo) & 15) >> 1);
+      sptr = ptr - sbase16;
+    }
     uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      uint32_t e;
-      x = rans_advance(x, tbl, &e);
+      // Lane l holds the word 32 - l below the read pointer, fetched before
+      // the state update so that it is off the dependency chain.
+      const uint32_t pre = stage[min(static_cast<uint32_t>(sptr - 32 + lane), pitch - 1)];
+      const uint32_t q = x >> 11;
+      const uint32_t e = *reinterpret_cast<const uint32_t *>(tbl_bytes + slot_offset(x, q));
+      x = q * (e >> 20) + (e & 0x7FFu);
       const bool need = active && x < kRansL;
       const uint32_t m = __ballot_sync(0xFFFFFFFFu, need);
       const int total = __popc(m);
       // ans_decode.cl:133-140: renormalising lanes read consecutive 16-bit
-      // words below the read pointer, the lowest lane the lowest address.
-      const int idx = ptr - total + __popc(m & lt);
-      if (FAST) {
-        const uint32_t si = min(static_cast<uint32_t>(idx - sbase16), static_cast<uint32_t>(kStagePitch - 1));
-        const uint32_t v = stage[si];
-        x = need ? __byte_perm(x, v, 0x1054) : x;
-      } else if (ptr - total >= fast_lo) {  // warp-uniform: every read is staged
-        if (need) x = __byte_perm(x, stage[idx - sbase16], 0x1054);
-      } else if (need) {
-        uint32_t v = 0;
-        if (idx >= fast_lo) v = stage[idx - sbase16];
-        else if (idx >= lo16) v = __ldg(words + idx);
-        else bad = true;
-        x = __byte_perm(x, v, 0x1054);
-      }
-      ptr -= total;
-      if (j < 4) w3 = __byte_perm(w3, e, 0x2107);
-      else if (j < 8) w2 = __byte_perm(w2, e, 0x2107);
-      else if (j < 12) w1 = __byte_perm(w1, e, 0x2107);
-      else w0 = __byte_perm(w0, e, 0x2107);
-      if (INDEX) total_sym += e >> 24;
+      // words below the read pointer, the lowest lane the lowest address:
+      // word ptr - total + rank, which lane 32 - total + rank prefetched.
+      const uint32_t v = __shfl_sync(0xFFFFFFFFu, pre, 32 - total + __popc(m & lt));
+      if (need) x = __byte_perm(x, v, 0x1054);
+      sptr -= total;
+      const uint32_t sym = e >> 12;  // symbol in the low byte
+      if (j < 4) w3 = __byte_perm(w3, sym, 0x2104);
+      else if (j < 8) w2 = __byte_perm(w2, sym, 0x2104);
+      else if (j < 12) w1 = __byte_perm(w1, sym, 0x2104);
+      else w0 = __byte_perm(w0, sym, 0x2104);
+      if (INDEX) total_sym += sym & 0xFFu;
     }
+    ptr = sptr + sbase16;
     // Steps 16k..16k+15 are positions 255-16k .. 240-16k of this stream
     // (ans_decode.cl:154-155 stores the symbols in reverse).
     if (active) *reinterpret_cast<uint4 *>(out + 240 - 16 * k) = make_uint4(w0, w1, w2, w3);
@@ -217,15 +227,17 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
     suf[0] = s0; suf[1] = s1; suf[2] = s2; suf[3] = s3;
     suf[4] = s4; suf[5] = s5; suf[6] = s6; suf[7] = s7;
   }
-  // In FAST mode the lowest word read is the final pointer.
-  if (FAST) bad = ptr < lo16;
-  return __any_sync(0xFFFFFFFFu, bad);
+  // The lowest word read is the final pointer.
+  return __any_sync(0xFFFFFFFFu, ptr < lo16);
 }
 
-__global__ void __launch_bounds__(256) gst_rans_kernel(const uint8_t *__restrict__ cmp,
-                                                       uint8_t *__restrict__ scratch, GstPlanView plan) {
+// MINB: CTAs per SM the register allocation must allow (the "blocks per SM"
+// tuning knob; 1 leaves ptxas free, 8 fills the SM with 64 warps).
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) gst_rans_kernel(const uint8_t *__restrict__ cmp,
+                                                             uint8_t *__restrict__ scratch, GstPlanView plan) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
-  RansSmem &sm = *reinterpret_cast<RansSmem *>(smem_raw);
+  RansHead &sm = *reinterpret_cast<RansHead *>(smem_raw);
 
   const GstRansItem it = plan.rans[blockIdx.x];
   const GstImageDesc &im = plan.images[it.image];
@@ -254,14 +266,10 @@ __global__ void __launch_bounds__(256) gst_rans_kernel(const uint8_t *__restrict
   int32_t suf[8];
   if (group_ok) {
     const uint32_t top = hi - 4u * ns;  // the group's final states sit at [top, hi)
-    const bool fits = top - lo <= 2u * kStageWords;  // warp-uniform
-    bool bad;
-    if (is_index)
-      bad = fits ? decode_group<true, true>(sec, lo, top, sm.tbl, sm.stage[warp], lane, active, out, suf)
-                 : decode_group<true, false>(sec, lo, top, sm.tbl, sm.stage[warp], lane, active, out, suf);
-    else
-      bad = fits ? decode_group<false, true>(sec, lo, top, sm.tbl, sm.stage[warp], lane, active, out, suf)
-                 : decode_group<false, false>(sec, lo, top, sm.tbl, sm.stage[warp], lane, active, out, suf);
+    uint16_t *stage = reinterpret_cast<uint16_t *>(smem_raw + kStageOffset) + warp * (plan.stage_words + 8);
+    const bool bad = is_index
+                         ? decode_group<true>(sec, lo, top, sm.tbl, stage, plan.stage_words, lane, active, out, suf)
+                         : decode_group<false>(sec, lo, top, sm.tbl, stage, plan.stage_words, lane, active, out, suf);
     if (bad && lane == 0) flag_error(err, kErrStream);
   } else if (lane == 0 && table_ok) {
     flag_error(err, kErrGroup);
@@ -452,20 +460,31 @@ __global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict
 }
 
 // Enqueues the decode of one plan.  With `ev` non-null, records ev[0] before
-// the first kernel and ev[i + 1] after kernel i (instrumentation).
-cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, const GstPlanView &plan,
-                          cudaStream_t stream, int *launches, cudaEvent_t *ev) {
+// the first kernel and ev[i + 1] after kernel i (instrumentation).  `tuning`
+// selects the rANS kernel's register budget (CTAs per SM) and staging depth.
+cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, GstPlanView plan,
+                          cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning) {
   *launches = 0;
   static bool configured = false;  // per process; the attribute applies to every device context
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(gst_rans_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(kRansSmemBytes));
+    const int bytes = static_cast<int>(rans_smem_bytes(kMaxStageWords));
+    cudaError_t e = cudaFuncSetAttribute(gst_rans_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(gst_rans_kernel<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(gst_rans_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
     configured = true;
   }
+  if (tuning.stage_words < kMinStageWords || tuning.stage_words > kMaxStageWords || (tuning.stage_words & 7))
+    return cudaErrorInvalidValue;
+  plan.stage_words = tuning.stage_words;
   if (ev) cudaEventRecord(ev[0], stream);
   if (plan.n_rans) {
-    gst_rans_kernel<<<plan.n_rans, 256, kRansSmemBytes, stream>>>(d_cmp, d_scratch, plan);
+    const size_t smem = rans_smem_bytes(plan.stage_words);
+    if (tuning.blocks_per_sm >= 7) gst_rans_kernel<8><<<plan.n_rans, 256, smem, stream>>>(d_cmp, d_scratch, plan);
+    else if (tuning.blocks_per_sm == 6) gst_rans_kernel<6><<<plan.n_rans, 256, smem, stream>>>(d_cmp, d_scratch, plan);
+    else gst_rans_kernel<1><<<plan.n_rans, 256, smem, stream>>>(d_cmp, d_scratch, plan);
     ++*launches;
     if (ev) cudaEventRecord(ev[*launches], stream);
   }
@@ -525,7 +544,7 @@ static __device__ __align__(256) uint8_t g_static_scratch[kStaticScratchBytes];
 __global__ void __launch_bounds__(256) gst_rans_static_kernel(const uint8_t *__restrict__ cmp, uint8_t *base,
                                                               GstImageDesc im) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
-  RansSmem &sm = *reinterpret_cast<RansSmem *>(smem_raw);
+  RansHead &sm = *reinterpret_cast<RansHead *>(smem_raw);
   uint32_t *err = reinterpret_cast<uint32_t *>(base);
   uint32_t *counter = err + 1;
   uint8_t *scratch = base + kStaticHeaderBytes;
@@ -561,14 +580,10 @@ __global__ void __launch_bounds__(256) gst_rans_static_kernel(const uint8_t *__r
   int32_t suf[8];
   if (group_ok) {
     const uint32_t top = hi - 4u * kStreamsPerGroup;
-    const bool fits = top - lo <= 2u * kStageWords;
-    bool bad;
-    if (is_index)
-      bad = fits ? decode_group<true, true>(sec, lo, top, sm.tbl, sm.stage[warp], lane, true, out, suf)
-                 : decode_group<true, false>(sec, lo, top, sm.tbl, sm.stage[warp], lane, true, out, suf);
-    else
-      bad = fits ? decode_group<false, true>(sec, lo, top, sm.tbl, sm.stage[warp], lane, true, out, suf)
-                 : decode_group<false, false>(sec, lo, top, sm.tbl, sm.stage[warp], lane, true, out, suf);
+    uint16_t *stage = reinterpret_cast<uint16_t *>(smem_raw + kStageOffset) + warp * (kDefaultStageWords + 8);
+    const bool bad =
+        is_index ? decode_group<true>(sec, lo, top, sm.tbl, stage, kDefaultStageWords, lane, true, out, suf)
+                 : decode_group<false>(sec, lo, top, sm.tbl, stage, kDefaultStageWords, lane, true, out, suf);
     if (bad && lane == 0) flag_error(err, kErrStream);
   } else if (lane == 0 && table_ok) {
     flag_error(err, kErrGroup);
@@ -713,7 +728,7 @@ gst_status static_setup(int device, uint8_t **base) {
     cudaError_t e = cudaGetSymbolAddress(&p, gst::g_static_scratch);
     if (e != cudaSuccess || !p) return GST_E_CUDA;
     e = cudaFuncSetAttribute(gst::gst_rans_static_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(gst::kRansSmemBytes));
+                             static_cast<int>(gst::rans_smem_bytes(gst::kDefaultStageWords)));
     if (e != cudaSuccess) return GST_E_CUDA;
     g_static_ptr[device] = p;
   }
@@ -778,7 +793,8 @@ extern "C" gst_status gst_load_compressed_dxt_static(const gst_header *hdr, cons
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // Words that must start at zero: the status word and the index-group counter.
   if (cudaMemsetAsync(base, 0, 8, s) != cudaSuccess) return GST_E_CUDA;
-  gst_rans_static_kernel<<<rans_ctas, 256, kRansSmemBytes, s>>>(static_cast<const uint8_t *>(d_cmp), base, im);
+  gst_rans_static_kernel<<<rans_ctas, 256, rans_smem_bytes(kDefaultStageWords), s>>>(
+      static_cast<const uint8_t *>(d_cmp), base, im);
   gst_tile_static_kernel<<<uint32_t(B / 1024), 256, 0, s>>>(base, static_cast<uint8_t *>(d_out), im);
   if (cudaGetLastError() != cudaSuccess) return GST_E_CUDA;
   if (device_status) {

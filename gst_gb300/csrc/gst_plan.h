@@ -23,6 +23,19 @@ constexpr uint32_t kSymsPerStream = 256;      //                    ans/ans.h:74
 constexpr uint32_t kStreamsPerGroup = 32;     //                    ans/ans.h:75
 constexpr uint32_t kSymsPerGroup = 8192;
 constexpr uint32_t kGroupsPerRansCta = 8;
+// rANS staging depth per warp, in 16-bit words (a multiple of 8, so that every
+// warp's stage starts 16-byte aligned).  Sixteen steps read at most 512 words
+// and a re-stage starts at most one word above the read pointer, so 520 words
+// always cover the next sixteen steps; 2816 keeps four CTAs per SM.
+constexpr uint32_t kMinStageWords = 520, kMaxStageWords = 2816, kDefaultStageWords = 1016;
+
+// Launch configuration of the rANS kernel.
+struct GstTuning {
+  int blocks_per_sm = 6;                       // register budget: 5 (unconstrained), 6 or 8 CTAs per SM
+  uint32_t stage_words = kDefaultStageWords;  // staging depth
+  bool operator==(const GstTuning &o) const { return blocks_per_sm == o.blocks_per_sm && stage_words == o.stage_words; }
+  bool operator!=(const GstTuning &o) const { return !(*this == o); }
+};
 constexpr uint32_t kRansL = 1u << 15;         // k * M, k = 2^4      ans/ans_ocl_encode.cpp:15-16
 constexpr uint32_t kFreqTableBytes = 512;
 constexpr uint32_t kWaveletDim = 32;          //                    codec/codec_base.h:22
@@ -78,6 +91,7 @@ struct GstPlanView {
   const GstTileItem *tiles;
   uint32_t *counters;  // one per image (index-group completion count)
   uint32_t n_rans, n_tiles;
+  uint32_t stage_words;  // rANS staging depth per warp, in 16-bit words
 };
 
 }  // namespace gst

@@ -43,8 +43,8 @@ EXPORTED_SYMBOLS = (
     "gst_decompress_dxt", "gst_load_compressed_dxt", "gst_load_compressed_dxts",
     "gst_batch_layout_bytes", "gst_pack_batch", "gst_decode_rans_groups",
     "gst_batch_create", "gst_batch_destroy", "gst_batch_device_bytes", "gst_batch_launch",
-    "gst_batch_graph_launch", "gst_load_compressed_dxt_static",
-    "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times",
+    "gst_batch_graph_launch", "gst_batch_autotune", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
+    "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times", "gst_set_option",
     "gst_status_string",
 )
 
@@ -119,11 +119,14 @@ def load_library() -> ctypes.CDLL:
         "gst_batch_destroy": (None, [P]),
         "gst_batch_device_bytes": (S, [P]),
         "gst_batch_launch": (I, [P, P, P, P]),
+        "gst_batch_autotune": (I, [P, P, P, P, I, ctypes.POINTER(I), ctypes.POINTER(I)]),
+        "gst_batch_set_tuning": (I, [P, I, I]),
         "gst_batch_graph_launch": (I, [P, P, P, P]),
         "gst_load_compressed_dxt_static": (I, [HP, P, P, P, ctypes.POINTER(U32)]),
         "gst_sync_status": (I, [P, P]),
         "gst_last_launch_count": (I, [P]),
         "gst_set_profiling": (I, [P, I]),
+        "gst_set_option": (I, [P, ctypes.c_char_p, I]),
         "gst_kernel_times": (I, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p), I]),
         "gst_status_string": (ctypes.c_char_p, [I]),
     }
@@ -204,6 +207,10 @@ class GPUContext:
     def last_launch_count(self) -> int:
         return int(load_library().gst_last_launch_count(self.handle))
 
+    def set_option(self, name: str, value: int) -> None:
+        """gst_set_option: a tuning knob ("rans_blocks_per_sm", "rans_stage_words")."""
+        _check(load_library().gst_set_option(self.handle, name.encode(), int(value)), "gst_set_option")
+
     def set_profiling(self, enable: bool) -> None:
         _check(load_library().gst_set_profiling(self.handle, int(enable)), "gst_set_profiling")
 
@@ -234,6 +241,20 @@ class ResidentBatch:
     def launch(self, cmp_data, output, stream=None, graph: bool = False) -> None:
         fn = load_library().gst_batch_graph_launch if graph else load_library().gst_batch_launch
         _check(fn(self._h, _ptr(cmp_data), _ptr(output), _stream(stream)), "gst_batch_launch")
+
+    def autotune(self, cmp_data, output, stream=None, iterations: int = 3) -> tuple[int, int]:
+        """gst_batch_autotune: times each (CTAs per SM, staging depth) rANS
+        configuration on this batch and keeps the fastest; returns it."""
+        bps, words = ctypes.c_int(0), ctypes.c_int(0)
+        _check(load_library().gst_batch_autotune(self._h, _ptr(cmp_data), _ptr(output), _stream(stream),
+                                                 int(iterations), ctypes.byref(bps), ctypes.byref(words)),
+               "gst_batch_autotune")
+        return bps.value, words.value
+
+    def set_tuning(self, blocks_per_sm: int, stage_words: int) -> None:
+        """gst_batch_set_tuning; (0, 0) returns to the context's configuration."""
+        _check(load_library().gst_batch_set_tuning(self._h, int(blocks_per_sm), int(stage_words)),
+               "gst_batch_set_tuning")
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:

@@ -119,6 +119,21 @@ size_t gst_batch_device_bytes(const gst_batch *batch);
 gst_status gst_batch_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
 gst_status gst_batch_graph_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
 
+/* Per-batch tuning of the rANS launch (no counterpart in the reference).
+ * gst_batch_autotune decodes the batch under each of a fixed set of
+ * (CTAs per SM, staging depth) configurations -- one warm-up and `iterations`
+ * timed launches each, on `stream`, blocking -- and keeps the fastest for the
+ * batch's later launches, writing it to *blocks_per_sm / *stage_words when
+ * those are non-null.  It writes the decoded output to d_out as a launch does
+ * and must not be called while `stream` is being captured.
+ * gst_batch_set_tuning sets the configuration directly (values as for the
+ * "rans_blocks_per_sm" and "rans_stage_words" options); (0, 0) returns the
+ * batch to the context's configuration.  Every configuration decodes
+ * bit-identically; only the time differs. */
+gst_status gst_batch_autotune(gst_batch *batch, const void *d_cmp, void *d_out, void *stream, int iterations,
+                              int *blocks_per_sm, int *stage_words);
+gst_status gst_batch_set_tuning(gst_batch *batch, int blocks_per_sm, int stage_words);
+
 /* One-image device-resident decode that allocates nothing -- no counterpart in
  * the reference, which allocates its decoder scratch per call or through
  * PreallocateDecompressor.  For callers that must not allocate device memory
@@ -176,6 +191,20 @@ int gst_last_launch_count(gst_ctx *ctx);
  * number written. */
 gst_status gst_set_profiling(gst_ctx *ctx, int enable);
 int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
+
+/* Tuning knobs of a context (no counterpart in the reference; its work-group
+ * sizes are fixed, codec/decoder.cpp:166-417).  Known names:
+ *   "rans_blocks_per_sm"  register budget of the rANS kernel in CTAs of 256
+ *                         threads per SM: 1-5 (no constraint), 6 (default)
+ *                         or 7-8 (eight).
+ *   "rans_stage_words"    16-bit renormalisation words each warp stages in
+ *                         shared memory: a multiple of 8 in [520, 2816];
+ *                         default 1016.  Deeper stages re-stage less often
+ *                         but leave room for fewer CTAs per SM.
+ * Invalid values and unknown names return GST_E_ARG.  They apply to the
+ * context's calls and to resident batches without a tuning of their own;
+ * such batches re-capture their graph after a change. */
+gst_status gst_set_option(gst_ctx *ctx, const char *name, int value);
 
 /* Human-readable name of a status code. */
 const char *gst_status_string(gst_status s);

@@ -245,3 +245,68 @@ def test_resident_batch_launch_and_graph_replay(gpu_ctx):
         assert decoder.sync_status(gpu_ctx, side) == decoder.GST_OK
         assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want), graph
     b.close()
+
+
+TUNINGS = [(8, 520), (8, 1016), (6, 1016), (6, 1528), (4, 2040), (4, 2816), (5, 904)]
+
+
+def test_every_tuning_decodes_identically(gpu_ctx):
+    # The rANS launch configuration (CTAs per SM x staging depth) changes only
+    # the time.  A high-entropy section (about 3,700 words per group, so every
+    # depth re-stages) and a mixed batch decode bit-identically under each.
+    sym = workloads.laplace_bytes(1 << 20, b=40.0, seed=11)
+    sec = encoder.encode_section(sym)
+    d_f, d_b = to_dev(sec[:512]), to_dev(sec[512:])
+    d_o = torch.zeros(sym.size, dtype=torch.uint8, device="cuda")
+    imgs = [workloads.encode_image(w, h, 700 + i) for i, (w, h) in enumerate([(1024, 1024), (512, 512), (2048, 512)])]
+    hdrs, packed = decoder.pack_batch([im.stream for im in imgs])
+    want = np.concatenate([im.blocks for im in imgs])
+    d_cmp = torch.from_numpy(packed).cuda()
+    d_out = torch.zeros(sum(h.dxt_bytes for h in hdrs), dtype=torch.uint8, device="cuda")
+    b = decoder.ResidentBatch(gpu_ctx, hdrs)
+    try:
+        for bps, words in TUNINGS:
+            gpu_ctx.set_option("rans_blocks_per_sm", bps)
+            gpu_ctx.set_option("rans_stage_words", words)
+            d_o.zero_()
+            decoder.decode_rans_groups(gpu_ctx, d_f, d_b, len(sec) - 512, sym.size // 8192, 32, d_o)
+            assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
+            assert np.array_equal(d_o.cpu().numpy(), sym), (bps, words)
+            for graph in (False, True):
+                d_out.zero_()
+                b.launch(d_cmp, d_out, graph=graph)  # untuned: follows the context
+                assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
+                assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want), (bps, words, graph)
+    finally:
+        gpu_ctx.set_option("rans_blocks_per_sm", 6)
+        gpu_ctx.set_option("rans_stage_words", 1016)
+        b.close()
+
+
+def test_batch_autotune_and_tuning_validation(gpu_ctx):
+    imgs = [workloads.encode_image(w, h, 720 + i) for i, (w, h) in enumerate([(2048, 2048), (1024, 512)])]
+    hdrs, packed = decoder.pack_batch([im.stream for im in imgs])
+    want = np.concatenate([im.blocks for im in imgs])
+    d_cmp = torch.from_numpy(packed).cuda()
+    d_out = torch.zeros(sum(h.dxt_bytes for h in hdrs), dtype=torch.uint8, device="cuda")
+    b = decoder.ResidentBatch(gpu_ctx, hdrs)
+    side = torch.cuda.Stream()
+    bps, words = b.autotune(d_cmp, d_out, side, iterations=2)
+    assert (bps, words) in TUNINGS[:6]
+    assert decoder.sync_status(gpu_ctx, side) == decoder.GST_OK
+    assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want)
+    d_out.zero_()
+    torch.cuda.synchronize()
+    b.launch(d_cmp, d_out, side, graph=True)
+    assert decoder.sync_status(gpu_ctx, side) == decoder.GST_OK
+    assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want)
+    for bad in ((6, 512), (6, 1001), (6, 2824), (9, 1016), (0, 1016)):
+        with pytest.raises(decoder.GstError) as ei:
+            b.set_tuning(*bad)
+        assert ei.value.status == decoder.GST_E_ARG
+    with pytest.raises(decoder.GstError):
+        gpu_ctx.set_option("rans_stage_words", 1004 + 1)
+    with pytest.raises(decoder.GstError):
+        gpu_ctx.set_option("no_such_option", 1)
+    b.set_tuning(0, 0)
+    b.close()

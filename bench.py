@@ -57,7 +57,7 @@ def parse_args():
     p.add_argument("--only", choices=("batched", "large", "plain", "rans"),
                    help="time one workload's decode call only (a small command for profilers)")
     p.add_argument("--rans-blocks-per-sm", type=int, default=0,
-                   help="fix the rANS kernel's CTAs per SM (4, 6 or 8) instead of autotuning")
+                   help="fix the rANS kernel's CTAs of 128 threads per SM (8, 12 or 16) instead of autotuning")
     p.add_argument("--rans-stage-words", type=int, default=1016,
                    help="staging depth with --rans-blocks-per-sm (a multiple of 8 in [520, 2816])")
     return p.parse_args()

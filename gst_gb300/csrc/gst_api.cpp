@@ -384,7 +384,7 @@ namespace {
 GstTuning batch_tuning(const gst_batch *b) { return b->tuned ? b->tuning : b->ctx->tuning; }
 
 bool valid_tuning(int blocks_per_sm, int stage_words) {
-  return blocks_per_sm >= 1 && blocks_per_sm <= 8 && stage_words >= int(kMinStageWords) &&
+  return blocks_per_sm >= 1 && blocks_per_sm <= 16 && stage_words >= int(kMinStageWords) &&
          stage_words <= int(kMaxStageWords) && (stage_words & 7) == 0;
 }
 
@@ -799,10 +799,10 @@ gst_status gst_batch_autotune(gst_batch *b, const void *d_cmp, void *d_out, void
   gst_ctx *ctx = b->ctx;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (capturing(st)) return GST_E_ARG;
-  // CTAs per SM x staging depth; each staging depth is the largest (or half
-  // the largest) that the shared memory of that many CTAs per SM holds.
+  // CTAs per SM x staging depth: the deepest stages that the shared memory
+  // of that many CTAs per SM holds, and shallower ones.
   static const GstTuning kCandidates[] = {
-      {8, 520}, {8, 1016}, {6, 1016}, {6, 1528}, {4, 2040}, {4, 2816},
+      {16, 520}, {12, 520}, {12, 1016}, {8, 1528}, {8, 2040}, {8, 2816},
   };
   std::lock_guard<std::mutex> lock(ctx->mu);
   cudaSetDevice(ctx->device);

@@ -5,8 +5,9 @@
 //
 //  gst_rans_kernel  (ans/build_table.cl + ans/ans_decode.cl + the group sums of
 //                    codec/decode_indices.cl)
-//     One CTA = 8 warps = up to 8 rANS groups of one section.  The CTA builds
-//     the section's 2048-slot decode table in shared memory (one packed u32 per
+//     One CTA = 4 warps = up to 4 rANS groups of one section (small CTAs keep
+//     the groups of a batch spread evenly over the SMs).  The CTA builds the
+//     section's 2048-slot decode table in shared memory (one packed u32 per
 //     slot), then each warp decodes one group of 32 interleaved streams x 256
 //     symbols: the 32 lanes are the 32 streams, a warp ballot + popcount gives
 //     each renormalising lane its read offset (the reference uses local-memory
@@ -42,39 +43,78 @@ __device__ __forceinline__ void flag_error(uint32_t *err, uint32_t bits) { atomi
 // ---------------------------------------------------------------------------
 // Decode table (ans/build_table.cl:12-83).  Slot s in [0, 2048) belongs to the
 // symbol x with cum[x] <= s < cum[x] + freq[x]; the table stores
-// freq << 20 | x << 12 | (s - cum) so that one lookup gives the next state,
-// x' = (x >> 11) * freq + (s - cum), equal to the reference's
-// (x >> 11) * freq - cum + s in u32 arithmetic; freq (at most 2048) is the
-// top 12 bits.  Requires blockDim.x == 256.
-// Returns false (block-uniformly) if the frequencies do not sum to 2048.
-__device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t *tbl, uint32_t *cum_s,
-                                   uint32_t *f_s, uint32_t *wsum) {
+// (s - cum) | freq << 11 | x << 24 (11, 12 and 8 bits) so that one lookup
+// gives the next state, x' = (x >> 11) * freq + (s - cum), equal to the
+// reference's (x >> 11) * freq - cum + s in u32 arithmetic, and the symbol as
+// the entry's top byte.
+//
+// Built without searching: each symbol with freq > 0 marks its first slot,
+// and since those first slots increase with x, a running maximum of the marks
+// over the slots gives every slot's symbol.  Entry = (freq << 11 | x << 24) -
+// cum + s, from one per-symbol word.  Requires blockDim.x == 128; `work` is
+// 3 KB of shared scratch (per-symbol words, slot marks) that is free again on
+// return.  Returns false (block-uniformly) if the frequencies do not sum to
+// 2048.
+__device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t *tbl, uint32_t *wred,
+                                   uint8_t *work) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const uint32_t f = freqs[t];
-  uint32_t v = f;
+  uint32_t *sym_word = reinterpret_cast<uint32_t *>(work);  // 256
+  uint8_t *marks = work + 1024;                             // 2048
+  reinterpret_cast<uint4 *>(marks)[t] = make_uint4(0, 0, 0, 0);
+  const uint32_t f0 = freqs[2 * t], f1 = freqs[2 * t + 1];
+  uint32_t v = f0 + f1;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, v, d);
     if (lane >= d) v += n;
   }
-  if (lane == 31) wsum[warp] = v;
+  if (lane == 31) wred[warp] = v;
   __syncthreads();
   uint32_t woff = 0;
 #pragma unroll
-  for (int w = 0; w < 8; ++w) woff += (w < warp) ? wsum[w] : 0u;
-  const uint32_t excl = woff + v - f;
-  cum_s[t] = excl;
-  f_s[t] = f;
-  if (t == 255) cum_s[256] = excl + f;
-  __syncthreads();
-  if (cum_s[256] != kTableSize) return false;
-  for (uint32_t s = t; s < kTableSize; s += 256) {
-    uint32_t x = 0;
-#pragma unroll
-    for (uint32_t step = 128; step >= 1; step >>= 1)
-      if (cum_s[x + step] <= s) x += step;
-    tbl[s] = (f_s[x] << 20) | (x << 12) | (s - cum_s[x]);
+  for (int w = 0; w < 4; ++w) woff += (w < warp) ? wred[w] : 0u;
+  const uint32_t total = wred[0] + wred[1] + wred[2] + wred[3];
+  const uint32_t c0 = woff + v - f0 - f1, c1 = c0 + f0;
+  const uint32_t x0 = 2 * t, x1 = 2 * t + 1;
+  sym_word[x0] = ((f0 << 11) | (x0 << 24)) - c0;
+  sym_word[x1] = ((f1 << 11) | (x1 << 24)) - c1;
+  if (total == kTableSize) {  // then every marked slot c < cum + freq <= 2048
+    if (f0) marks[c0] = static_cast<uint8_t>(x0);
+    if (f1) marks[c1] = static_cast<uint8_t>(x1);
   }
+  __syncthreads();
+  if (total != kTableSize) return false;
+  // Thread t owns slots [16t, 16t + 16): running maximum within, then an
+  // exclusive maximum over the preceding threads.
+  const uint4 mk = reinterpret_cast<const uint4 *>(marks)[t];
+  const uint32_t mw[4] = {mk.x, mk.y, mk.z, mk.w};
+  uint32_t own[16], run = 0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    run = max(run, (mw[k >> 2] >> (8 * (k & 3))) & 0xFFu);
+    own[k] = run;
+  }
+  uint32_t incl = run;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+    if (lane >= d) incl = max(incl, n);
+  }
+  if (lane == 31) wred[4 + warp] = incl;
+  uint32_t excl = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+  if (lane == 0) excl = 0;
+  __syncthreads();
+#pragma unroll
+  for (int w = 0; w < 3; ++w)
+    if (w < warp) excl = max(excl, wred[4 + w]);
+  uint32_t e[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) e[k] = sym_word[max(own[k], excl)] + static_cast<uint32_t>(16 * t + k);
+  uint4 *dst = reinterpret_cast<uint4 *>(tbl) + 4 * t;
+  dst[0] = make_uint4(e[0], e[1], e[2], e[3]);
+  dst[1] = make_uint4(e[4], e[5], e[6], e[7]);
+  dst[2] = make_uint4(e[8], e[9], e[10], e[11]);
+  dst[3] = make_uint4(e[12], e[13], e[14], e[15]);
   __syncthreads();
   return true;
 }
@@ -86,11 +126,10 @@ __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t 
 // The stage holds `stage_words` 16-bit words per warp (a launch parameter, the
 // "staging depth" tuning knob), each warp's stage padded by 8 words of slack
 // for the 16-byte alignment of the copy.
+// The table build's 3 KB of scratch lives in the (not yet used) stages.
 struct alignas(16) RansHead {
   uint32_t tbl[kTableSize];
-  uint32_t cum[257];
-  uint32_t f[256];
-  uint32_t wsum[8];
+  uint32_t wred[8];
 };
 constexpr size_t kStageOffset = (sizeof(RansHead) + 15) & ~size_t(15);
 __host__ __device__ constexpr size_t rans_smem_bytes(uint32_t stage_words) {
@@ -128,13 +167,22 @@ __device__ __forceinline__ void stage_range(uint8_t *buf, const uint8_t *a, cons
   __syncwarp();
 }
 
-// Byte offset of table slot (x mod 2048) computed on the FMA pipe as
-// 4x - 8192 (x >> 11), sparing the integer ALU pipe the mask and shift.
-__device__ __forceinline__ uint32_t slot_offset(uint32_t x, uint32_t q) {
-  uint32_t x4, off;
-  asm("mul.lo.u32 %0, %1, 4;" : "=r"(x4) : "r"(x));
-  asm("mad.lo.u32 %0, %1, 4294959104, %2;" : "=r"(off) : "r"(q), "r"(x4));  // 4294959104 = -8192 mod 2^32
-  return off;
+// Integer multiply-adds, kept as such so that they issue to the FMA pipe and
+// leave the integer ALU pipe to the shifts, logic and warp votes.
+__device__ __forceinline__ uint32_t mad_lo(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ uint32_t mad_hi(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ uint32_t mul_hi(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("mul.hi.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
 }
 
 // Decodes one group: ns <= 32 interleaved streams of 256 symbols whose final
@@ -146,16 +194,27 @@ __device__ __forceinline__ uint32_t slot_offset(uint32_t x, uint32_t q) {
 // The top stage_words words of [lo, top) are staged in shared memory; every 16
 // steps, if the next 16 steps could read below the staged words, the warp
 // re-stages the stage_words words below its read pointer (a warp-uniform test;
-// groups that fit never re-stage).  Every lane reads the stage each step at a
-// clamped, always in-bounds index and keeps the word only if it renormalises;
-// a valid stream never reads below its group, and the final read pointer tells
-// if a malformed one did.
+// groups that fit never re-stage).
+//
+// One step, with q = x >> 11 and the table entry e of slot x mod 2048:
+//   x' = q * freq + (s - cum), computed as (q - 2048) * (e' >> 11) + e' with
+//   e' = e mod 2^24 (the freq << 11 term cancels), and the slot's byte offset
+//   4x - 8192 q, all as multiply-adds.  Renormalising lanes read consecutive
+//   words below the read pointer, the lowest lane the lowest address
+//   (ans_decode.cl:133-140); lane l's word lies popc(renormalising lanes >= l)
+//   words below the pointer.  Every lane prefetches, off the dependency chain,
+//   the word d = l (d = 32 for lane 0) below the pointer, so a shuffle from
+//   lane (d mod 32) hands each renormalising lane its word.
+// For a valid stream the read pointer never goes below the staged words; a
+// malformed one is caught at the end of a 16-step run (the pointer is then
+// clamped so that every prefetch stays inside the CTA's shared memory) or by
+// the final pointer.
 template <bool INDEX>
 __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, uint32_t lo, uint32_t top,
                                              const uint32_t *__restrict__ tbl, uint16_t *stage, uint32_t stage_words,
                                              int lane, bool active, uint8_t *__restrict__ out, int32_t suf[8]) {
-  const uint32_t pitch = stage_words + 8;
   const uint8_t *tbl_bytes = reinterpret_cast<const uint8_t *>(tbl);
+  const uint8_t *stage_bytes = reinterpret_cast<const uint8_t *>(stage);
   const int lo16 = static_cast<int>(lo >> 1);
   uint32_t stage_lo = (top - lo > 2u * stage_words) ? top - 2u * stage_words : lo;
   stage_range(reinterpret_cast<uint8_t *>(stage), sec + stage_lo, sec + top, lane);
@@ -164,11 +223,13 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
   int sbase16 = static_cast<int>(stage_lo >> 1) -
                 static_cast<int>((reinterpret_cast<uintptr_t>(sec + stage_lo) & 15) >> 1);
   uint32_t x = active ? reinterpret_cast<const uint32_t *>(sec + top)[lane] : kRansL;
-  int ptr = static_cast<int>(top >> 1);  // word index of the section
-  int sptr = ptr - sbase16;              // the same, relative to the stage
-  const uint32_t lt = lanemask_lt();
+  int ptr = static_cast<int>(top >> 1);      // word index of the section
+  uint32_t s2 = 2u * (ptr - sbase16);        // byte offset of word ptr in the stage
+  const uint32_t pre_off = 0u - 2u * static_cast<uint32_t>(lane == 0 ? 32 : lane);
+  const uint32_t ge = ~lanemask_lt();
+  bool bad = false;
   uint32_t total_sym = 0;
-  int32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0;
+  int32_t s0 = 0, s1 = 0, s2_ = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0;
 #pragma unroll 1
   for (int k = 0; k < 16; ++k) {
     if (ptr - 16 * 32 < static_cast<int>(stage_lo >> 1) && static_cast<int>(stage_lo) > static_cast<int>(lo) &&
@@ -179,43 +240,42 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
       stage_range(reinterpret_cast<uint8_t *>(stage), sec + stage_lo, sec + new_top, lane);
       sbase16 = static_cast<int>(stage_lo >> 1) -
                 static_cast<int>((reinterpret_cast<uintptr_t>(sec + stage_lo) & 15) >> 1);
-      sptr = ptr - sbase16;
+      s2 = 2u * (ptr - sbase16);
+    }
+    if (static_cast<int>(s2) < 0) {  // only a malformed stream gets here
+      bad = true;
+      s2 = 0;
     }
     uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      // Lane l holds the word 32 - l below the read pointer, fetched before
-      // the state update so that it is off the dependency chain.
-      const uint32_t pre = stage[min(static_cast<uint32_t>(sptr - 32 + lane), pitch - 1)];
-      const uint32_t q = x >> 11;
-      const uint32_t e = *reinterpret_cast<const uint32_t *>(tbl_bytes + slot_offset(x, q));
-      x = q * (e >> 20) + (e & 0x7FFu);
+      const uint32_t pre = *reinterpret_cast<const uint16_t *>(stage_bytes + static_cast<int>(s2 + pre_off));
+      const uint32_t qm = mad_hi(x, 1u << 21, 0u - 2048u);                          // q - 2048
+      const uint32_t off = mad_lo(qm, 0u - 8192u, mad_lo(x, 4u, 0u - (1u << 24)));  // 4 (x mod 2048)
+      const uint32_t e = *reinterpret_cast<const uint32_t *>(tbl_bytes + off);
+      const uint32_t ec = e & 0xFFFFFFu;
+      x = mad_lo(mul_hi(ec, 1u << 21), qm, ec);
       const bool need = active && x < kRansL;
       const uint32_t m = __ballot_sync(0xFFFFFFFFu, need);
-      const int total = __popc(m);
-      // ans_decode.cl:133-140: renormalising lanes read consecutive 16-bit
-      // words below the read pointer, the lowest lane the lowest address:
-      // word ptr - total + rank, which lane 32 - total + rank prefetched.
-      const uint32_t v = __shfl_sync(0xFFFFFFFFu, pre, 32 - total + __popc(m & lt));
-      if (need) x = __byte_perm(x, v, 0x1054);
-      sptr -= total;
-      const uint32_t sym = e >> 12;  // symbol in the low byte
-      if (j < 4) w3 = __byte_perm(w3, sym, 0x2104);
-      else if (j < 8) w2 = __byte_perm(w2, sym, 0x2104);
-      else if (j < 12) w1 = __byte_perm(w1, sym, 0x2104);
-      else w0 = __byte_perm(w0, sym, 0x2104);
-      if (INDEX) total_sym += sym & 0xFFu;
+      const uint32_t v = __shfl_sync(0xFFFFFFFFu, pre, __popc(m & ge));
+      if (need) x = mad_lo(x, 65536u, v);
+      s2 = mad_lo(static_cast<uint32_t>(__popc(m)), 0u - 2u, s2);
+      // Steps 16k..16k+15 are positions 255-16k .. 240-16k of this stream
+      // (ans_decode.cl:154-155 stores the symbols in reverse).
+      if (j < 4) w3 = __byte_perm(w3, e, 0x2107);
+      else if (j < 8) w2 = __byte_perm(w2, e, 0x2107);
+      else if (j < 12) w1 = __byte_perm(w1, e, 0x2107);
+      else w0 = __byte_perm(w0, e, 0x2107);
+      if (INDEX) total_sym = mad_hi(e, 256u, total_sym);
     }
-    ptr = sptr + sbase16;
-    // Steps 16k..16k+15 are positions 255-16k .. 240-16k of this stream
-    // (ans_decode.cl:154-155 stores the symbols in reverse).
+    ptr = static_cast<int>(s2 >> 1) + sbase16;
     if (active) *reinterpret_cast<uint4 *>(out + 240 - 16 * k) = make_uint4(w0, w1, w2, w3);
     if (INDEX && (k & 1)) {
       const int mm = k >> 1;
       const int32_t v = static_cast<int32_t>(total_sym) - 4096 * (mm + 1);
       s0 = mm == 0 ? v : s0;
       s1 = mm == 1 ? v : s1;
-      s2 = mm == 2 ? v : s2;
+      s2_ = mm == 2 ? v : s2_;
       s3 = mm == 3 ? v : s3;
       s4 = mm == 4 ? v : s4;
       s5 = mm == 5 ? v : s5;
@@ -224,52 +284,48 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
     }
   }
   if (INDEX) {
-    suf[0] = s0; suf[1] = s1; suf[2] = s2; suf[3] = s3;
+    suf[0] = s0; suf[1] = s1; suf[2] = s2_; suf[3] = s3;
     suf[4] = s4; suf[5] = s5; suf[6] = s6; suf[7] = s7;
   }
   // The lowest word read is the final pointer.
-  return __any_sync(0xFFFFFFFFu, ptr < lo16);
+  return __any_sync(0xFFFFFFFFu, bad || ptr < lo16);
 }
 
-// MINB: CTAs per SM the register allocation must allow (the "blocks per SM"
-// tuning knob; 1 leaves ptxas free, 8 fills the SM with 64 warps).
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) gst_rans_kernel(const uint8_t *__restrict__ cmp,
-                                                             uint8_t *__restrict__ scratch, GstPlanView plan) {
+// One rANS work item: ngroups <= 4 groups of one section, group first_group + w
+// decoded by warp w with `ns` streams (lanes).  `counter` counts the image's
+// finished index groups.  The CTA is 128 threads.
+__device__ __forceinline__ void rans_item(const uint8_t *__restrict__ cmp, uint8_t *__restrict__ scratch,
+                                          uint32_t *err, uint32_t *counter, const GstImageDesc &im,
+                                          uint32_t section, uint32_t first_group, uint32_t ngroups, uint32_t ns,
+                                          uint32_t stage_words) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   RansHead &sm = *reinterpret_cast<RansHead *>(smem_raw);
-
-  const GstRansItem it = plan.rans[blockIdx.x];
-  const GstImageDesc &im = plan.images[it.image];
-  uint32_t *err = plan.err;
-  const uint16_t *freqs = reinterpret_cast<const uint16_t *>(cmp + im.freq_off + kFreqTableBytes * it.section);
-  const bool table_ok = build_decode_table(freqs, sm.tbl, sm.cum, sm.f, sm.wsum);
+  const uint16_t *freqs = reinterpret_cast<const uint16_t *>(cmp + im.freq_off + kFreqTableBytes * section);
+  const bool table_ok = build_decode_table(freqs, sm.tbl, sm.wred, smem_raw + kStageOffset);
   if (!table_ok && threadIdx.x == 0) flag_error(err, kErrTable);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (static_cast<uint32_t>(warp) >= it.ngroups) return;
-  const uint32_t g = it.first_group + warp;
-  const uint32_t G = im.sec_groups[it.section];
-  const uint32_t len = im.sec_len[it.section];
-  const uint8_t *sec = cmp + im.body_off + im.sec_in[it.section];
+  if (static_cast<uint32_t>(warp) >= ngroups) return;
+  const uint32_t g = first_group + warp;
+  const uint32_t G = im.sec_groups[section];
+  const uint32_t len = im.sec_len[section];
+  const uint8_t *sec = cmp + im.body_off + im.sec_in[section];
   const uint32_t *ends = reinterpret_cast<const uint32_t *>(sec);
   const uint32_t hi = ends[g];
   const uint32_t lo = g == 0 ? 4u * G : ends[g - 1];
-  const uint32_t ns = it.streams;
   const bool active = static_cast<uint32_t>(lane) < ns;
   const bool group_ok = table_ok && (hi & 3u) == 0 && (lo & 3u) == 0 && hi <= len && lo <= len &&
                         hi >= lo + 4u * ns;
-  const bool is_index = it.section == 3;
-  uint8_t *out = scratch + im.sym_off + im.sec_out[it.section] + static_cast<size_t>(g) * ns * kSymsPerStream +
+  const bool is_index = section == 3;
+  uint8_t *out = scratch + im.sym_off + im.sec_out[section] + static_cast<size_t>(g) * ns * kSymsPerStream +
                  static_cast<size_t>(lane) * kSymsPerStream;
 
   int32_t suf[8];
   if (group_ok) {
     const uint32_t top = hi - 4u * ns;  // the group's final states sit at [top, hi)
-    uint16_t *stage = reinterpret_cast<uint16_t *>(smem_raw + kStageOffset) + warp * (plan.stage_words + 8);
-    const bool bad = is_index
-                         ? decode_group<true>(sec, lo, top, sm.tbl, stage, plan.stage_words, lane, active, out, suf)
-                         : decode_group<false>(sec, lo, top, sm.tbl, stage, plan.stage_words, lane, active, out, suf);
+    uint16_t *stage = reinterpret_cast<uint16_t *>(smem_raw + kStageOffset) + warp * (stage_words + 8);
+    const bool bad = is_index ? decode_group<true>(sec, lo, top, sm.tbl, stage, stage_words, lane, active, out, suf)
+                              : decode_group<false>(sec, lo, top, sm.tbl, stage, stage_words, lane, active, out, suf);
     if (bad && lane == 0) flag_error(err, kErrStream);
   } else if (lane == 0 && table_ok) {
     flag_error(err, kErrGroup);
@@ -300,28 +356,39 @@ __global__ void __launch_bounds__(256, MINB) gst_rans_kernel(const uint8_t *__re
   if (lane == 31) {
     gsum[g] = incl;
     __threadfence();
-    last = atomicAdd(&plan.counters[it.image], 1u) == G - 1;
+    last = atomicAdd(counter, 1u) == G - 1;
   }
   last = __shfl_sync(0xFFFFFFFFu, last, 31);
   if (!last) return;
   __threadfence();
-  // Every index group of this image is done: re-arm its counter so a resident
-  // plan can be launched again without a re-upload.
-  if (lane == 0) plan.counters[it.image] = 0;
+  // Every index group of this image is done: re-arm the counter so that a
+  // resident plan can be launched again without a re-upload.
+  if (lane == 0) *counter = 0;
   // Exclusive prefix of the G group sums, one warp, 32 at a time.
   int32_t carry = 0;
   for (uint32_t base = 0; base < G; base += 32) {
     const uint32_t i = base + lane;
-    const int32_t s = i < G ? __ldcg(gsum + i) : 0;
-    int32_t v = s;
+    const int32_t sv = i < G ? __ldcg(gsum + i) : 0;
+    int32_t v = sv;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const int32_t n = __shfl_up_sync(0xFFFFFFFFu, v, d);
       if (lane >= d) v += n;
     }
-    if (i < G) gsum[G + i] = carry + v - s;
+    if (i < G) gsum[G + i] = carry + v - sv;
     carry += __shfl_sync(0xFFFFFFFFu, v, 31);
   }
+}
+
+// MINB: CTAs of 128 threads per SM that the register allocation must allow
+// (the "blocks per SM" tuning knob: 8 leaves 64 registers, 12 about 40,
+// 16 fills the SM with 64 warps at 32).
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) gst_rans_kernel(const uint8_t *__restrict__ cmp,
+                                                             uint8_t *__restrict__ scratch, GstPlanView plan) {
+  const GstRansItem it = plan.rans[blockIdx.x];
+  rans_item(cmp, scratch, plan.err, plan.counters + it.image, plan.images[it.image], it.section, it.first_group,
+            it.ngroups, it.streams, plan.stage_words);
 }
 
 // ---------------------------------------------------------------------------
@@ -468,11 +535,11 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
   static bool configured = false;  // per process; the attribute applies to every device context
   if (!configured) {
     const int bytes = static_cast<int>(rans_smem_bytes(kMaxStageWords));
-    cudaError_t e = cudaFuncSetAttribute(gst_rans_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e = cudaFuncSetAttribute(gst_rans_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(gst_rans_kernel<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      e = cudaFuncSetAttribute(gst_rans_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(gst_rans_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      e = cudaFuncSetAttribute(gst_rans_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
     configured = true;
   }
@@ -482,9 +549,9 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
   if (ev) cudaEventRecord(ev[0], stream);
   if (plan.n_rans) {
     const size_t smem = rans_smem_bytes(plan.stage_words);
-    if (tuning.blocks_per_sm >= 7) gst_rans_kernel<8><<<plan.n_rans, 256, smem, stream>>>(d_cmp, d_scratch, plan);
-    else if (tuning.blocks_per_sm == 6) gst_rans_kernel<6><<<plan.n_rans, 256, smem, stream>>>(d_cmp, d_scratch, plan);
-    else gst_rans_kernel<1><<<plan.n_rans, 256, smem, stream>>>(d_cmp, d_scratch, plan);
+    if (tuning.blocks_per_sm >= 14) gst_rans_kernel<16><<<plan.n_rans, 128, smem, stream>>>(d_cmp, d_scratch, plan);
+    else if (tuning.blocks_per_sm >= 10) gst_rans_kernel<12><<<plan.n_rans, 128, smem, stream>>>(d_cmp, d_scratch, plan);
+    else gst_rans_kernel<8><<<plan.n_rans, 128, smem, stream>>>(d_cmp, d_scratch, plan);
     ++*launches;
     if (ev) cudaEventRecord(ev[*launches], stream);
   }
@@ -539,16 +606,10 @@ constexpr size_t kStaticHeaderBytes = 256;  // [status word][index-group counter
 static __device__ __align__(256) uint8_t g_static_scratch[kStaticScratchBytes];
 
 // gst_rans_kernel for a single image whose descriptor arrives by value; the
-// work item is derived from blockIdx (ceil(G/8) CTAs per section, in section
+// work item is derived from blockIdx (ceil(G/4) CTAs per section, in section
 // order).  `base` is g_static_scratch: [status][counter] then the image scratch.
-__global__ void __launch_bounds__(256) gst_rans_static_kernel(const uint8_t *__restrict__ cmp, uint8_t *base,
+__global__ void __launch_bounds__(128) gst_rans_static_kernel(const uint8_t *__restrict__ cmp, uint8_t *base,
                                                               GstImageDesc im) {
-  extern __shared__ __align__(16) uint8_t smem_raw[];
-  RansHead &sm = *reinterpret_cast<RansHead *>(smem_raw);
-  uint32_t *err = reinterpret_cast<uint32_t *>(base);
-  uint32_t *counter = err + 1;
-  uint8_t *scratch = base + kStaticHeaderBytes;
-
   uint32_t b = blockIdx.x, section = 0;
   for (; section < 3; ++section) {
     const uint32_t c = (im.sec_groups[section] + kGroupsPerRansCta - 1) / kGroupsPerRansCta;
@@ -557,78 +618,9 @@ __global__ void __launch_bounds__(256) gst_rans_static_kernel(const uint8_t *__r
   }
   const uint32_t first = b * kGroupsPerRansCta;
   const uint32_t ngroups = min(kGroupsPerRansCta, im.sec_groups[section] - first);
-
-  const uint16_t *freqs = reinterpret_cast<const uint16_t *>(cmp + im.freq_off + kFreqTableBytes * section);
-  const bool table_ok = build_decode_table(freqs, sm.tbl, sm.cum, sm.f, sm.wsum);
-  if (!table_ok && threadIdx.x == 0) flag_error(err, kErrTable);
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (static_cast<uint32_t>(warp) >= ngroups) return;
-  const uint32_t g = first + warp;
-  const uint32_t G = im.sec_groups[section];
-  const uint32_t len = im.sec_len[section];
-  const uint8_t *sec = cmp + im.body_off + im.sec_in[section];
-  const uint32_t *ends = reinterpret_cast<const uint32_t *>(sec);
-  const uint32_t hi = ends[g];
-  const uint32_t lo = g == 0 ? 4u * G : ends[g - 1];
-  const bool group_ok = table_ok && (hi & 3u) == 0 && (lo & 3u) == 0 && hi <= len && lo <= len &&
-                        hi >= lo + 4u * kStreamsPerGroup;
-  const bool is_index = section == 3;
-  uint8_t *out = scratch + im.sym_off + im.sec_out[section] + static_cast<size_t>(g) * kSymsPerGroup +
-                 static_cast<size_t>(lane) * kSymsPerStream;
-
-  int32_t suf[8];
-  if (group_ok) {
-    const uint32_t top = hi - 4u * kStreamsPerGroup;
-    uint16_t *stage = reinterpret_cast<uint16_t *>(smem_raw + kStageOffset) + warp * (kDefaultStageWords + 8);
-    const bool bad =
-        is_index ? decode_group<true>(sec, lo, top, sm.tbl, stage, kDefaultStageWords, lane, true, out, suf)
-                 : decode_group<false>(sec, lo, top, sm.tbl, stage, kDefaultStageWords, lane, true, out, suf);
-    if (bad && lane == 0) flag_error(err, kErrStream);
-  } else if (lane == 0 && table_ok) {
-    flag_error(err, kErrGroup);
-  }
-  if (!is_index) return;
-
-  const int32_t T = group_ok ? suf[7] : 0;
-  int32_t incl = T;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const int32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-    if (lane >= d) incl += n;
-  }
-  if (group_ok) {
-    const int32_t lane_off = incl - T;
-    int32_t pre[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) pre[c] = lane_off + T - suf[7 - c];
-    int32_t *chunk = reinterpret_cast<int32_t *>(scratch + im.chunk_off) + static_cast<size_t>(g) * 256 + lane * 8;
-    reinterpret_cast<int4 *>(chunk)[0] = make_int4(pre[0], pre[1], pre[2], pre[3]);
-    reinterpret_cast<int4 *>(chunk)[1] = make_int4(pre[4], pre[5], pre[6], pre[7]);
-  }
-  int32_t *gsum = reinterpret_cast<int32_t *>(scratch + im.gsum_off);
-  uint32_t last = 0;
-  if (lane == 31) {
-    gsum[g] = incl;
-    __threadfence();
-    last = atomicAdd(counter, 1u) == G - 1;
-  }
-  last = __shfl_sync(0xFFFFFFFFu, last, 31);
-  if (!last) return;
-  __threadfence();
-  int32_t carry = 0;
-  for (uint32_t i0 = 0; i0 < G; i0 += 32) {
-    const uint32_t i = i0 + lane;
-    const int32_t s = i < G ? __ldcg(gsum + i) : 0;
-    int32_t v = s;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const int32_t n = __shfl_up_sync(0xFFFFFFFFu, v, d);
-      if (lane >= d) v += n;
-    }
-    if (i < G) gsum[G + i] = carry + v - s;
-    carry += __shfl_sync(0xFFFFFFFFu, v, 31);
-  }
+  uint32_t *err = reinterpret_cast<uint32_t *>(base);
+  rans_item(cmp, base + kStaticHeaderBytes, err, err + 1, im, section, first, ngroups, kStreamsPerGroup,
+            kDefaultStageWords);
 }
 
 // gst_tile_kernel for a single image whose descriptor arrives by value; the
@@ -793,7 +785,7 @@ extern "C" gst_status gst_load_compressed_dxt_static(const gst_header *hdr, cons
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // Words that must start at zero: the status word and the index-group counter.
   if (cudaMemsetAsync(base, 0, 8, s) != cudaSuccess) return GST_E_CUDA;
-  gst_rans_static_kernel<<<rans_ctas, 256, rans_smem_bytes(kDefaultStageWords), s>>>(
+  gst_rans_static_kernel<<<rans_ctas, 128, rans_smem_bytes(kDefaultStageWords), s>>>(
       static_cast<const uint8_t *>(d_cmp), base, im);
   gst_tile_static_kernel<<<uint32_t(B / 1024), 256, 0, s>>>(base, static_cast<uint8_t *>(d_out), im);
   if (cudaGetLastError() != cudaSuccess) return GST_E_CUDA;

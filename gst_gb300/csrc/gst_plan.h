@@ -7,8 +7,8 @@
 //     in the compressed buffer (offsets as codec/decoder.cpp:132-149 computes
 //     them), where its decoded symbols and index prefixes go in scratch, and
 //     where its DXT1 blocks go in the output;
-//   * the rANS work list: one item per (image, section, run of <= 8 groups of
-//     32 x 256 symbols) -- a CTA of 8 warps, one warp per group;
+//   * the rANS work list: one item per (image, section, run of <= 4 groups of
+//     32 x 256 symbols) -- a CTA of 4 warps, one warp per group;
 //   * the tile work list: one item per (image, 32x32-block wavelet tile).
 // The plan is copied to the device in one cudaMemcpyAsync; it also carries the
 // per-image counters, so the copy resets them for every call.
@@ -22,16 +22,16 @@ constexpr uint32_t kTableSize = 2048;         // M = 2^11           ans/ans.h:73
 constexpr uint32_t kSymsPerStream = 256;      //                    ans/ans.h:74
 constexpr uint32_t kStreamsPerGroup = 32;     //                    ans/ans.h:75
 constexpr uint32_t kSymsPerGroup = 8192;
-constexpr uint32_t kGroupsPerRansCta = 8;
+constexpr uint32_t kGroupsPerRansCta = 4;
 // rANS staging depth per warp, in 16-bit words (a multiple of 8, so that every
 // warp's stage starts 16-byte aligned).  Sixteen steps read at most 512 words
 // and a re-stage starts at most one word above the read pointer, so 520 words
-// always cover the next sixteen steps; 2816 keeps four CTAs per SM.
+// always cover the next sixteen steps; 2816 keeps seven CTAs per SM.
 constexpr uint32_t kMinStageWords = 520, kMaxStageWords = 2816, kDefaultStageWords = 1016;
 
 // Launch configuration of the rANS kernel.
 struct GstTuning {
-  int blocks_per_sm = 6;                       // register budget: 5 (unconstrained), 6 or 8 CTAs per SM
+  int blocks_per_sm = 12;                      // register budget: 8, 12 or 16 CTAs of 128 threads per SM
   uint32_t stage_words = kDefaultStageWords;  // staging depth
   bool operator==(const GstTuning &o) const { return blocks_per_sm == o.blocks_per_sm && stage_words == o.stage_words; }
   bool operator!=(const GstTuning &o) const { return !(*this == o); }

@@ -194,13 +194,14 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
 
 /* Tuning knobs of a context (no counterpart in the reference; its work-group
  * sizes are fixed, codec/decoder.cpp:166-417).  Known names:
- *   "rans_blocks_per_sm"  register budget of the rANS kernel in CTAs of 256
- *                         threads per SM: 1-5 (no constraint), 6 (default)
- *                         or 7-8 (eight).
+ *   "rans_blocks_per_sm"  register budget of the rANS kernel in CTAs of 128
+ *                         threads per SM: 1-9 (eight, 64 registers), 10-13
+ *                         (twelve, default) or 14-16 (sixteen).
  *   "rans_stage_words"    16-bit renormalisation words each warp stages in
  *                         shared memory: a multiple of 8 in [520, 2816];
  *                         default 1016.  Deeper stages re-stage less often
- *                         but leave room for fewer CTAs per SM.
+ *                         but leave room for fewer CTAs per SM (16 CTAs at
+ *                         520 words, 13 at 1016, 8 at 2040).
  * Invalid values and unknown names return GST_E_ARG.  They apply to the
  * context's calls and to resident batches without a tuning of their own;
  * such batches re-capture their graph after a change. */

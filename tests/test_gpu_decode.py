@@ -247,7 +247,7 @@ def test_resident_batch_launch_and_graph_replay(gpu_ctx):
     b.close()
 
 
-TUNINGS = [(8, 520), (8, 1016), (6, 1016), (6, 1528), (4, 2040), (4, 2816), (5, 904)]
+TUNINGS = [(16, 520), (12, 520), (12, 1016), (8, 1528), (8, 2040), (8, 2816), (10, 904)]
 
 
 def test_every_tuning_decodes_identically(gpu_ctx):
@@ -278,7 +278,7 @@ def test_every_tuning_decodes_identically(gpu_ctx):
                 assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
                 assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want), (bps, words, graph)
     finally:
-        gpu_ctx.set_option("rans_blocks_per_sm", 6)
+        gpu_ctx.set_option("rans_blocks_per_sm", 12)
         gpu_ctx.set_option("rans_stage_words", 1016)
         b.close()
 
@@ -300,7 +300,7 @@ def test_batch_autotune_and_tuning_validation(gpu_ctx):
     b.launch(d_cmp, d_out, side, graph=True)
     assert decoder.sync_status(gpu_ctx, side) == decoder.GST_OK
     assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want)
-    for bad in ((6, 512), (6, 1001), (6, 2824), (9, 1016), (0, 1016)):
+    for bad in ((12, 512), (12, 1001), (12, 2824), (17, 1016), (0, 1016)):
         with pytest.raises(decoder.GstError) as ei:
             b.set_tuning(*bad)
         assert ei.value.status == decoder.GST_E_ARG

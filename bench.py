@@ -54,10 +54,13 @@ def parse_args():
     p.add_argument("--impl", choices=("gst", "reference"), default="gst")
     p.add_argument("--skip-extra", action="store_true", help="headline workload only")
     p.add_argument("--cpu-sample", type=int, default=16, help="images of the batch the CPU baseline decodes")
-    p.add_argument("--only", choices=("batched", "large", "plain", "rans"),
+    p.add_argument("--only", choices=("batched", "large", "plain", "rans", "serving"),
                    help="time one workload's decode call only (a small command for profilers)")
     p.add_argument("--rans-blocks-per-sm", type=int, default=0,
                    help="fix the rANS kernel's CTAs of 128 threads per SM (8, 12 or 16) instead of autotuning")
+    p.add_argument("--serve-seconds", type=float, default=2.0,
+                   help="length of each open-loop serving run (the serving config names 60 s)")
+    p.add_argument("--serve-rates", default="1000,5000,20000", help="Poisson arrival rates, requests/s")
     p.add_argument("--rans-stage-words", type=int, default=1016,
                    help="staging depth with --rans-blocks-per-sm (a multiple of 8 in [520, 2816])")
     return p.parse_args()
@@ -254,6 +257,10 @@ def run_only(args, local):
         ctx.set_option("rans_stage_words", args.rans_stage_words)
     stream = torch.cuda.Stream(device)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=device)
+    if args.only == "serving":
+        out = serving(ctx, args)
+        ctx.close()
+        return {"only": "serving", **out}
     if args.only == "rans":
         sec = workloads.rans_section()
         d_f = torch.from_numpy(np.frombuffer(sec.section[:512], np.uint8).copy()).to(device)
@@ -414,6 +421,7 @@ def run_gst(args, rank, world, local):
     }
     if not args.skip_extra:
         line["workloads"] = extra_workloads(ctx, stream, flush, device, peak, args)
+        line["serving"] = serving(ctx, args)
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(images[: args.cpu_sample])
     rb.close()
@@ -466,6 +474,45 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
         "hbm_frac": round(alg / (statistics.mean(t) / 1e3) / 1e9 / peak, 4),
         "bits_per_symbol": round(8 * (len(sec.section) - 512) / sec.symbols.size, 3), "bit_exact": ok,
     }
+    return out
+
+
+def serving(ctx, args) -> dict:
+    """Open-loop Poisson arrivals through the continuous-batching server, and
+    the same arrival trace through per-request plain decodes (one image per
+    launch, one launch at a time).  Sizes w, h from {512, 1024, 2048, 4096}
+    with weights 0.4/0.3/0.2/0.1; a pool of pre-encoded streams; 32 GiB
+    device budget; every 50th result is read back and checked."""
+    from gst_gb300 import workloads
+    from gst_gb300.server import DecodeServer, run_poisson
+    pool = workloads.serving_pool(per_class=2)
+    dims = workloads.SERVING_DIMS
+    weights = np.array([0.4, 0.3, 0.2, 0.1])
+    keys = [(w, h) for w in dims for h in dims]
+    key_p = np.array([weights[dims.index(w)] * weights[dims.index(h)] for w, h in keys])
+    reqs, owner = [], []
+    for k, key in enumerate(keys):
+        for im in pool[key]:
+            reqs.append((im.stream, im.blocks))
+            owner.append(k)
+    by_key = {k: [i for i, o in enumerate(owner) if o == k] for k in range(len(keys))}
+
+    def pick(rng):
+        k = int(rng.choice(len(keys), p=key_p))
+        return by_key[k][int(rng.integers(len(by_key[k])))]
+
+    out = {"config": {"dims": list(dims), "weights": weights.tolist(), "pool_streams": len(reqs),
+                      "device_budget_gib": 32, "seconds_per_rate": args.serve_seconds,
+                      "verify_every": 50}}
+    for rate in [float(r) for r in args.serve_rates.split(",") if r]:
+        row = {}
+        for mode, kw in (("batched", dict(max_inflight=4, max_batch_images=256)),
+                         ("plain", dict(max_inflight=1, max_batch_images=1))):
+            with DecodeServer(ctx, device_budget_bytes=32 << 30, **kw) as srv:
+                run_poisson(srv, reqs, rate, 0.2, seed=7, pick=pick)  # warm-up
+                res = run_poisson(srv, reqs, rate, args.serve_seconds, seed=int(rate), verify_every=50, pick=pick)
+            row[mode] = res.summary()
+        out[f"{int(rate)}_req_s"] = row
     return out
 
 

@@ -25,8 +25,8 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 DECODER_LIB = PKG / "libgst_gb300.so"
 ENCODER_LIB = PKG / "libgst_encoder.so"
 
-DECODER_SOURCES = [CSRC / "gst_kernels.cu", CSRC / "gst_api.cpp"]
-DECODER_HEADERS = [CSRC / "gst_plan.h", INCLUDE / "gst_decoder.h"]
+DECODER_SOURCES = [CSRC / "gst_kernels.cu", CSRC / "gst_api.cpp", CSRC / "gst_server.cpp"]
+DECODER_HEADERS = [CSRC / "gst_plan.h", CSRC / "gst_host.h", INCLUDE / "gst_decoder.h"]
 ENCODER_SOURCES = [CSRC / "gst_encoder.cpp"]
 ENCODER_HEADERS = [CSRC / "gst_encoder.h"]
 
@@ -48,9 +48,9 @@ def _stale(target: Path, deps) -> bool:
 def decoder_cmd() -> list[str]:
     return [
         nvcc_path(), *ARCH_FLAGS, "-lineinfo", "-O3", "-std=c++17",
-        "-Xcompiler", "-fPIC", "-shared",
+        "-Xcompiler", "-fPIC", "-Xcompiler", "-pthread", "-shared",
         f"-I{INCLUDE}", f"-I{CSRC}",
-        *map(str, DECODER_SOURCES), "-o", str(DECODER_LIB),
+        *map(str, DECODER_SOURCES), "-o", str(DECODER_LIB), "-lpthread",
     ]
 
 

@@ -14,19 +14,16 @@
 #include <mutex>
 #include <vector>
 
+#include "gst_host.h"
 #include "gst_plan.h"
-
-namespace gst {
-const char *kernel_name(int i);
-cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, GstPlanView plan,
-                          cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning);
-}
 
 constexpr int kMaxTimedKernels = 4;
 
 using namespace gst;
+using namespace gst::host;
 
-namespace {
+namespace gst {
+namespace host {
 
 constexpr size_t kAlign = 256;
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -59,10 +56,6 @@ uint64_t section_bytes(const gst_header &h) {
   return uint64_t(h.y_cmp_sz) + h.chroma_cmp_sz + h.palette_sz + h.indices_sz;
 }
 
-// Scratch layout of one image: decoded symbols, chunk prefixes, group sums.
-struct ScratchLayout {
-  size_t sym, chunk, gsum, total;
-};
 ScratchLayout scratch_layout(const gst_header &h) {
   const uint64_t B = image_blocks(h);
   ScratchLayout s;
@@ -90,7 +83,8 @@ struct PlanBuf {
   bool used = false;
 };
 
-}  // namespace
+}  // namespace host
+}  // namespace gst
 
 struct gst_ctx {
   int device = 0;
@@ -124,7 +118,8 @@ struct gst_ctx {
   int timed_kernels = 0;
 };
 
-namespace {
+namespace gst {
+namespace host {
 
 gst_status cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return GST_OK;
@@ -215,6 +210,7 @@ gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, size_
   view.rans = reinterpret_cast<const GstRansItem *>(pb->d + off_rans);
   view.tiles = n_tiles ? reinterpret_cast<const GstTileItem *>(pb->d + off_tiles) : nullptr;
   view.counters = reinterpret_cast<uint32_t *>(pb->d + off_counters);
+  view.image_err = nullptr;
   view.n_rans = n_rans;
   view.n_tiles = n_tiles;
   cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
@@ -229,13 +225,6 @@ gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, size_
   return GST_OK;
 }
 
-// Where everything of a plan for these headers goes.
-struct PlanLayout {
-  size_t off_images, off_rans, off_tiles, off_counters, bytes;
-  uint32_t n_rans, n_tiles;
-  size_t scratch_bytes;
-  std::vector<ScratchLayout> lay;
-};
 
 PlanLayout plan_layout(const gst_header *hdrs, int n) {
   PlanLayout L;
@@ -255,14 +244,20 @@ PlanLayout plan_layout(const gst_header *hdrs, int n) {
   L.off_rans = L.off_images + sizeof(GstImageDesc) * n;
   L.off_tiles = align_up(L.off_rans + sizeof(GstRansItem) * L.n_rans, 16);
   L.off_counters = align_up(L.off_tiles + sizeof(GstTileItem) * L.n_tiles, 16);
-  L.bytes = align_up(L.off_counters + 4 * size_t(n), 16);
+  L.off_image_err = L.off_counters + 4 * size_t(n);
+  L.bytes = align_up(L.off_image_err + 4 * size_t(n), 16);
   return L;
 }
 
 // Writes the plan (L.bytes) for n images whose compressed data sit in the
 // reference's layout: codec/decoder.cpp:132-149 and demo/photos_sf.cpp:753-791
-// (offsets page, then 4n frequency tables, then each image's four sections).
-void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph) {
+// (offsets page, then 4n frequency tables, then each image's four sections),
+// and whose DXT1 blocks go back to back.  With stream_at, image i is instead a
+// whole GST stream (header, tables, sections) at device address stream_at[i],
+// and with out_at its blocks go to device address out_at[i]; the kernels then
+// get null compressed and output bases.
+void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph, const uint64_t *stream_at,
+                const uint64_t *out_at) {
   memset(ph, 0, L.bytes);
   GstPlanHead *head = reinterpret_cast<GstPlanHead *>(ph);
   head->n_images = uint32_t(n);
@@ -279,12 +274,12 @@ void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph)
     const gst_header &h = hdrs[i];
     GstImageDesc &d = imgs[i];
     const uint32_t B = uint32_t(image_blocks(h));
-    d.freq_off = page + size_t(i) * 4 * kFreqTableBytes;
-    d.body_off = body;
+    d.freq_off = stream_at ? stream_at[i] + 28 : page + size_t(i) * 4 * kFreqTableBytes;
+    d.body_off = stream_at ? stream_at[i] + 28 + 4 * kFreqTableBytes : body;
     d.sym_off = scratch_off + L.lay[i].sym;
     d.chunk_off = scratch_off + L.lay[i].chunk;
     d.gsum_off = scratch_off + L.lay[i].gsum;
-    d.out_off = out_off;
+    d.out_off = out_at ? out_at[i] : out_off;
     const uint32_t lens[4] = {h.y_cmp_sz, h.chroma_cmp_sz, h.palette_sz, h.indices_sz};
     const uint32_t syms[4] = {2 * B, 4 * B, h.palette_bytes, B};
     uint32_t in = 0, o = 0;
@@ -317,6 +312,7 @@ GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) 
   view.rans = reinterpret_cast<const GstRansItem *>(plan_d + L.off_rans);
   view.tiles = L.n_tiles ? reinterpret_cast<const GstTileItem *>(plan_d + L.off_tiles) : nullptr;
   view.counters = reinterpret_cast<uint32_t *>(plan_d + L.off_counters);
+  view.image_err = reinterpret_cast<uint32_t *>(plan_d + L.off_image_err);
   view.n_rans = L.n_rans;
   view.n_tiles = L.n_tiles;
   return view;
@@ -334,7 +330,7 @@ gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8
   PlanBuf *pb = nullptr;
   st = acquire_plan(ctx, L.bytes, stream, cap, &pb);
   if (st != GST_OK) return st;
-  write_plan(L, hdrs, n, pb->h);
+  write_plan(L, hdrs, n, pb->h, nullptr, nullptr);
   st = upload_and_launch(ctx, pb, L.bytes, L.off_images, L.off_rans, L.off_tiles, L.off_counters, L.n_rans, L.n_tiles,
                          d_cmp, ctx->scratch, d_out, stream, cap);
   if (st != GST_OK) return st;
@@ -360,7 +356,18 @@ gst_status read_device_status(gst_ctx *ctx, cudaStream_t stream) {
   return GST_OK;
 }
 
-}  // namespace
+}  // namespace host
+}  // namespace gst
+
+namespace gst {
+namespace host {
+int ctx_device(const gst_ctx *ctx) { return ctx->device; }
+GstTuning ctx_tuning(gst_ctx *ctx) {
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return ctx->tuning;
+}
+}  // namespace host
+}  // namespace gst
 
 // A resident batch: its plan is uploaded once and it owns its scratch, so a
 // launch enqueues kernels only (and can be captured in a CUDA graph).
@@ -682,7 +689,7 @@ gst_status gst_batch_create(gst_ctx *ctx, const gst_header *hdrs, int n, gst_bat
   b->compressed_bytes = gst_batch_layout_bytes(hdrs, n);
   for (int i = 0; i < n; ++i) b->out_bytes += size_t(image_blocks(hdrs[i])) * 8;
   std::vector<uint8_t> plan(b->layout.bytes);
-  write_plan(b->layout, hdrs, n, plan.data());
+  write_plan(b->layout, hdrs, n, plan.data(), nullptr, nullptr);
   cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&b->plan_d), b->layout.bytes);
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(&b->scratch), std::max<size_t>(b->layout.scratch_bytes, 256));
   if (e == cudaSuccess) e = cudaMemcpy(b->plan_d, plan.data(), b->layout.bytes, cudaMemcpyHostToDevice);

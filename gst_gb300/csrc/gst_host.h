@@ -1,0 +1,52 @@
+// gst_host.h -- host-side helpers shared by the C ABI (gst_api.cpp) and the
+// serving loop (gst_server.cpp).  Internal to the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "gst_decoder.h"
+#include "gst_plan.h"
+
+namespace gst {
+
+// gst_kernels.cu
+const char *kernel_name(int i);
+cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, GstPlanView plan,
+                          cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning);
+
+namespace host {
+
+size_t align_up(size_t x, size_t a);
+gst_status cuda_status(cudaError_t e);
+// Dimension and size rules a header must meet before anything is launched.
+gst_status check_header(const gst_header &h);
+uint64_t image_blocks(const gst_header &h);
+uint64_t section_bytes(const gst_header &h);
+
+// Scratch layout of one image: decoded symbols, chunk prefixes, group sums.
+struct ScratchLayout {
+  size_t sym, chunk, gsum, total;
+};
+ScratchLayout scratch_layout(const gst_header &h);
+
+// Where everything of a plan for these headers goes.
+struct PlanLayout {
+  size_t off_images, off_rans, off_tiles, off_counters, off_image_err, bytes;
+  uint32_t n_rans, n_tiles;
+  size_t scratch_bytes;
+  std::vector<ScratchLayout> lay;
+};
+PlanLayout plan_layout(const gst_header *hdrs, int n);
+void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph, const uint64_t *stream_at,
+                const uint64_t *out_at);
+GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d);
+
+int ctx_device(const gst_ctx *ctx);
+GstTuning ctx_tuning(gst_ctx *ctx);
+
+}  // namespace host
+}  // namespace gst

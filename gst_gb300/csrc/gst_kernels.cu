@@ -38,7 +38,12 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-__device__ __forceinline__ void flag_error(uint32_t *err, uint32_t bits) { atomicOr(err, bits); }
+// Error bits go to the call's status word and, where the plan has them, to the
+// image's own word (so that a batch can report per image).
+__device__ __forceinline__ void flag_error(uint32_t *err, uint32_t *image_err, uint32_t bits) {
+  atomicOr(err, bits);
+  if (image_err) atomicOr(image_err, bits);
+}
 
 // ---------------------------------------------------------------------------
 // Decode table (ans/build_table.cl:12-83).  Slot s in [0, 2048) belongs to the
@@ -293,16 +298,18 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
 
 // One rANS work item: ngroups <= 4 groups of one section, group first_group + w
 // decoded by warp w with `ns` streams (lanes).  `counter` counts the image's
-// finished index groups.  The CTA is 128 threads.
+// finished index groups; image_err (may be null) is the image's error word.
+// The CTA is 128 threads.
 __device__ __forceinline__ void rans_item(const uint8_t *__restrict__ cmp, uint8_t *__restrict__ scratch,
-                                          uint32_t *err, uint32_t *counter, const GstImageDesc &im,
+                                          uint32_t *err, uint32_t *image_err, uint32_t *counter,
+                                          const GstImageDesc &im,
                                           uint32_t section, uint32_t first_group, uint32_t ngroups, uint32_t ns,
                                           uint32_t stage_words) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   RansHead &sm = *reinterpret_cast<RansHead *>(smem_raw);
   const uint16_t *freqs = reinterpret_cast<const uint16_t *>(cmp + im.freq_off + kFreqTableBytes * section);
   const bool table_ok = build_decode_table(freqs, sm.tbl, sm.wred, smem_raw + kStageOffset);
-  if (!table_ok && threadIdx.x == 0) flag_error(err, kErrTable);
+  if (!table_ok && threadIdx.x == 0) flag_error(err, image_err, kErrTable);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (static_cast<uint32_t>(warp) >= ngroups) return;
@@ -326,9 +333,9 @@ __device__ __forceinline__ void rans_item(const uint8_t *__restrict__ cmp, uint8
     uint16_t *stage = reinterpret_cast<uint16_t *>(smem_raw + kStageOffset) + warp * (stage_words + 8);
     const bool bad = is_index ? decode_group<true>(sec, lo, top, sm.tbl, stage, stage_words, lane, active, out, suf)
                               : decode_group<false>(sec, lo, top, sm.tbl, stage, stage_words, lane, active, out, suf);
-    if (bad && lane == 0) flag_error(err, kErrStream);
+    if (bad && lane == 0) flag_error(err, image_err, kErrStream);
   } else if (lane == 0 && table_ok) {
-    flag_error(err, kErrGroup);
+    flag_error(err, image_err, kErrGroup);
   }
 
   if (!is_index) return;
@@ -387,8 +394,8 @@ template <int MINB>
 __global__ void __launch_bounds__(128, MINB) gst_rans_kernel(const uint8_t *__restrict__ cmp,
                                                              uint8_t *__restrict__ scratch, GstPlanView plan) {
   const GstRansItem it = plan.rans[blockIdx.x];
-  rans_item(cmp, scratch, plan.err, plan.counters + it.image, plan.images[it.image], it.section, it.first_group,
-            it.ngroups, it.streams, plan.stage_words);
+  rans_item(cmp, scratch, plan.err, plan.image_err ? plan.image_err + it.image : nullptr, plan.counters + it.image,
+            plan.images[it.image], it.section, it.first_group, it.ngroups, it.streams, plan.stage_words);
 }
 
 // ---------------------------------------------------------------------------
@@ -523,7 +530,8 @@ __global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict
     const uint32_t ep1 = ycocg_to_565(y1, co1, cg1), ep2 = ycocg_to_565(y2, co2, cg2);
     *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) = make_uint2(ep1 | (ep2 << 16), word[i]);
   }
-  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(plan.err, kErrPalette);
+  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0)
+    flag_error(plan.err, plan.image_err ? plan.image_err + it.image : nullptr, kErrPalette);
 }
 
 // Enqueues the decode of one plan.  With `ev` non-null, records ev[0] before
@@ -619,7 +627,7 @@ __global__ void __launch_bounds__(128) gst_rans_static_kernel(const uint8_t *__r
   const uint32_t first = b * kGroupsPerRansCta;
   const uint32_t ngroups = min(kGroupsPerRansCta, im.sec_groups[section] - first);
   uint32_t *err = reinterpret_cast<uint32_t *>(base);
-  rans_item(cmp, base + kStaticHeaderBytes, err, err + 1, im, section, first, ngroups, kStreamsPerGroup,
+  rans_item(cmp, base + kStaticHeaderBytes, err, nullptr, err + 1, im, section, first, ngroups, kStreamsPerGroup,
             kDefaultStageWords);
 }
 
@@ -693,7 +701,7 @@ __global__ void __launch_bounds__(256) gst_tile_static_kernel(const uint8_t *bas
     const uint32_t ep1 = ycocg_to_565(y1, co1, cg1), ep2 = ycocg_to_565(y2, co2, cg2);
     *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) = make_uint2(ep1 | (ep2 << 16), word[i]);
   }
-  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(err, kErrPalette);
+  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(err, nullptr, kErrPalette);
 }
 
 }  // namespace gst

@@ -11,7 +11,7 @@
 //     32 x 256 symbols) -- a CTA of 4 warps, one warp per group;
 //   * the tile work list: one item per (image, 32x32-block wavelet tile).
 // The plan is copied to the device in one cudaMemcpyAsync; it also carries the
-// per-image counters, so the copy resets them for every call.
+// per-image counters and error words, so the copy resets them for every call.
 #pragma once
 
 #include <stdint.h>
@@ -89,7 +89,8 @@ struct GstPlanView {
   const GstImageDesc *images;
   const GstRansItem *rans;
   const GstTileItem *tiles;
-  uint32_t *counters;  // one per image (index-group completion count)
+  uint32_t *counters;   // one per image (index-group completion count)
+  uint32_t *image_err;  // one per image (error bits), or null
   uint32_t n_rans, n_tiles;
   uint32_t stage_words;  // rANS staging depth per warp, in 16-bit words
 };

@@ -46,6 +46,8 @@ EXPORTED_SYMBOLS = (
     "gst_batch_graph_launch", "gst_batch_autotune", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
     "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times", "gst_set_option",
     "gst_status_string",
+    "gst_server_create", "gst_server_destroy", "gst_server_now_ns", "gst_server_submit", "gst_server_poll",
+    "gst_server_read", "gst_server_release", "gst_server_read_stats",
 )
 
 
@@ -55,6 +57,32 @@ class GstError(RuntimeError):
     def __init__(self, status: int, what: str):
         self.status = status
         super().__init__(f"{what}: {STATUS_NAMES.get(status, status)}")
+
+
+class ServerConfig(ctypes.Structure):
+    """gst_server_config."""
+    _fields_ = [("device_budget_bytes", ctypes.c_size_t), ("host_staging_bytes", ctypes.c_size_t),
+                ("slot_scratch_bytes", ctypes.c_size_t), ("max_inflight", ctypes.c_int),
+                ("max_batch_images", ctypes.c_int)]
+
+
+class ServerResult(ctypes.Structure):
+    """gst_server_result."""
+    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int), ("d_dxt", ctypes.c_void_p),
+                ("dxt_bytes", ctypes.c_size_t), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("arrival_ns", ctypes.c_uint64), ("launch_ns", ctypes.c_uint64), ("done_ns", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    """gst_server_stats."""
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "rejected", "launches", "launched_images",
+                                                "pixels", "queued")] + \
+               [("device_bytes_in_use", ctypes.c_size_t), ("device_bytes_peak", ctypes.c_size_t)] + \
+               [(n, ctypes.c_double) for n in ("seconds", "latency_mean_us", "latency_p50_us", "latency_p99_us",
+                                                "latency_max_us")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
 
 
 class GenTCHeader(ctypes.Structure):
@@ -129,6 +157,14 @@ def load_library() -> ctypes.CDLL:
         "gst_set_option": (I, [P, ctypes.c_char_p, I]),
         "gst_kernel_times": (I, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_char_p), I]),
         "gst_status_string": (ctypes.c_char_p, [I]),
+        "gst_server_create": (I, [P, ctypes.POINTER(ServerConfig), ctypes.POINTER(P)]),
+        "gst_server_destroy": (None, [P]),
+        "gst_server_now_ns": (ctypes.c_uint64, [P]),
+        "gst_server_submit": (I, [P, P, S, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
+        "gst_server_poll": (I, [P, ctypes.POINTER(ServerResult), I, ctypes.POINTER(I), I]),
+        "gst_server_read": (I, [P, ctypes.c_uint64, P, S]),
+        "gst_server_release": (I, [P, ctypes.c_uint64]),
+        "gst_server_read_stats": (I, [P, ctypes.POINTER(ServerStats), I]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

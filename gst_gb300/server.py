@@ -1,0 +1,181 @@
+"""Python binding of the continuous-batching decode server (gst_server_* in
+include/gst_decoder.h) and an open-loop Poisson load generator for it.
+
+The server itself is native: a scheduler thread in libgst_gb300.so admits
+requests against a device-memory budget, launches whatever is admitted as one
+batch whenever a launch slot is free, and keeps every result resident on the
+device until it is released.  This module only submits, polls and releases."""
+from __future__ import annotations
+
+import ctypes
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Sequence
+
+import numpy as np
+
+from .decoder import (GST_E_OOM, GST_OK, GPUContext, ServerConfig, ServerResult, ServerStats, _check,
+                      load_library)
+
+
+class DecodeServer:
+    """gst_server_create / gst_server_destroy and friends."""
+
+    def __init__(self, ctx: GPUContext, device_budget_bytes: int = 32 << 30, host_staging_bytes: int = 1 << 30,
+                 slot_scratch_bytes: int = 256 << 20, max_inflight: int = 4, max_batch_images: int = 256):
+        self.ctx = ctx
+        cfg = ServerConfig(device_budget_bytes, host_staging_bytes, slot_scratch_bytes, max_inflight,
+                           max_batch_images)
+        h = ctypes.c_void_p()
+        _check(load_library().gst_server_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)), "gst_server_create")
+        self._h = h
+        self._res = (ServerResult * 1024)()
+
+    def now_ns(self) -> int:
+        return int(load_library().gst_server_now_ns(self._h))
+
+    def submit(self, stream: bytes, arrival_ns: int = 0) -> int | None:
+        """Queues one GST stream; returns its id, or None if the staging is full."""
+        rid = ctypes.c_uint64(0)
+        st = load_library().gst_server_submit(self._h, stream, len(stream), int(arrival_ns), ctypes.byref(rid))
+        if st == GST_E_OOM:
+            return None
+        _check(st, "gst_server_submit")
+        return rid.value
+
+    def poll(self, wait_us: int = 0) -> list[ServerResult]:
+        n = ctypes.c_int(0)
+        _check(load_library().gst_server_poll(self._h, self._res, len(self._res), ctypes.byref(n), int(wait_us)),
+               "gst_server_poll")
+        out = []
+        for i in range(n.value):
+            r = ServerResult()
+            ctypes.pointer(r)[0] = self._res[i]
+            out.append(r)
+        return out
+
+    def read(self, rid: int, nbytes: int) -> np.ndarray:
+        buf = np.empty(nbytes, dtype=np.uint8)
+        _check(load_library().gst_server_read(self._h, rid, buf.ctypes.data, nbytes), "gst_server_read")
+        return buf
+
+    def release(self, rid: int) -> None:
+        _check(load_library().gst_server_release(self._h, rid), "gst_server_release")
+
+    def stats(self, reset: bool = False) -> dict:
+        st = ServerStats()
+        _check(load_library().gst_server_read_stats(self._h, ctypes.byref(st), int(reset)), "gst_server_read_stats")
+        return st.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            load_library().gst_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class LoadResult:
+    rate: float
+    seconds: float
+    submitted: int = 0
+    completed: int = 0
+    rejected: int = 0
+    verified: int = 0
+    mismatched: int = 0
+    errors: int = 0
+    stats: dict = field(default_factory=dict)
+    latencies_us: list = field(default_factory=list)
+
+    def summary(self) -> dict:
+        lat = np.asarray(self.latencies_us) if self.latencies_us else np.zeros(1)
+        s = self.stats
+        return {
+            "rate_req_s": self.rate, "seconds": round(self.seconds, 3),
+            "submitted": self.submitted, "completed": self.completed, "rejected": self.rejected,
+            "throughput_req_s": round(self.completed / self.seconds, 1) if self.seconds else 0.0,
+            "throughput_mpix_s": round(s.get("pixels", 0) / self.seconds / 1e6, 1) if self.seconds else 0.0,
+            "p50_ms": round(float(np.percentile(lat, 50)) / 1e3, 4),
+            "p99_ms": round(float(np.percentile(lat, 99)) / 1e3, 4),
+            "max_ms": round(float(lat.max()) / 1e3, 4),
+            "images_per_launch": round(s.get("launched_images", 0) / max(1, s.get("launches", 0)), 2),
+            "device_bytes_peak": int(s.get("device_bytes_peak", 0)),
+            "verified": self.verified, "bit_exact": self.mismatched == 0 and self.errors == 0,
+        }
+
+
+def run_poisson(server: DecodeServer, requests: Sequence[tuple[bytes, np.ndarray | None]], rate: float,
+                seconds: float, seed: int = 0, verify_every: int = 0,
+                pick: Callable[[np.random.Generator], int] | None = None) -> LoadResult:
+    """Open-loop Poisson arrivals at `rate` requests/s for `seconds`.
+
+    requests: (GST stream, expected DXT1 blocks as uint64 or None); `pick`
+    chooses the next one (uniform by default).  Each request is stamped with
+    its scheduled arrival time, so queueing behind a late submitter counts as
+    latency.  Every `verify_every`-th result is read back and compared with
+    its expected blocks; results are released as soon as they are polled."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.poisson(rate * seconds))
+    arrivals = np.sort(rng.uniform(0.0, seconds, n))
+    choice = [pick(rng) if pick else int(rng.integers(len(requests))) for _ in range(n)]
+    res = LoadResult(rate, seconds)
+    server.poll()
+    server.stats(reset=True)
+    expected = {}
+    t0 = server.now_ns()
+    i = 0
+    outstanding = 0
+    last_done = t0
+
+    def drain(wait_us: int) -> None:
+        nonlocal outstanding, last_done
+        for r in server.poll(wait_us):
+            outstanding -= 1
+            last_done = max(last_done, r.done_ns)
+            res.completed += 1
+            res.latencies_us.append((r.done_ns - r.arrival_ns) / 1e3)
+            if r.status != GST_OK:
+                res.errors += 1
+            want = expected.pop(r.id, None)
+            if want is not None:
+                got = server.read(r.id, r.dxt_bytes).view(np.uint64)
+                res.verified += 1
+                if not np.array_equal(got, want):
+                    res.mismatched += 1
+            server.release(r.id)
+
+    while i < n:
+        now = (server.now_ns() - t0) / 1e9
+        while i < n and arrivals[i] <= now:
+            stream, want = requests[choice[i]]
+            rid = server.submit(stream, t0 + int(arrivals[i] * 1e9))
+            if rid is None:
+                res.rejected += 1
+            else:
+                res.submitted += 1
+                outstanding += 1
+                if verify_every and want is not None and res.submitted % verify_every == 0:
+                    expected[rid] = want
+            i += 1
+        drain(0)
+        if i < n:
+            gap = arrivals[i] - (server.now_ns() - t0) / 1e9
+            if gap > 0.0002:
+                time.sleep(min(gap - 0.0001, 0.002))
+    deadline = time.monotonic() + 60.0
+    while outstanding > 0 and time.monotonic() < deadline:
+        drain(100000)
+    res.seconds = max(seconds, (last_done - t0) / 1e9)
+    res.stats = server.stats()
+    return res

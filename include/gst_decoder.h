@@ -207,6 +207,61 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
  * such batches re-capture their graph after a change. */
 gst_status gst_set_option(gst_ctx *ctx, const char *name, int value);
 
+/* Serving: a continuous-batching decode server (no counterpart in the
+ * reference, whose demos decode fixed pages of pre-packed streams,
+ * demo/photos_sf.cpp:688-830).
+ *   - gst_server_submit copies one whole GST stream (header, tables, sections)
+ *     into pinned host staging and queues it; it returns at once.  The stream
+ *     is validated first (as gst_parse_header).  GST_E_OOM: the staging is
+ *     full (retry later) or the request could never fit the device budget.
+ *     arrival_ns (server clock, gst_server_now_ns) stamps the request's
+ *     arrival for latency; 0 = now.
+ *   - A scheduler thread admits queued requests in arrival order while their
+ *     compressed bytes plus DXT1 output fit in device_budget_bytes, and
+ *     launches everything admitted as one batch whenever one of max_inflight
+ *     launch slots is free; launches run on their own streams and overlap on
+ *     the device, and requests that arrive meanwhile ride in the next launch.
+ *   - gst_server_poll returns finished requests (waiting up to wait_us for
+ *     the first); each result's DXT1 blocks stay resident on the device at
+ *     d_dxt until gst_server_release, which returns its memory to the budget.
+ *     gst_server_read copies one result to host memory (blocking).
+ *   - gst_server_read_stats reports counts and submit-to-finish latency
+ *     percentiles since the last reset (reset != 0 starts a new period).
+ *   - gst_server_destroy waits for the launches in flight and drops requests
+ *     not yet launched.
+ * Each request's result is bit-identical to its plain single-image decode:
+ * images of a launch share nothing but the launch. */
+typedef struct gst_server gst_server;
+typedef struct {
+  size_t device_budget_bytes; /* compressed input + DXT1 output of admitted requests; 0 = 32 GiB */
+  size_t host_staging_bytes;  /* pinned staging of submitted streams; 0 = 1 GiB */
+  size_t slot_scratch_bytes;  /* decode scratch of one launch; a launch takes images while they fit; 0 = 256 MiB */
+  int max_inflight;           /* launches in flight, each on its own stream; 0 = 4 */
+  int max_batch_images;       /* images per launch; 0 = 256; 1 decodes every request alone */
+} gst_server_config;
+typedef struct {
+  uint64_t id;
+  gst_status status; /* GST_E_FORMAT if the kernels met a malformed stream in its launch */
+  void *d_dxt;       /* device address of the DXT1 blocks, valid until gst_server_release */
+  size_t dxt_bytes;
+  uint32_t width, height;
+  uint64_t arrival_ns, launch_ns, done_ns; /* server clock */
+} gst_server_result;
+typedef struct {
+  uint64_t submitted, completed, rejected, launches, launched_images, pixels, queued;
+  size_t device_bytes_in_use, device_bytes_peak;
+  double seconds; /* length of the statistics period */
+  double latency_mean_us, latency_p50_us, latency_p99_us, latency_max_us;
+} gst_server_stats;
+gst_status gst_server_create(gst_ctx *ctx, const gst_server_config *cfg, gst_server **server);
+void gst_server_destroy(gst_server *server);
+uint64_t gst_server_now_ns(gst_server *server);
+gst_status gst_server_submit(gst_server *server, const void *gst, size_t len, uint64_t arrival_ns, uint64_t *id);
+gst_status gst_server_poll(gst_server *server, gst_server_result *out, int cap, int *n, int wait_us);
+gst_status gst_server_read(gst_server *server, uint64_t id, void *dst, size_t cap);
+gst_status gst_server_release(gst_server *server, uint64_t id);
+gst_status gst_server_read_stats(gst_server *server, gst_server_stats *stats, int reset);
+
 /* Human-readable name of a status code. */
 const char *gst_status_string(gst_status s);
 

@@ -1,0 +1,90 @@
+"""Host logic of the serving load generator (gst_gb300.server.run_poisson)
+against a fake server, on the CPU: open-loop arrivals, latency from the
+scheduled arrival time, verification and release of every result."""
+import numpy as np
+
+from gst_gb300 import decoder
+from gst_gb300.server import run_poisson
+
+
+class FakeResult:
+    def __init__(self, rid, arrival, done, nbytes):
+        self.id, self.arrival_ns, self.done_ns, self.dxt_bytes = rid, arrival, done, nbytes
+        self.status = decoder.GST_OK
+        self.launch_ns = arrival
+
+
+class FakeServer:
+    """Completes each request 100 us after its arrival; one output is wrong."""
+
+    def __init__(self, bad_payload=None, capacity=None):
+        import time
+        self._t0 = time.monotonic_ns()
+        self.next_id = 1
+        self.pending = []
+        self.outputs = {}
+        self.released = set()
+        self.bad_payload = bad_payload
+        self.capacity = capacity
+        self.submitted = self.completed = 0
+
+    def now_ns(self):
+        import time
+        return time.monotonic_ns() - self._t0
+
+    def submit(self, stream, arrival_ns=0):
+        if self.capacity is not None and len(self.pending) >= self.capacity:
+            return None
+        rid = self.next_id
+        self.next_id += 1
+        self.pending.append((rid, arrival_ns, stream))
+        self.submitted += 1
+        return rid
+
+    def poll(self, wait_us=0):
+        out = []
+        for rid, arrival, stream in self.pending:
+            payload = self.bad_payload if stream == b"bad" else np.frombuffer(stream, np.uint8).copy()
+            self.outputs[rid] = payload
+            out.append(FakeResult(rid, arrival, arrival + 100_000, payload.size))
+        self.pending = []
+        self.completed += len(out)
+        return out
+
+    def read(self, rid, nbytes):
+        return self.outputs[rid]
+
+    def release(self, rid):
+        assert rid not in self.released
+        self.released.add(rid)
+
+    def stats(self, reset=False):
+        return {"pixels": 0, "launches": 1, "launched_images": self.completed, "device_bytes_peak": 0,
+                "queued": len(self.pending), "submitted": self.submitted, "completed": self.completed}
+
+
+def requests():
+    good = [(bytes(range(i, i + 16)), np.frombuffer(bytes(range(i, i + 16)), np.uint64)) for i in range(4)]
+    return good
+
+
+def test_open_loop_counts_and_latency():
+    srv = FakeServer()
+    res = run_poisson(srv, requests(), rate=4000.0, seconds=0.25, seed=5, verify_every=2)
+    s = res.summary()
+    assert abs(s["submitted"] - 1000) < 150  # Poisson(1000)
+    assert s["completed"] == s["submitted"] and s["rejected"] == 0
+    assert len(srv.released) == s["completed"]
+    assert s["verified"] == s["submitted"] // 2 and s["bit_exact"]
+    assert abs(s["p50_ms"] - 0.1) < 1e-6 and abs(s["p99_ms"] - 0.1) < 1e-6
+
+
+def test_mismatch_and_rejection_are_reported():
+    reqs = requests() + [(b"bad", np.zeros(2, np.uint64))]
+    srv = FakeServer(bad_payload=np.ones(16, np.uint8))
+    res = run_poisson(srv, reqs, rate=2000.0, seconds=0.2, seed=6, verify_every=1,
+                      pick=lambda rng: 4)
+    assert res.mismatched == res.verified > 0 and not res.summary()["bit_exact"]
+    srv2 = FakeServer(capacity=0)
+    res2 = run_poisson(srv2, requests(), rate=2000.0, seconds=0.1, seed=7)
+    assert res2.rejected > 0 and res2.submitted == 0

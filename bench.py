@@ -58,6 +58,8 @@ def parse_args():
                    help="time one workload's decode call only (a small command for profilers)")
     p.add_argument("--rans-blocks-per-sm", type=int, default=0,
                    help="fix the rANS kernel's CTAs of 128 threads per SM (8, 12 or 16) instead of autotuning")
+    p.add_argument("--persistent", type=int, default=0, choices=(0, 1),
+                   help="with --rans-blocks-per-sm: 1 = the persistent single-kernel form")
     p.add_argument("--serve-seconds", type=float, default=2.0,
                    help="length of each open-loop serving run (the serving config names 60 s)")
     p.add_argument("--serve-rates", default="1000,5000,20000", help="Poisson arrival rates, requests/s")
@@ -70,11 +72,11 @@ def tune(rb, b, stream, args) -> dict:
     """The resident batch's rANS launch configuration: fixed by the command
     line, or chosen by gst_batch_autotune (outside any timed region)."""
     if args.rans_blocks_per_sm:
-        rb.set_tuning(args.rans_blocks_per_sm, args.rans_stage_words)
+        rb.set_tuning(args.rans_blocks_per_sm, args.rans_stage_words, args.persistent)
         return {"blocks_per_sm": args.rans_blocks_per_sm, "stage_words": args.rans_stage_words,
-                "chosen_by": "command line"}
-    bps, words = rb.autotune(b.d_cmp, b.d_out, stream, iterations=3)
-    return {"blocks_per_sm": bps, "stage_words": words, "chosen_by": "gst_batch_autotune"}
+                "persistent": args.persistent, "chosen_by": "command line"}
+    bps, words, pers = rb.autotune(b.d_cmp, b.d_out, stream, iterations=3)
+    return {"blocks_per_sm": bps, "stage_words": words, "persistent": pers, "chosen_by": "gst_batch_autotune"}
 
 
 # ---------------------------------------------------------------------------
@@ -255,6 +257,7 @@ def run_only(args, local):
     if args.rans_blocks_per_sm:
         ctx.set_option("rans_blocks_per_sm", args.rans_blocks_per_sm)
         ctx.set_option("rans_stage_words", args.rans_stage_words)
+        ctx.set_option("persistent", args.persistent)
     stream = torch.cuda.Stream(device)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=device)
     if args.only == "serving":

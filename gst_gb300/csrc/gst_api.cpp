@@ -116,6 +116,7 @@ struct gst_ctx {
   bool profiling = false;
   cudaEvent_t ev[kMaxTimedKernels + 1] = {};
   int timed_kernels = 0;
+  const char *timed_names[kMaxTimedKernels] = {};
 };
 
 namespace gst {
@@ -196,25 +197,16 @@ gst_status acquire_scratch(gst_ctx *ctx, size_t bytes, cudaStream_t stream, bool
   return grow_device(&ctx->scratch, &ctx->scratch_cap, bytes);
 }
 
-// Uploads the plan staged in pb->h and launches the kernels on it.
-gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, size_t off_images, size_t off_rans,
-                             size_t off_tiles, size_t off_counters, uint32_t n_rans, uint32_t n_tiles,
+// Uploads the plan staged in pb->h (plan_bytes) and launches the kernels on
+// `view`, whose pointers lie in pb->d.
+gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, const GstPlanView &view,
                              const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, cudaStream_t stream,
                              bool cap) {
   cudaError_t e = cudaMemcpyAsync(pb->d, pb->h, plan_bytes, cudaMemcpyHostToDevice, stream);
   if (e != cudaSuccess) return cuda_status(e);
   if (!cap) cudaEventRecord(pb->copied, stream);
-  GstPlanView view;
-  view.err = ctx->status_d;
-  view.images = reinterpret_cast<const GstImageDesc *>(pb->d + off_images);
-  view.rans = reinterpret_cast<const GstRansItem *>(pb->d + off_rans);
-  view.tiles = n_tiles ? reinterpret_cast<const GstTileItem *>(pb->d + off_tiles) : nullptr;
-  view.counters = reinterpret_cast<uint32_t *>(pb->d + off_counters);
-  view.image_err = nullptr;
-  view.n_rans = n_rans;
-  view.n_tiles = n_tiles;
   cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
-  e = launch_decode(d_cmp, d_scratch, d_out, view, stream, &ctx->last_launches, ev, ctx->tuning);
+  e = launch_decode(d_cmp, d_scratch, d_out, view, stream, &ctx->last_launches, ev, ctx->tuning, ctx->timed_names);
   ctx->timed_kernels = ev ? ctx->last_launches : 0;
   if (e != cudaSuccess) return cuda_status(e);
   if (!cap) {
@@ -224,7 +216,6 @@ gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, size_
   }
   return GST_OK;
 }
-
 
 PlanLayout plan_layout(const gst_header *hdrs, int n) {
   PlanLayout L;
@@ -245,7 +236,9 @@ PlanLayout plan_layout(const gst_header *hdrs, int n) {
   L.off_tiles = align_up(L.off_rans + sizeof(GstRansItem) * L.n_rans, 16);
   L.off_counters = align_up(L.off_tiles + sizeof(GstTileItem) * L.n_tiles, 16);
   L.off_image_err = L.off_counters + 4 * size_t(n);
-  L.bytes = align_up(L.off_image_err + 4 * size_t(n), 16);
+  L.off_sync = align_up(L.off_image_err + 4 * size_t(n), 16);
+  L.bytes = align_up(L.off_sync + 16 + 4 * size_t(n), 16);
+  L.n_images = n;
   return L;
 }
 
@@ -313,6 +306,8 @@ GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) 
   view.tiles = L.n_tiles ? reinterpret_cast<const GstTileItem *>(plan_d + L.off_tiles) : nullptr;
   view.counters = reinterpret_cast<uint32_t *>(plan_d + L.off_counters);
   view.image_err = reinterpret_cast<uint32_t *>(plan_d + L.off_image_err);
+  view.sync = reinterpret_cast<uint32_t *>(plan_d + L.off_sync);
+  view.n_images = uint32_t(L.n_images);
   view.n_rans = L.n_rans;
   view.n_tiles = L.n_tiles;
   return view;
@@ -331,8 +326,9 @@ gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8
   st = acquire_plan(ctx, L.bytes, stream, cap, &pb);
   if (st != GST_OK) return st;
   write_plan(L, hdrs, n, pb->h, nullptr, nullptr);
-  st = upload_and_launch(ctx, pb, L.bytes, L.off_images, L.off_rans, L.off_tiles, L.off_counters, L.n_rans, L.n_tiles,
-                         d_cmp, ctx->scratch, d_out, stream, cap);
+  GstPlanView view = plan_view(L, pb->d, ctx->status_d);
+  view.image_err = nullptr;  // the context reports per call
+  st = upload_and_launch(ctx, pb, L.bytes, view, d_cmp, ctx->scratch, d_out, stream, cap);
   if (st != GST_OK) return st;
   if (!cap) {
     cudaEventRecord(ctx->scratch_done, stream);
@@ -351,7 +347,7 @@ gst_status read_device_status(gst_ctx *ctx, cudaStream_t stream) {
   if (bits) {
     e = cudaMemset(ctx->status_d, 0, sizeof(uint32_t));
     if (e != cudaSuccess) return cuda_status(e);
-    return GST_E_FORMAT;
+    return (bits & kErrTimeout) ? GST_E_TIMEOUT : GST_E_FORMAT;
   }
   return GST_OK;
 }
@@ -390,9 +386,9 @@ namespace {
 
 GstTuning batch_tuning(const gst_batch *b) { return b->tuned ? b->tuning : b->ctx->tuning; }
 
-bool valid_tuning(int blocks_per_sm, int stage_words) {
+bool valid_tuning(int blocks_per_sm, int stage_words, int persistent = 0) {
   return blocks_per_sm >= 1 && blocks_per_sm <= 16 && stage_words >= int(kMinStageWords) &&
-         stage_words <= int(kMaxStageWords) && (stage_words & 7) == 0;
+         stage_words <= int(kMaxStageWords) && (stage_words & 7) == 0 && (persistent == 0 || persistent == 1);
 }
 
 // Launches the batch's kernels under `t`; the caller holds ctx->mu.
@@ -400,7 +396,8 @@ cudaError_t batch_launch_locked(gst_batch *b, const void *d_cmp, void *d_out, cu
                                 cudaEvent_t *ev) {
   gst_ctx *ctx = b->ctx;
   return launch_decode(static_cast<const uint8_t *>(d_cmp), b->scratch, static_cast<uint8_t *>(d_out),
-                       plan_view(b->layout, b->plan_d, ctx->status_d), st, &ctx->last_launches, ev, t);
+                       plan_view(b->layout, b->plan_d, ctx->status_d), st, &ctx->last_launches, ev, t,
+                       ctx->timed_names);
 }
 
 }  // namespace
@@ -670,8 +667,14 @@ gst_status gst_decode_rans_groups(gst_ctx *ctx, const void *d_freqs, const void 
   GstRansItem *rans = reinterpret_cast<GstRansItem *>(ph + off_rans);
   for (uint32_t g = 0, r = 0; g < n_groups; g += kGroupsPerRansCta, ++r)
     rans[r] = {0u, 0u, g, uint16_t(std::min(kGroupsPerRansCta, n_groups - g)), uint16_t(streams_per_group)};
-  return upload_and_launch(ctx, pb, plan_bytes, off_images, off_rans, 0, off_counters, n_rans, 0, nullptr, nullptr,
-                           nullptr, st, cap);
+  GstPlanView view = {};
+  view.err = ctx->status_d;
+  view.images = reinterpret_cast<const GstImageDesc *>(pb->d + off_images);
+  view.rans = reinterpret_cast<const GstRansItem *>(pb->d + off_rans);
+  view.counters = reinterpret_cast<uint32_t *>(pb->d + off_counters);
+  view.n_images = 1;
+  view.n_rans = n_rans;  // no sync words: always the rANS kernel alone
+  return upload_and_launch(ctx, pb, plan_bytes, view, nullptr, nullptr, nullptr, st, cap);
 }
 
 gst_status gst_batch_create(gst_ctx *ctx, const gst_header *hdrs, int n, gst_batch **out) {
@@ -782,34 +785,42 @@ gst_status gst_set_option(gst_ctx *ctx, const char *name, int value) {
     ctx->tuning.stage_words = uint32_t(value);
     return GST_OK;
   }
+  if (strcmp(name, "persistent") == 0) {
+    if (value != 0 && value != 1) return GST_E_ARG;
+    ctx->tuning.persistent = value;
+    return GST_OK;
+  }
   return GST_E_ARG;
 }
 
-gst_status gst_batch_set_tuning(gst_batch *b, int blocks_per_sm, int stage_words) {
+gst_status gst_batch_set_tuning(gst_batch *b, int blocks_per_sm, int stage_words, int persistent) {
   if (!b) return GST_E_ARG;
   if (blocks_per_sm == 0 && stage_words == 0) {  // back to the context's configuration
     b->tuned = false;
     return GST_OK;
   }
-  if (!valid_tuning(blocks_per_sm, stage_words)) return GST_E_ARG;
+  if (!valid_tuning(blocks_per_sm, stage_words, persistent)) return GST_E_ARG;
   std::lock_guard<std::mutex> lock(b->ctx->mu);
   b->tuning.blocks_per_sm = blocks_per_sm;
   b->tuning.stage_words = uint32_t(stage_words);
+  b->tuning.persistent = persistent;
   b->tuned = true;
   return GST_OK;
 }
 
 gst_status gst_batch_autotune(gst_batch *b, const void *d_cmp, void *d_out, void *stream, int iterations,
-                              int *blocks_per_sm, int *stage_words) {
+                              int *blocks_per_sm, int *stage_words, int *persistent) {
   if (!b || !d_cmp || !d_out || iterations < 1) return GST_E_ARG;
   if ((reinterpret_cast<uintptr_t>(d_cmp) & 15) || (reinterpret_cast<uintptr_t>(d_out) & 7)) return GST_E_ARG;
   gst_ctx *ctx = b->ctx;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (capturing(st)) return GST_E_ARG;
-  // CTAs per SM x staging depth: the deepest stages that the shared memory
-  // of that many CTAs per SM holds, and shallower ones.
+  // Two kernels: CTAs per SM x staging depth, the deepest stages that the
+  // shared memory of that many CTAs per SM holds and shallower ones.  The
+  // persistent kernel: its tile buffers fit 2040-word stages at 8 CTAs per SM.
   static const GstTuning kCandidates[] = {
-      {16, 520}, {12, 520}, {12, 1016}, {8, 1528}, {8, 2040}, {8, 2816},
+      {16, 520, 0}, {12, 520, 0}, {12, 1016, 0}, {8, 1528, 0}, {8, 2040, 0}, {8, 2816, 0},
+      {8, 1016, 1}, {8, 2040, 1},
   };
   std::lock_guard<std::mutex> lock(ctx->mu);
   cudaSetDevice(ctx->device);
@@ -841,6 +852,7 @@ gst_status gst_batch_autotune(gst_batch *b, const void *d_cmp, void *d_out, void
   b->tuned = true;
   if (blocks_per_sm) *blocks_per_sm = best.blocks_per_sm;
   if (stage_words) *stage_words = int(best.stage_words);
+  if (persistent) *persistent = best.persistent;
   return GST_OK;
 }
 
@@ -877,7 +889,7 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap) {
   if (cudaEventSynchronize(ctx->ev[n]) != cudaSuccess) return 0;
   for (int i = 0; i < n; ++i) {
     if (cudaEventElapsedTime(&ms[i], ctx->ev[i], ctx->ev[i + 1]) != cudaSuccess) return 0;
-    if (names) names[i] = gst::kernel_name(ctx->last_launches == 1 ? 0 : i);
+    if (names) names[i] = ctx->timed_names[i];
   }
   return n;
 }

@@ -14,9 +14,11 @@
 namespace gst {
 
 // gst_kernels.cu
-const char *kernel_name(int i);
+// Enqueues the kernels of one plan; names (may be null) receives the name of
+// each kernel launched, in order.
 cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, GstPlanView plan,
-                          cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning);
+                          cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning,
+                          const char **names = nullptr);
 
 namespace host {
 
@@ -35,7 +37,8 @@ ScratchLayout scratch_layout(const gst_header &h);
 
 // Where everything of a plan for these headers goes.
 struct PlanLayout {
-  size_t off_images, off_rans, off_tiles, off_counters, off_image_err, bytes;
+  size_t off_images, off_rans, off_tiles, off_counters, off_image_err, off_sync, bytes;
+  int n_images;
   uint32_t n_rans, n_tiles;
   size_t scratch_bytes;
   std::vector<ScratchLayout> lay;

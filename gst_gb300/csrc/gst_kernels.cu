@@ -28,6 +28,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "gst_plan.h"
 
 namespace gst {
@@ -296,24 +298,15 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
   return __any_sync(0xFFFFFFFFu, bad || ptr < lo16);
 }
 
-// One rANS work item: ngroups <= 4 groups of one section, group first_group + w
-// decoded by warp w with `ns` streams (lanes).  `counter` counts the image's
+// Group g of `section`, decoded by one warp with `ns` streams (lanes) against
+// the table in `tbl`, staging through `stage`.  `counter` counts the image's
 // finished index groups; image_err (may be null) is the image's error word.
-// The CTA is 128 threads.
-__device__ __forceinline__ void rans_item(const uint8_t *__restrict__ cmp, uint8_t *__restrict__ scratch,
-                                          uint32_t *err, uint32_t *image_err, uint32_t *counter,
-                                          const GstImageDesc &im,
-                                          uint32_t section, uint32_t first_group, uint32_t ngroups, uint32_t ns,
-                                          uint32_t stage_words) {
-  extern __shared__ __align__(16) uint8_t smem_raw[];
-  RansHead &sm = *reinterpret_cast<RansHead *>(smem_raw);
-  const uint16_t *freqs = reinterpret_cast<const uint16_t *>(cmp + im.freq_off + kFreqTableBytes * section);
-  const bool table_ok = build_decode_table(freqs, sm.tbl, sm.wred, smem_raw + kStageOffset);
-  if (!table_ok && threadIdx.x == 0) flag_error(err, image_err, kErrTable);
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (static_cast<uint32_t>(warp) >= ngroups) return;
-  const uint32_t g = first_group + warp;
+__device__ __forceinline__ void rans_group(const uint8_t *__restrict__ cmp, uint8_t *__restrict__ scratch,
+                                           uint32_t *err, uint32_t *image_err, uint32_t *counter,
+                                           const GstImageDesc &im, uint32_t section, uint32_t g, uint32_t ns,
+                                           bool table_ok, const uint32_t *tbl, uint16_t *stage,
+                                           uint32_t stage_words) {
+  const int lane = threadIdx.x & 31;
   const uint32_t G = im.sec_groups[section];
   const uint32_t len = im.sec_len[section];
   const uint8_t *sec = cmp + im.body_off + im.sec_in[section];
@@ -330,9 +323,8 @@ __device__ __forceinline__ void rans_item(const uint8_t *__restrict__ cmp, uint8
   int32_t suf[8];
   if (group_ok) {
     const uint32_t top = hi - 4u * ns;  // the group's final states sit at [top, hi)
-    uint16_t *stage = reinterpret_cast<uint16_t *>(smem_raw + kStageOffset) + warp * (stage_words + 8);
-    const bool bad = is_index ? decode_group<true>(sec, lo, top, sm.tbl, stage, stage_words, lane, active, out, suf)
-                              : decode_group<false>(sec, lo, top, sm.tbl, stage, stage_words, lane, active, out, suf);
+    const bool bad = is_index ? decode_group<true>(sec, lo, top, tbl, stage, stage_words, lane, active, out, suf)
+                              : decode_group<false>(sec, lo, top, tbl, stage, stage_words, lane, active, out, suf);
     if (bad && lane == 0) flag_error(err, image_err, kErrStream);
   } else if (lane == 0 && table_ok) {
     flag_error(err, image_err, kErrGroup);
@@ -387,6 +379,25 @@ __device__ __forceinline__ void rans_item(const uint8_t *__restrict__ cmp, uint8
   }
 }
 
+// One rANS work item: ngroups <= 4 groups of one section, group first_group + w
+// decoded by warp w.  The CTA is 128 threads; all of them return.
+__device__ __forceinline__ void rans_item(const uint8_t *__restrict__ cmp, uint8_t *__restrict__ scratch,
+                                          uint32_t *err, uint32_t *image_err, uint32_t *counter,
+                                          const GstImageDesc &im, uint32_t section, uint32_t first_group,
+                                          uint32_t ngroups, uint32_t ns, uint32_t stage_words) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  RansHead &sm = *reinterpret_cast<RansHead *>(smem_raw);
+  const uint16_t *freqs = reinterpret_cast<const uint16_t *>(cmp + im.freq_off + kFreqTableBytes * section);
+  const bool table_ok = build_decode_table(freqs, sm.tbl, sm.wred, smem_raw + kStageOffset);
+  if (!table_ok && threadIdx.x == 0) flag_error(err, image_err, kErrTable);
+  const uint32_t warp = threadIdx.x >> 5;
+  if (warp < ngroups) {
+    uint16_t *stage = reinterpret_cast<uint16_t *>(smem_raw + kStageOffset) + warp * (stage_words + 8);
+    rans_group(cmp, scratch, err, image_err, counter, im, section, first_group + warp, ns, table_ok, sm.tbl, stage,
+               stage_words);
+  }
+}
+
 // MINB: CTAs of 128 threads per SM that the register allocation must allow
 // (the "blocks per SM" tuning knob: 8 leaves 64 registers, 12 about 40,
 // 16 fills the SM with 64 warps at 32).
@@ -425,16 +436,18 @@ __device__ __forceinline__ void inv53_line(int32_t *p, int step) {
 constexpr int kPlanePitch = 33;  // row pitch in words: rows and columns both bank-conflict free
 constexpr int kPlaneWords = 32 * kPlanePitch;
 
-// One level over the top-left L x L of all six planes: rows, then columns.
-template <int L>
+// One level over the top-left L x L of all six planes: rows, then columns;
+// NT threads take the 6L lines of each pass.
+template <int L, int NT>
 __device__ __forceinline__ void inv53_level(int32_t *pl) {
-  const int t = threadIdx.x;
-  if (t < 6 * L) {
+#pragma unroll
+  for (int t = threadIdx.x; t < 6 * L; t += NT) {
     const int p = t / L, r = t % L;
     inv53_line<L>(pl + p * kPlaneWords + r * kPlanePitch, 1);
   }
   __syncthreads();
-  if (t < 6 * L) {
+#pragma unroll
+  for (int t = threadIdx.x; t < 6 * L; t += NT) {
     const int p = t / L, c = t % L;
     inv53_line<L>(pl + p * kPlaneWords + c, kPlanePitch);
   }
@@ -450,55 +463,75 @@ __device__ __forceinline__ uint32_t ycocg_to_565(int y, int co, int cg) {
   return ((static_cast<uint32_t>(r) << 11) | (static_cast<uint32_t>(g) << 5) | static_cast<uint32_t>(b)) & 0xFFFFu;
 }
 
-__global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict__ scratch, uint8_t *__restrict__ out,
-                                                       GstPlanView plan) {
-  __shared__ int32_t pl[6 * kPlaneWords];
-  const GstTileItem it = plan.tiles[blockIdx.x];
-  const GstImageDesc &im = plan.images[it.image];
+// Loads of decoded symbols: through the read-only path when another kernel
+// wrote them (COH false), coherently at L2 when CTAs of the same kernel did.
+template <bool COH, typename T>
+__device__ __forceinline__ T ld_sym(const T *p) {
+  if constexpr (COH) return __ldcg(p);
+  else return __ldg(p);
+}
+
+constexpr size_t kTileSmemBytes = 6 * kPlaneWords * sizeof(int32_t);
+
+// One 32x32-block tile of one image with NT threads; `pl` is kTileSmemBytes
+// of shared memory.  All threads return.
+template <int NT, bool COH>
+__device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, uint8_t *__restrict__ out,
+                                          uint32_t *err, uint32_t *image_err, const GstImageDesc &im,
+                                          uint32_t tile, int32_t *pl) {
+  constexpr int kWarps = NT / 32;
+  constexpr int kRows = 32 / kWarps;            // block rows a warp assembles
+  constexpr int kChunks = (384 + NT - 1) / NT;  // 16-byte plane chunks a thread loads
   const size_t B = static_cast<size_t>(im.bx) * im.by;
-  const uint32_t tx = it.tile % im.tiles_x, ty = it.tile / im.tiles_x;
+  const uint32_t tx = tile % im.tiles_x, ty = tile / im.tiles_x;
   const uint8_t *sym = scratch + im.sym_off;
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
 
   // 1. The tile's 1024 coefficients of plane p are the tile-th 1024-byte run of
   //    the plane (inverse_wavelet.cl:79-104); planes Y1 Y2 Co1 Cg1 Co2 Cg2 are
-  //    consecutive B-byte runs of the decoded Y and chroma sections.  384
-  //    16-byte chunks, one or two per thread.
-  const uint8_t *tile_base = sym + static_cast<size_t>(it.tile) * 1024;
-  const uint4 c0 = __ldg(reinterpret_cast<const uint4 *>(tile_base + (t >> 6) * B) + (t & 63));
-  uint4 c1 = make_uint4(0, 0, 0, 0);
-  if (t < 128) c1 = __ldg(reinterpret_cast<const uint4 *>(tile_base + ((t + 256) >> 6) * B) + ((t + 256) & 63));
+  //    consecutive B-byte runs of the decoded Y and chroma sections: 384
+  //    16-byte chunks.
+  const uint8_t *tile_base = sym + static_cast<size_t>(tile) * 1024;
+  uint4 c[kChunks];
+#pragma unroll
+  for (int k = 0; k < kChunks; ++k) {
+    const int chunk = t + k * NT;
+    c[k] = make_uint4(0, 0, 0, 0);
+    if (chunk < 384) c[k] = ld_sym<COH>(reinterpret_cast<const uint4 *>(tile_base + (chunk >> 6) * B) + (chunk & 63));
+  }
 
-  // 2. Palette indices of the four rows this thread assembles (rows warp+8i,
+  // 2. Palette indices of the rows this thread assembles (rows warp + kWarps i,
   //    column lane): loads first, so that they overlap the wavelet.
   const int32_t *chunk_pref = reinterpret_cast<const int32_t *>(scratch + im.chunk_off);
   const int32_t *gpref = reinterpret_cast<const int32_t *>(scratch + im.gsum_off) + im.sec_groups[3];
   const uint8_t *deltas = sym + im.sec_out[3];
-  uint32_t d[4], base[4];
+  uint32_t d[kRows], base[kRows];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const uint32_t p0 = (ty * 32 + warp + 8 * i) * im.bx + tx * 32;  // first block of the row segment
-    d[i] = static_cast<uint32_t>(__ldg(deltas + p0 + lane)) - 128u;
-    base[i] = static_cast<uint32_t>(__ldg(gpref + (p0 >> 13))) + static_cast<uint32_t>(__ldg(chunk_pref + (p0 >> 5)));
+  for (int i = 0; i < kRows; ++i) {
+    const uint32_t p0 = (ty * 32 + warp + kWarps * i) * im.bx + tx * 32;  // first block of the row segment
+    d[i] = static_cast<uint32_t>(ld_sym<COH>(deltas + p0 + lane)) - 128u;
+    base[i] = static_cast<uint32_t>(ld_sym<COH>(gpref + (p0 >> 13))) +
+              static_cast<uint32_t>(ld_sym<COH>(chunk_pref + (p0 >> 5)));
   }
 
   // 3. Coefficients to int32 (byte - 128), rows of pitch kPlanePitch.
-  auto unpack = [&](uint4 c, int chunk) {
-    const int p = chunk >> 6, q = chunk & 63;          // plane, 16-byte chunk in the plane's block
+  auto unpack = [&](uint4 cv, int chunk) {
+    const int p = chunk >> 6, q = chunk & 63;  // plane, 16-byte chunk in the plane's block
     int32_t *dst = pl + p * kPlaneWords + (q >> 1) * kPlanePitch + (q & 1) * 16;
-    const uint32_t w[4] = {c.x, c.y, c.z, c.w};
+    const uint32_t w[4] = {cv.x, cv.y, cv.z, cv.w};
 #pragma unroll
     for (int k = 0; k < 16; ++k) dst[k] = static_cast<int32_t>((w[k >> 2] >> (8 * (k & 3))) & 0xFFu) - 128;
   };
-  unpack(c0, t);
-  if (t < 128) unpack(c1, t + 256);
+#pragma unroll
+  for (int k = 0; k < kChunks; ++k)
+    if (t + k * NT < 384) unpack(c[k], t + k * NT);
 
   // 4. Finish the index prefix sums (warp scans) and start the palette gathers.
   const uint32_t *pal = reinterpret_cast<const uint32_t *>(sym + im.sec_out[2]);
-  uint32_t word[4];
+  uint32_t word[kRows];
   bool bad = false;
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < kRows; ++i) {
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, d[i], o);
@@ -506,22 +539,22 @@ __global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict
     }
     const uint32_t idx = base[i] + d[i];
     word[i] = 0;
-    if (idx < im.palette_words) word[i] = __ldg(pal + idx);
+    if (idx < im.palette_words) word[i] = ld_sym<COH>(pal + idx);
     else bad = true;
   }
   __syncthreads();
 
   // 5. Five levels of the inverse 5/3 wavelet.
-  inv53_level<2>(pl);
-  inv53_level<4>(pl);
-  inv53_level<8>(pl);
-  inv53_level<16>(pl);
-  inv53_level<32>(pl);
+  inv53_level<2, NT>(pl);
+  inv53_level<4, NT>(pl);
+  inv53_level<8, NT>(pl);
+  inv53_level<16, NT>(pl);
+  inv53_level<32, NT>(pl);
 
   // 6. YCoCg667 -> RGB565 endpoints and whole 8-byte DXT1 blocks.
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int r = warp + 8 * i;
+  for (int i = 0; i < kRows; ++i) {
+    const int r = warp + kWarps * i;
     const uint32_t p = (ty * 32 + r) * im.bx + tx * 32 + lane;
     const int32_t *row = pl + r * kPlanePitch + lane;
     const int y1 = static_cast<int8_t>(row[0]), y2 = static_cast<int8_t>(row[kPlaneWords]);
@@ -530,15 +563,109 @@ __global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict
     const uint32_t ep1 = ycocg_to_565(y1, co1, cg1), ep2 = ycocg_to_565(y2, co2, cg2);
     *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) = make_uint2(ep1 | (ep2 << 16), word[i]);
   }
-  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0)
-    flag_error(plan.err, plan.image_err ? plan.image_err + it.image : nullptr, kErrPalette);
+  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(err, image_err, kErrPalette);
+}
+
+__global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict__ scratch, uint8_t *__restrict__ out,
+                                                       GstPlanView plan) {
+  __shared__ int32_t pl[6 * kPlaneWords];
+  const GstTileItem it = plan.tiles[blockIdx.x];
+  tile_work<256, false>(scratch, out, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
+                        plan.images[it.image], it.tile, pl);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent form: one launch of CTAs that drain the whole plan as a work
+// queue -- first every rANS item, then every tile -- so that tiles of images
+// whose groups are done run beside the remaining rANS work instead of after
+// the last of it.  A tile item waits (bounded) until its image's groups are
+// all decoded.  Every item a tile can wait for was taken from the queue
+// before the tile and is held by a running CTA that never waits, so the
+// waits end whether or not all CTAs are resident.  The last CTA to finish
+// re-arms the queue and the counters, so a resident plan can be relaunched.
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // a tile waits at most 2 s for its image
+constexpr uint32_t kWaitLimitSpins = 1u << 24;
+
+__host__ __device__ constexpr size_t persistent_smem_bytes(uint32_t stage_words) {
+  return rans_smem_bytes(stage_words) > kTileSmemBytes ? rans_smem_bytes(stage_words) : kTileSmemBytes;
+}
+
+__global__ void __launch_bounds__(128, 8) gst_persistent_kernel(const uint8_t *__restrict__ cmp,
+                                                                uint8_t *__restrict__ scratch,
+                                                                uint8_t *__restrict__ out, GstPlanView plan) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  __shared__ uint32_t item_s, ok_s;
+  uint32_t *queue = plan.sync, *exits = plan.sync + 1, *ready = plan.sync + 4;
+  const uint32_t n_items = plan.n_rans + plan.n_tiles;
+  for (;;) {
+    __syncthreads();  // the previous item is done with shared memory and item_s
+    if (threadIdx.x == 0) item_s = atomicAdd(queue, 1u);
+    __syncthreads();
+    const uint32_t item = item_s;
+    if (item >= n_items) break;
+    if (item < plan.n_rans) {
+      const GstRansItem it = plan.rans[item];
+      rans_item(cmp, scratch, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
+                plan.counters + it.image, plan.images[it.image], it.section, it.first_group, it.ngroups, it.streams,
+                plan.stage_words);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ready + it.image, static_cast<uint32_t>(it.ngroups));
+      }
+    } else {
+      const GstTileItem it = plan.tiles[item - plan.n_rans];
+      const GstImageDesc &im = plan.images[it.image];
+      uint32_t *image_err = plan.image_err ? plan.image_err + it.image : nullptr;
+      if (threadIdx.x == 0) {
+        const uint32_t need = im.sec_groups[0] + im.sec_groups[1] + im.sec_groups[2] + im.sec_groups[3];
+        uint32_t ok = 1;
+        if (ld_acquire(ready + it.image) < need) {
+          const uint64_t t0 = global_ns();
+          for (uint32_t spin = 0;; ++spin) {
+            __nanosleep(256);
+            if (ld_acquire(ready + it.image) >= need) break;
+            if (spin > kWaitLimitSpins || global_ns() - t0 > kWaitLimitNs) {
+              ok = 0;
+              flag_error(plan.err, image_err, kErrTimeout);
+              break;
+            }
+          }
+        }
+        ok_s = ok;
+      }
+      __syncthreads();
+      if (ok_s) tile_work<128, true>(scratch, out, plan.err, image_err, im, it.tile, reinterpret_cast<int32_t *>(smem_raw));
+    }
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(exits, 1u) == gridDim.x - 1) {
+      for (uint32_t i = 0; i < plan.n_images; ++i) ready[i] = 0;
+      *queue = 0;
+      *exits = 0;
+      __threadfence();
+    }
+  }
 }
 
 // Enqueues the decode of one plan.  With `ev` non-null, records ev[0] before
 // the first kernel and ev[i + 1] after kernel i (instrumentation).  `tuning`
-// selects the rANS kernel's register budget (CTAs per SM) and staging depth.
+// selects the form (two kernels, or the persistent kernel where the plan has
+// its sync words), the rANS kernel's register budget and the staging depth.
 cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, GstPlanView plan,
-                          cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning) {
+                          cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning,
+                          const char **names) {
   *launches = 0;
   static bool configured = false;  // per process; the attribute applies to every device context
   if (!configured) {
@@ -548,6 +675,9 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
       e = cudaFuncSetAttribute(gst_rans_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(gst_rans_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(gst_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(persistent_smem_bytes(kMaxStageWords)));
     if (e != cudaSuccess) return e;
     configured = true;
   }
@@ -555,23 +685,39 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
     return cudaErrorInvalidValue;
   plan.stage_words = tuning.stage_words;
   if (ev) cudaEventRecord(ev[0], stream);
+  if (tuning.persistent && plan.sync && plan.n_rans + plan.n_tiles > 0) {
+    const size_t smem = persistent_smem_bytes(plan.stage_words);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gst_persistent_kernel, 128, smem);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid = std::min<uint32_t>(plan.n_rans + plan.n_tiles, uint32_t(std::max(1, sms * per_sm)));
+    gst_persistent_kernel<<<grid, 128, smem, stream>>>(d_cmp, d_scratch, d_out, plan);
+    if (names) names[*launches] = "gst_persistent_kernel";
+    ++*launches;
+    if (ev) cudaEventRecord(ev[*launches], stream);
+    return cudaGetLastError();
+  }
   if (plan.n_rans) {
     const size_t smem = rans_smem_bytes(plan.stage_words);
     if (tuning.blocks_per_sm >= 14) gst_rans_kernel<16><<<plan.n_rans, 128, smem, stream>>>(d_cmp, d_scratch, plan);
     else if (tuning.blocks_per_sm >= 10) gst_rans_kernel<12><<<plan.n_rans, 128, smem, stream>>>(d_cmp, d_scratch, plan);
     else gst_rans_kernel<8><<<plan.n_rans, 128, smem, stream>>>(d_cmp, d_scratch, plan);
+    if (names) names[*launches] = "gst_rans_kernel";
     ++*launches;
     if (ev) cudaEventRecord(ev[*launches], stream);
   }
   if (plan.n_tiles) {
     gst_tile_kernel<<<plan.n_tiles, 256, 0, stream>>>(d_scratch, d_out, plan);
+    if (names) names[*launches] = "gst_tile_kernel";
     ++*launches;
     if (ev) cudaEventRecord(ev[*launches], stream);
   }
   return cudaGetLastError();
 }
 
-const char *kernel_name(int i) { return i == 0 ? "gst_rans_kernel" : "gst_tile_kernel"; }
 
 }  // namespace gst
 
@@ -637,71 +783,7 @@ __global__ void __launch_bounds__(256) gst_tile_static_kernel(const uint8_t *bas
                                                               GstImageDesc im) {
   __shared__ int32_t pl[6 * kPlaneWords];
   uint32_t *err = reinterpret_cast<uint32_t *>(const_cast<uint8_t *>(base));
-  const uint8_t *scratch = base + kStaticHeaderBytes;
-  const uint32_t tile = blockIdx.x;
-  const size_t B = static_cast<size_t>(im.bx) * im.by;
-  const uint32_t tx = tile % im.tiles_x, ty = tile / im.tiles_x;
-  const uint8_t *sym = scratch + im.sym_off;
-  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-
-  const uint8_t *tile_base = sym + static_cast<size_t>(tile) * 1024;
-  const uint4 c0 = *(reinterpret_cast<const uint4 *>(tile_base + (t >> 6) * B) + (t & 63));
-  uint4 c1 = make_uint4(0, 0, 0, 0);
-  if (t < 128) c1 = *(reinterpret_cast<const uint4 *>(tile_base + ((t + 256) >> 6) * B) + ((t + 256) & 63));
-
-  const int32_t *chunk_pref = reinterpret_cast<const int32_t *>(scratch + im.chunk_off);
-  const int32_t *gpref = reinterpret_cast<const int32_t *>(scratch + im.gsum_off) + im.sec_groups[3];
-  const uint8_t *deltas = sym + im.sec_out[3];
-  uint32_t d[4], basev[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const uint32_t p0 = (ty * 32 + warp + 8 * i) * im.bx + tx * 32;
-    d[i] = static_cast<uint32_t>(deltas[p0 + lane]) - 128u;
-    basev[i] = static_cast<uint32_t>(gpref[p0 >> 13]) + static_cast<uint32_t>(chunk_pref[p0 >> 5]);
-  }
-  auto unpack = [&](uint4 c, int chunk) {
-    const int p = chunk >> 6, q = chunk & 63;
-    int32_t *dst = pl + p * kPlaneWords + (q >> 1) * kPlanePitch + (q & 1) * 16;
-    const uint32_t w[4] = {c.x, c.y, c.z, c.w};
-#pragma unroll
-    for (int k = 0; k < 16; ++k) dst[k] = static_cast<int32_t>((w[k >> 2] >> (8 * (k & 3))) & 0xFFu) - 128;
-  };
-  unpack(c0, t);
-  if (t < 128) unpack(c1, t + 256);
-
-  const uint32_t *pal = reinterpret_cast<const uint32_t *>(sym + im.sec_out[2]);
-  uint32_t word[4];
-  bool bad = false;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, d[i], o);
-      if (lane >= o) d[i] += n;
-    }
-    const uint32_t idx = basev[i] + d[i];
-    word[i] = 0;
-    if (idx < im.palette_words) word[i] = pal[idx];
-    else bad = true;
-  }
-  __syncthreads();
-  inv53_level<2>(pl);
-  inv53_level<4>(pl);
-  inv53_level<8>(pl);
-  inv53_level<16>(pl);
-  inv53_level<32>(pl);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int r = warp + 8 * i;
-    const uint32_t p = (ty * 32 + r) * im.bx + tx * 32 + lane;
-    const int32_t *row = pl + r * kPlanePitch + lane;
-    const int y1 = static_cast<int8_t>(row[0]), y2 = static_cast<int8_t>(row[kPlaneWords]);
-    const int co1 = static_cast<int8_t>(row[2 * kPlaneWords]), cg1 = static_cast<int8_t>(row[3 * kPlaneWords]);
-    const int co2 = static_cast<int8_t>(row[4 * kPlaneWords]), cg2 = static_cast<int8_t>(row[5 * kPlaneWords]);
-    const uint32_t ep1 = ycocg_to_565(y1, co1, cg1), ep2 = ycocg_to_565(y2, co2, cg2);
-    *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) = make_uint2(ep1 | (ep2 << 16), word[i]);
-  }
-  if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(err, nullptr, kErrPalette);
+  tile_work<256, false>(base + kStaticHeaderBytes, out, err, nullptr, im, blockIdx.x, pl);
 }
 
 }  // namespace gst

@@ -29,11 +29,14 @@ constexpr uint32_t kGroupsPerRansCta = 4;
 // always cover the next sixteen steps; 2816 keeps seven CTAs per SM.
 constexpr uint32_t kMinStageWords = 520, kMaxStageWords = 2816, kDefaultStageWords = 1016;
 
-// Launch configuration of the rANS kernel.
+// Launch configuration of a decode.
 struct GstTuning {
-  int blocks_per_sm = 12;                      // register budget: 8, 12 or 16 CTAs of 128 threads per SM
+  int blocks_per_sm = 12;                      // rANS register budget: 8, 12 or 16 CTAs of 128 threads per SM
   uint32_t stage_words = kDefaultStageWords;  // staging depth
-  bool operator==(const GstTuning &o) const { return blocks_per_sm == o.blocks_per_sm && stage_words == o.stage_words; }
+  int persistent = 0;                          // 1: one persistent kernel drains the whole plan
+  bool operator==(const GstTuning &o) const {
+    return blocks_per_sm == o.blocks_per_sm && stage_words == o.stage_words && persistent == o.persistent;
+  }
   bool operator!=(const GstTuning &o) const { return !(*this == o); }
 };
 constexpr uint32_t kRansL = 1u << 15;         // k * M, k = 2^4      ans/ans_ocl_encode.cpp:15-16
@@ -45,6 +48,7 @@ constexpr uint32_t kErrTable = 1u;       // a frequency table does not sum to 20
 constexpr uint32_t kErrGroup = 2u;       // a group end offset is out of order or range
 constexpr uint32_t kErrStream = 4u;      // a renormalisation read left its group
 constexpr uint32_t kErrPalette = 8u;     // a palette index is outside the palette
+constexpr uint32_t kErrTimeout = 16u;    // a bounded wait of the persistent kernel gave up
 
 struct alignas(16) GstImageDesc {
   uint64_t freq_off;    // bytes from the compressed base to this image's 4 tables
@@ -91,6 +95,10 @@ struct GstPlanView {
   const GstTileItem *tiles;
   uint32_t *counters;   // one per image (index-group completion count)
   uint32_t *image_err;  // one per image (error bits), or null
+  // Persistent kernel (may be null otherwise): [0] work-queue head, [1] CTAs
+  // finished, [4 + i] groups of image i decoded.  Every launch leaves them 0.
+  uint32_t *sync;
+  uint32_t n_images;
   uint32_t n_rans, n_tiles;
   uint32_t stage_words;  // rANS staging depth per warp, in 16-bit words
 };

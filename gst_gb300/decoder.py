@@ -147,8 +147,8 @@ def load_library() -> ctypes.CDLL:
         "gst_batch_destroy": (None, [P]),
         "gst_batch_device_bytes": (S, [P]),
         "gst_batch_launch": (I, [P, P, P, P]),
-        "gst_batch_autotune": (I, [P, P, P, P, I, ctypes.POINTER(I), ctypes.POINTER(I)]),
-        "gst_batch_set_tuning": (I, [P, I, I]),
+        "gst_batch_autotune": (I, [P, P, P, P, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]),
+        "gst_batch_set_tuning": (I, [P, I, I, I]),
         "gst_batch_graph_launch": (I, [P, P, P, P]),
         "gst_load_compressed_dxt_static": (I, [HP, P, P, P, ctypes.POINTER(U32)]),
         "gst_sync_status": (I, [P, P]),
@@ -278,18 +278,19 @@ class ResidentBatch:
         fn = load_library().gst_batch_graph_launch if graph else load_library().gst_batch_launch
         _check(fn(self._h, _ptr(cmp_data), _ptr(output), _stream(stream)), "gst_batch_launch")
 
-    def autotune(self, cmp_data, output, stream=None, iterations: int = 3) -> tuple[int, int]:
-        """gst_batch_autotune: times each (CTAs per SM, staging depth) rANS
-        configuration on this batch and keeps the fastest; returns it."""
-        bps, words = ctypes.c_int(0), ctypes.c_int(0)
+    def autotune(self, cmp_data, output, stream=None, iterations: int = 3) -> tuple[int, int, int]:
+        """gst_batch_autotune: times each launch configuration on this batch
+        and keeps the fastest; returns (blocks_per_sm, stage_words, persistent)."""
+        bps, words, pers = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
         _check(load_library().gst_batch_autotune(self._h, _ptr(cmp_data), _ptr(output), _stream(stream),
-                                                 int(iterations), ctypes.byref(bps), ctypes.byref(words)),
+                                                 int(iterations), ctypes.byref(bps), ctypes.byref(words),
+                                                 ctypes.byref(pers)),
                "gst_batch_autotune")
-        return bps.value, words.value
+        return bps.value, words.value, pers.value
 
-    def set_tuning(self, blocks_per_sm: int, stage_words: int) -> None:
+    def set_tuning(self, blocks_per_sm: int, stage_words: int, persistent: int = 0) -> None:
         """gst_batch_set_tuning; (0, 0) returns to the context's configuration."""
-        _check(load_library().gst_batch_set_tuning(self._h, int(blocks_per_sm), int(stage_words)),
+        _check(load_library().gst_batch_set_tuning(self._h, int(blocks_per_sm), int(stage_words), int(persistent)),
                "gst_batch_set_tuning")
 
     def close(self) -> None:

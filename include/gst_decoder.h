@@ -119,20 +119,21 @@ size_t gst_batch_device_bytes(const gst_batch *batch);
 gst_status gst_batch_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
 gst_status gst_batch_graph_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
 
-/* Per-batch tuning of the rANS launch (no counterpart in the reference).
+/* Per-batch tuning of the launch (no counterpart in the reference).
  * gst_batch_autotune decodes the batch under each of a fixed set of
- * (CTAs per SM, staging depth) configurations -- one warm-up and `iterations`
- * timed launches each, on `stream`, blocking -- and keeps the fastest for the
- * batch's later launches, writing it to *blocks_per_sm / *stage_words when
- * those are non-null.  It writes the decoded output to d_out as a launch does
- * and must not be called while `stream` is being captured.
+ * configurations -- two kernels at (CTAs per SM, staging depth), or the
+ * persistent kernel at a staging depth -- one warm-up and `iterations` timed
+ * launches each, on `stream`, blocking, and keeps the fastest for the batch's
+ * later launches, writing it to *blocks_per_sm / *stage_words / *persistent
+ * when those are non-null.  It writes the decoded output to d_out as a launch
+ * does and must not be called while `stream` is being captured.
  * gst_batch_set_tuning sets the configuration directly (values as for the
- * "rans_blocks_per_sm" and "rans_stage_words" options); (0, 0) returns the
- * batch to the context's configuration.  Every configuration decodes
- * bit-identically; only the time differs. */
+ * "rans_blocks_per_sm", "rans_stage_words" and "persistent" options); (0, 0, 0)
+ * returns the batch to the context's configuration.  Every configuration
+ * decodes bit-identically; only the time differs. */
 gst_status gst_batch_autotune(gst_batch *batch, const void *d_cmp, void *d_out, void *stream, int iterations,
-                              int *blocks_per_sm, int *stage_words);
-gst_status gst_batch_set_tuning(gst_batch *batch, int blocks_per_sm, int stage_words);
+                              int *blocks_per_sm, int *stage_words, int *persistent);
+gst_status gst_batch_set_tuning(gst_batch *batch, int blocks_per_sm, int stage_words, int persistent);
 
 /* One-image device-resident decode that allocates nothing -- no counterpart in
  * the reference, which allocates its decoder scratch per call or through
@@ -202,6 +203,12 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
  *                         default 1016.  Deeper stages re-stage less often
  *                         but leave room for fewer CTAs per SM (16 CTAs at
  *                         520 words, 13 at 1016, 8 at 2040).
+ *   "persistent"          0 (default): a rANS kernel, then a tile kernel;
+ *                         1: one persistent kernel whose CTAs take rANS
+ *                         items, then tiles, from a work queue in the plan
+ *                         (a tile waits, bounded, for its image's groups;
+ *                         GST_E_TIMEOUT from gst_sync_status if it gave up).
+ *                         gst_decode_rans_groups always uses the rANS kernel.
  * Invalid values and unknown names return GST_E_ARG.  They apply to the
  * context's calls and to resident batches without a tuning of their own;
  * such batches re-capture their graph after a change. */

@@ -247,7 +247,9 @@ def test_resident_batch_launch_and_graph_replay(gpu_ctx):
     b.close()
 
 
-TUNINGS = [(16, 520), (12, 520), (12, 1016), (8, 1528), (8, 2040), (8, 2816), (10, 904)]
+AUTOTUNED = [(16, 520, 0), (12, 520, 0), (12, 1016, 0), (8, 1528, 0), (8, 2040, 0), (8, 2816, 0), (8, 1016, 1),
+             (8, 2040, 1)]
+TUNINGS = AUTOTUNED + [(10, 904, 0), (12, 520, 1)]
 
 
 def test_every_tuning_decodes_identically(gpu_ctx):
@@ -265,21 +267,26 @@ def test_every_tuning_decodes_identically(gpu_ctx):
     d_out = torch.zeros(sum(h.dxt_bytes for h in hdrs), dtype=torch.uint8, device="cuda")
     b = decoder.ResidentBatch(gpu_ctx, hdrs)
     try:
-        for bps, words in TUNINGS:
+        for bps, words, pers in TUNINGS:
             gpu_ctx.set_option("rans_blocks_per_sm", bps)
             gpu_ctx.set_option("rans_stage_words", words)
+            gpu_ctx.set_option("persistent", pers)
             d_o.zero_()
             decoder.decode_rans_groups(gpu_ctx, d_f, d_b, len(sec) - 512, sym.size // 8192, 32, d_o)
             assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
             assert np.array_equal(d_o.cpu().numpy(), sym), (bps, words)
-            for graph in (False, True):
+            for graph in (False, False, True, True):  # the persistent plan re-arms itself
                 d_out.zero_()
                 b.launch(d_cmp, d_out, graph=graph)  # untuned: follows the context
                 assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
-                assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want), (bps, words, graph)
+                assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want), (bps, words, pers, graph)
+            st, outs = batch_decode(gpu_ctx, [im.stream for im in imgs])  # per-call plans
+            assert st == decoder.GST_OK
+            assert np.array_equal(np.concatenate(outs).view(np.uint64), want), (bps, words, pers)
     finally:
         gpu_ctx.set_option("rans_blocks_per_sm", 12)
         gpu_ctx.set_option("rans_stage_words", 1016)
+        gpu_ctx.set_option("persistent", 0)
         b.close()
 
 
@@ -291,8 +298,8 @@ def test_batch_autotune_and_tuning_validation(gpu_ctx):
     d_out = torch.zeros(sum(h.dxt_bytes for h in hdrs), dtype=torch.uint8, device="cuda")
     b = decoder.ResidentBatch(gpu_ctx, hdrs)
     side = torch.cuda.Stream()
-    bps, words = b.autotune(d_cmp, d_out, side, iterations=2)
-    assert (bps, words) in TUNINGS[:6]
+    tuned = b.autotune(d_cmp, d_out, side, iterations=2)
+    assert tuned in AUTOTUNED
     assert decoder.sync_status(gpu_ctx, side) == decoder.GST_OK
     assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want)
     d_out.zero_()
@@ -300,7 +307,7 @@ def test_batch_autotune_and_tuning_validation(gpu_ctx):
     b.launch(d_cmp, d_out, side, graph=True)
     assert decoder.sync_status(gpu_ctx, side) == decoder.GST_OK
     assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want)
-    for bad in ((12, 512), (12, 1001), (12, 2824), (17, 1016), (0, 1016)):
+    for bad in ((12, 512, 0), (12, 1001, 0), (12, 2824, 0), (17, 1016, 0), (0, 1016, 0), (12, 1016, 2)):
         with pytest.raises(decoder.GstError) as ei:
             b.set_tuning(*bad)
         assert ei.value.status == decoder.GST_E_ARG
@@ -308,5 +315,7 @@ def test_batch_autotune_and_tuning_validation(gpu_ctx):
         gpu_ctx.set_option("rans_stage_words", 1004 + 1)
     with pytest.raises(decoder.GstError):
         gpu_ctx.set_option("no_such_option", 1)
+    with pytest.raises(decoder.GstError):
+        gpu_ctx.set_option("persistent", 2)
     b.set_tuning(0, 0)
     b.close()

@@ -250,7 +250,7 @@ PlanLayout plan_layout(const gst_header *hdrs, int n) {
 // and with out_at its blocks go to device address out_at[i]; the kernels then
 // get null compressed and output bases.
 void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph, const uint64_t *stream_at,
-                const uint64_t *out_at) {
+                const uint64_t *out_at, uint32_t out_block_bytes) {
   memset(ph, 0, L.bytes);
   GstPlanHead *head = reinterpret_cast<GstPlanHead *>(ph);
   head->n_images = uint32_t(n);
@@ -294,7 +294,7 @@ void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph,
     for (uint32_t t = 0; t < B / 1024; ++t) tiles[ti++] = {uint32_t(i), t};
     body += section_bytes(h);
     scratch_off += L.lay[i].total;
-    out_off += 8ull * B;
+    out_off += uint64_t(out_block_bytes) * B;
   }
 }
 
@@ -308,6 +308,7 @@ GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) 
   view.image_err = reinterpret_cast<uint32_t *>(plan_d + L.off_image_err);
   view.sync = reinterpret_cast<uint32_t *>(plan_d + L.off_sync);
   view.n_images = uint32_t(L.n_images);
+  view.rgb = 0;
   view.n_rans = L.n_rans;
   view.n_tiles = L.n_tiles;
   return view;
@@ -317,7 +318,7 @@ GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) 
 // layout at d_cmp, uploads it through the plan ring and launches.  hdrs have
 // passed check_header.
 gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8_t *d_cmp, uint8_t *d_out,
-                        cudaStream_t stream) {
+                        cudaStream_t stream, bool rgb = false) {
   const bool cap = capturing(stream);
   const PlanLayout L = plan_layout(hdrs, n);
   gst_status st = acquire_scratch(ctx, L.scratch_bytes, stream, cap);
@@ -325,9 +326,10 @@ gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8
   PlanBuf *pb = nullptr;
   st = acquire_plan(ctx, L.bytes, stream, cap, &pb);
   if (st != GST_OK) return st;
-  write_plan(L, hdrs, n, pb->h, nullptr, nullptr);
+  write_plan(L, hdrs, n, pb->h, nullptr, nullptr, rgb ? 48 : 8);
   GstPlanView view = plan_view(L, pb->d, ctx->status_d);
   view.image_err = nullptr;  // the context reports per call
+  view.rgb = rgb ? 1 : 0;
   st = upload_and_launch(ctx, pb, L.bytes, view, d_cmp, ctx->scratch, d_out, stream, cap);
   if (st != GST_OK) return st;
   if (!cap) {
@@ -598,6 +600,23 @@ gst_status gst_load_compressed_dxts(gst_ctx *ctx, const gst_header *hdrs, int n,
 gst_status gst_load_compressed_dxt(gst_ctx *ctx, const gst_header *hdr, const void *d_cmp, void *d_out,
                                    void *stream) {
   return gst_load_compressed_dxts(ctx, hdr, 1, d_cmp, d_out, stream);
+}
+
+gst_status gst_load_rgbs(gst_ctx *ctx, const gst_header *hdrs, int n, const void *d_cmp, void *d_out, void *stream) {
+  if (!ctx || !hdrs || n <= 0 || !d_cmp || !d_out) return GST_E_ARG;
+  if ((reinterpret_cast<uintptr_t>(d_cmp) & 15) || (reinterpret_cast<uintptr_t>(d_out) & 3)) return GST_E_ARG;
+  for (int i = 0; i < n; ++i) {
+    gst_status st = check_header(hdrs[i]);
+    if (st != GST_OK) return st;
+  }
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  return decode_batch(ctx, hdrs, n, static_cast<const uint8_t *>(d_cmp), static_cast<uint8_t *>(d_out),
+                      static_cast<cudaStream_t>(stream), true);
+}
+
+gst_status gst_load_rgb(gst_ctx *ctx, const gst_header *hdr, const void *d_cmp, void *d_out, void *stream) {
+  return gst_load_rgbs(ctx, hdr, 1, d_cmp, d_out, stream);
 }
 
 gst_status gst_decompress_dxt(gst_ctx *ctx, const uint8_t *gst, size_t len, uint8_t *dxt_out, size_t out_cap) {

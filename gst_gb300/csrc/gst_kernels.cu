@@ -463,6 +463,47 @@ __device__ __forceinline__ uint32_t ycocg_to_565(int y, int co, int cg) {
   return ((static_cast<uint32_t>(r) << 11) | (static_cast<uint32_t>(g) << 5) | static_cast<uint32_t>(b)) & 0xFFFFu;
 }
 
+// assemble.cl:83-129 (assemble_rgb): an endpoint as 8-bit R, G, B by bit
+// replication of its 5:6:5 integers, packed as bytes 0-2 of a word (each the
+// low 8 bits of the reference's int).
+__device__ __forceinline__ void ycocg_to_rgb8(int y, int co, int cg, int c[3]) {
+  const int t = y - cg / 2;
+  const int g = cg + t;
+  const int b = (t - co) / 2;
+  const int r = b + co;
+  c[0] = static_cast<int>(static_cast<uint32_t>(r) << 3) | (r >> 2);
+  c[1] = static_cast<int>(static_cast<uint32_t>(g) << 2) | (g >> 4);
+  c[2] = static_cast<int>(static_cast<uint32_t>(b) << 3) | (b >> 2);
+}
+__device__ __forceinline__ uint32_t pack_rgb8(int r, int g, int b) {
+  return (static_cast<uint32_t>(r) & 0xFFu) | ((static_cast<uint32_t>(g) & 0xFFu) << 8) |
+         ((static_cast<uint32_t>(b) & 0xFFu) << 16);
+}
+
+// Writes the 4x4 RGB8 pixels of one block (48 bytes over four pixel rows of
+// `pitch` bytes): the reference's four-colour palette, endpoints, then
+// (2a + b) / 3 and (a + 2b) / 3 in C integer division, selected by 2-bit
+// fields of `word`, low bits first, raster order within the block.
+__device__ __forceinline__ void store_rgb_block(uint8_t *o, size_t pitch, int y1, int co1, int cg1, int y2, int co2,
+                                                int cg2, uint32_t word) {
+  int a[3], b[3];
+  ycocg_to_rgb8(y1, co1, cg1, a);
+  ycocg_to_rgb8(y2, co2, cg2, b);
+  const uint32_t c0 = pack_rgb8(a[0], a[1], a[2]), c1 = pack_rgb8(b[0], b[1], b[2]);
+  const uint32_t c2 = pack_rgb8((2 * a[0] + b[0]) / 3, (2 * a[1] + b[1]) / 3, (2 * a[2] + b[2]) / 3);
+  const uint32_t c3 = pack_rgb8((a[0] + 2 * b[0]) / 3, (a[1] + 2 * b[1]) / 3, (a[2] + 2 * b[2]) / 3);
+  auto pick = [&](uint32_t s) { return (s & 2u) ? ((s & 1u) ? c3 : c2) : ((s & 1u) ? c1 : c0); };
+#pragma unroll
+  for (int py = 0; py < 4; ++py) {
+    const uint32_t q0 = pick(word), q1 = pick(word >> 2), q2 = pick(word >> 4), q3 = pick(word >> 6);
+    word >>= 8;
+    uint32_t *dst = reinterpret_cast<uint32_t *>(o + pitch * py);
+    dst[0] = __byte_perm(q0, q1, 0x4210);  // r0 g0 b0 r1
+    dst[1] = __byte_perm(q1, q2, 0x5421);  // g1 b1 r2 g2
+    dst[2] = __byte_perm(q2, q3, 0x6542);  // b2 r3 g3 b3
+  }
+}
+
 // Loads of decoded symbols: through the read-only path when another kernel
 // wrote them (COH false), coherently at L2 when CTAs of the same kernel did.
 template <bool COH, typename T>
@@ -474,8 +515,9 @@ __device__ __forceinline__ T ld_sym(const T *p) {
 constexpr size_t kTileSmemBytes = 6 * kPlaneWords * sizeof(int32_t);
 
 // One 32x32-block tile of one image with NT threads; `pl` is kTileSmemBytes
-// of shared memory.  All threads return.
-template <int NT, bool COH>
+// of shared memory.  Writes DXT1 blocks, or with RGB the blocks' RGB8 pixels
+// (LoadRGB).  All threads return.
+template <int NT, bool COH, bool RGB = false>
 __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, uint8_t *__restrict__ out,
                                           uint32_t *err, uint32_t *image_err, const GstImageDesc &im,
                                           uint32_t tile, int32_t *pl) {
@@ -551,7 +593,8 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
   inv53_level<16, NT>(pl);
   inv53_level<32, NT>(pl);
 
-  // 6. YCoCg667 -> RGB565 endpoints and whole 8-byte DXT1 blocks.
+  // 6. YCoCg667 -> RGB565 endpoints and whole 8-byte DXT1 blocks (or the
+  //    blocks' pixels).
 #pragma unroll
   for (int i = 0; i < kRows; ++i) {
     const int r = warp + kWarps * i;
@@ -560,18 +603,26 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
     const int y1 = static_cast<int8_t>(row[0]), y2 = static_cast<int8_t>(row[kPlaneWords]);
     const int co1 = static_cast<int8_t>(row[2 * kPlaneWords]), cg1 = static_cast<int8_t>(row[3 * kPlaneWords]);
     const int co2 = static_cast<int8_t>(row[4 * kPlaneWords]), cg2 = static_cast<int8_t>(row[5 * kPlaneWords]);
-    const uint32_t ep1 = ycocg_to_565(y1, co1, cg1), ep2 = ycocg_to_565(y2, co2, cg2);
-    *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) = make_uint2(ep1 | (ep2 << 16), word[i]);
+    if constexpr (RGB) {
+      const size_t pitch = static_cast<size_t>(im.bx) * 12;  // W * 3 bytes
+      uint8_t *o = out + im.out_off + pitch * 4 * (ty * 32 + r) + 12 * static_cast<size_t>(tx * 32 + lane);
+      store_rgb_block(o, pitch, y1, co1, cg1, y2, co2, cg2, word[i]);
+    } else {
+      const uint32_t ep1 = ycocg_to_565(y1, co1, cg1), ep2 = ycocg_to_565(y2, co2, cg2);
+      *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) =
+          make_uint2(ep1 | (ep2 << 16), word[i]);
+    }
   }
   if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(err, image_err, kErrPalette);
 }
 
+template <bool RGB>
 __global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict__ scratch, uint8_t *__restrict__ out,
                                                        GstPlanView plan) {
   __shared__ int32_t pl[6 * kPlaneWords];
   const GstTileItem it = plan.tiles[blockIdx.x];
-  tile_work<256, false>(scratch, out, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
-                        plan.images[it.image], it.tile, pl);
+  tile_work<256, false, RGB>(scratch, out, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
+                             plan.images[it.image], it.tile, pl);
 }
 
 // ---------------------------------------------------------------------------
@@ -685,7 +736,7 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
     return cudaErrorInvalidValue;
   plan.stage_words = tuning.stage_words;
   if (ev) cudaEventRecord(ev[0], stream);
-  if (tuning.persistent && plan.sync && plan.n_rans + plan.n_tiles > 0) {
+  if (tuning.persistent && plan.sync && !plan.rgb && plan.n_rans + plan.n_tiles > 0) {
     const size_t smem = persistent_smem_bytes(plan.stage_words);
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -710,8 +761,9 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
     if (ev) cudaEventRecord(ev[*launches], stream);
   }
   if (plan.n_tiles) {
-    gst_tile_kernel<<<plan.n_tiles, 256, 0, stream>>>(d_scratch, d_out, plan);
-    if (names) names[*launches] = "gst_tile_kernel";
+    if (plan.rgb) gst_tile_kernel<true><<<plan.n_tiles, 256, 0, stream>>>(d_scratch, d_out, plan);
+    else gst_tile_kernel<false><<<plan.n_tiles, 256, 0, stream>>>(d_scratch, d_out, plan);
+    if (names) names[*launches] = plan.rgb ? "gst_tile_rgb_kernel" : "gst_tile_kernel";
     ++*launches;
     if (ev) cudaEventRecord(ev[*launches], stream);
   }

@@ -99,6 +99,7 @@ struct GstPlanView {
   // finished, [4 + i] groups of image i decoded.  Every launch leaves them 0.
   uint32_t *sync;
   uint32_t n_images;
+  uint32_t rgb;  // 1: the tiles write RGB8 pixels (48 bytes per block) instead of DXT1
   uint32_t n_rans, n_tiles;
   uint32_t stage_words;  // rANS staging depth per warp, in 16-bit words
 };

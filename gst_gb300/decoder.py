@@ -40,7 +40,7 @@ STATUS_NAMES = {
 EXPORTED_SYMBOLS = (
     "gst_init", "gst_destroy", "gst_initialize_decoder", "gst_parse_header",
     "gst_required_scratch", "gst_preallocate", "gst_free_decompressor",
-    "gst_decompress_dxt", "gst_load_compressed_dxt", "gst_load_compressed_dxts",
+    "gst_decompress_dxt", "gst_load_compressed_dxt", "gst_load_compressed_dxts", "gst_load_rgb", "gst_load_rgbs",
     "gst_batch_layout_bytes", "gst_pack_batch", "gst_decode_rans_groups",
     "gst_batch_create", "gst_batch_destroy", "gst_batch_device_bytes", "gst_batch_launch",
     "gst_batch_graph_launch", "gst_batch_autotune", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
@@ -140,6 +140,8 @@ def load_library() -> ctypes.CDLL:
         "gst_decompress_dxt": (I, [P, P, S, P, S]),
         "gst_load_compressed_dxt": (I, [P, HP, P, P, P]),
         "gst_load_compressed_dxts": (I, [P, HP, I, P, P, P]),
+        "gst_load_rgb": (I, [P, HP, P, P, P]),
+        "gst_load_rgbs": (I, [P, HP, I, P, P, P]),
         "gst_batch_layout_bytes": (S, [HP, I]),
         "gst_pack_batch": (I, [ctypes.POINTER(P), ctypes.POINTER(S), I, P, S]),
         "gst_decode_rans_groups": (I, [P, P, P, U32, U32, U32, P, P]),
@@ -333,6 +335,19 @@ def load_compressed_dxts(ctx: GPUContext, hdrs: Sequence[GenTCHeader], cmp_data,
     arr = (GenTCHeader * len(hdrs))(*hdrs)
     _check(load_library().gst_load_compressed_dxts(ctx.handle, arr, len(hdrs), _ptr(cmp_data), _ptr(output),
                                                    _stream(stream)), "gst_load_compressed_dxts")
+
+
+def load_rgbs(ctx: GPUContext, hdrs: Sequence[GenTCHeader], cmp_data, output, stream=None) -> None:
+    """LoadRGBs (codec/decoder.cpp:552-556): the decode as RGB8, w*h*3 bytes per image."""
+    arr = (GenTCHeader * len(hdrs))(*hdrs)
+    _check(load_library().gst_load_rgbs(ctx.handle, arr, len(hdrs), _ptr(cmp_data), _ptr(output), _stream(stream)),
+           "gst_load_rgbs")
+
+
+def load_rgb(ctx: GPUContext, hdr: GenTCHeader, cmp_data, output, stream=None) -> None:
+    """LoadRGB (codec/decoder.cpp:546-550)."""
+    _check(load_library().gst_load_rgb(ctx.handle, ctypes.byref(hdr), _ptr(cmp_data), _ptr(output),
+                                       _stream(stream)), "gst_load_rgb")
 
 
 def load_compressed_dxt(ctx: GPUContext, hdr: GenTCHeader, cmp_data, output, stream=None) -> None:

@@ -14,6 +14,7 @@
  *   DecompressDXT                 :16-17     gst_decompress_dxt
  *   LoadCompressedDXT             :19-21     gst_load_compressed_dxt
  *   LoadCompressedDXTs            :23-25     gst_load_compressed_dxts
+ *   LoadRGB / LoadRGBs            :27-33     gst_load_rgb / gst_load_rgbs
  *   RequiredScratchMem            :35        gst_required_scratch
  *   PreallocateDecompressor       :36        gst_preallocate
  *   FreeDecompressor              :37        gst_free_decompressor
@@ -101,6 +102,17 @@ gst_status gst_load_compressed_dxt(gst_ctx *ctx, const gst_header *hdr, const vo
                                    void *d_out, void *stream);
 gst_status gst_load_compressed_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const void *d_cmp,
                                     void *d_out, void *stream);
+
+/* LoadRGB / LoadRGBs (codec/decoder.h:27-33, codec/decoder.cpp:546-556): the
+ * same decode, written as 8-bit RGB instead of DXT1 -- w*h*3 bytes per image,
+ * raster order, 3 bytes per pixel, images back to back from d_out (4-byte
+ * aligned).  The pixels are the reference's assemble_rgb
+ * (codec/assemble.cl:83-129): endpoints widened from 5:6:5 by bit
+ * replication, the four-colour palette (2a + b) / 3, (a + 2b) / 3 whatever
+ * the endpoints' order, and 2-bit selectors low bits first. */
+gst_status gst_load_rgb(gst_ctx *ctx, const gst_header *hdr, const void *d_cmp, void *d_out, void *stream);
+gst_status gst_load_rgbs(gst_ctx *ctx, const gst_header *hdrs, int n, const void *d_cmp, void *d_out,
+                         void *stream);
 
 /* Resident batches (the serving and benchmark form of LoadCompressedDXTs):
  * gst_batch_create builds the batch's work plan once, uploads it and reserves

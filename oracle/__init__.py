@@ -61,6 +61,7 @@ def load() -> ctypes.CDLL:
         lib.gsto_ycocg_to_565.argtypes = [I, I, I]
         lib.gsto_ycocg_to_565.restype = ctypes.c_uint16
         lib.gsto_decode.argtypes = [P, S, P, S, I, I]
+        lib.gsto_decode_rgb.argtypes = [P, S, P, S, I, I]
         lib.gsto_decode_symbols.argtypes = [P, S, P, S, I]
         lib.gsto_section_search.argtypes = [P, U32, U32]
         lib.gsto_section_search.restype = U32
@@ -96,6 +97,16 @@ def decode(stream: bytes, scan_mode: int = SCAN_REFERENCE, nthreads: int = 1) ->
     out = np.zeros(max(w * h // 2, 8), dtype=np.uint8)
     st = lib.gsto_decode(stream, len(stream), out.ctypes.data, out.nbytes, scan_mode, nthreads)
     return int(st), out[: w * h // 2]
+
+
+def decode_rgb(stream: bytes, scan_mode: int = SCAN_REFERENCE, nthreads: int = 1) -> tuple[int, np.ndarray]:
+    """Whole decode of one GST stream to RGB8 (assemble_rgb) -> (status, W*H*3 bytes)."""
+    lib = load()
+    w = int.from_bytes(stream[0:4], "little")
+    h = int.from_bytes(stream[4:8], "little")
+    out = np.zeros(max(w * h * 3, 8), dtype=np.uint8)
+    st = lib.gsto_decode_rgb(stream, len(stream), out.ctypes.data, out.nbytes, scan_mode, nthreads)
+    return int(st), out[: w * h * 3]
 
 
 def decode_symbols(stream: bytes, nthreads: int = 1) -> tuple[int, np.ndarray]:

@@ -395,6 +395,7 @@ typedef struct {
   int8_t *planes;         /* 6 x B raster */
   int32_t *indices;       /* B */
   uint8_t *dxt;
+  uint8_t *rgb; /* when set, assemble_rgb output (W*H*3) instead of DXT1 */
   uint32_t B, bx, by;
 } decode_ctx;
 
@@ -453,6 +454,56 @@ static void assemble_range(void *vctx, uint32_t lo, uint32_t hi, int *status) {
   }
 }
 
+/* assemble.cl:39-45 (YCoCgToRGB) and :83-129 (assemble_rgb), rows [lo, hi)
+ * of blocks: the two endpoints to 5:6:5 integers, widened to 8 bits by bit
+ * replication, two interpolated colours (2a + b) / 3 and (a + 2b) / 3 in C
+ * integer division (four-colour mode only), and each pixel's 2-bit selector
+ * from the palette word, low bits first in raster order within the block.
+ * Every channel is stored as its low 8 bits. */
+static void ycocg_to_rgb(int y, int co, int cg, int rgb[3]) {
+  const int t = y - (cg / 2);
+  const int g = cg + t;
+  const int b = (t - co) / 2;
+  const int r = b + co;
+  rgb[0] = (int)((uint32_t)r << 3) | (r >> 2);
+  rgb[1] = (int)((uint32_t)g << 2) | (g >> 4);
+  rgb[2] = (int)((uint32_t)b << 3) | (b >> 2);
+}
+
+static void assemble_rgb_range(void *vctx, uint32_t lo, uint32_t hi, int *status) {
+  decode_ctx *c = (decode_ctx *)vctx;
+  const uint8_t *palette = c->symbols + c->sec[2].out_off;
+  const uint32_t nwords = c->hdr.palette_bytes / 4;
+  const size_t B = c->B;
+  const int8_t *P = c->planes;
+  const size_t W = c->hdr.width;
+  for (uint32_t by = lo; by < hi; ++by) {
+    for (uint32_t bx = 0; bx < c->bx; ++bx) {
+      const size_t i = (size_t)by * c->bx + bx;
+      int pal[4][3];
+      ycocg_to_rgb(P[i], P[2 * B + i], P[3 * B + i], pal[0]);
+      ycocg_to_rgb(P[B + i], P[4 * B + i], P[5 * B + i], pal[1]);
+      for (int k = 0; k < 3; ++k) {
+        pal[2][k] = (2 * pal[0][k] + pal[1][k]) / 3;
+        pal[3][k] = (pal[0][k] + 2 * pal[1][k]) / 3;
+      }
+      const uint32_t idx = (uint32_t)c->indices[i];
+      uint32_t word = 0;
+      if (idx < nwords) word = rd32(palette + 4 * (size_t)idx);
+      else *status = GSTO_E_FORMAT;
+      for (int p = 0; p < 16; ++p) {
+        const int *col = pal[word & 3];
+        const size_t x = 4 * (size_t)bx + (p % 4), y = 4 * (size_t)by + (p / 4);
+        uint8_t *o = c->rgb + 3 * (W * y + x);
+        o[0] = (uint8_t)col[0];
+        o[1] = (uint8_t)col[1];
+        o[2] = (uint8_t)col[2];
+        word >>= 2;
+      }
+    }
+  }
+}
+
 static int setup_ctx(decode_ctx *c, const uint8_t *gst, size_t n) {
   int st = gsto_parse_header(gst, n, &c->hdr);
   if (st != GSTO_OK) return st;
@@ -487,8 +538,8 @@ int gsto_decode_symbols(const uint8_t *gst, size_t n, uint8_t *symbols, size_t c
   return st;
 }
 
-int gsto_decode(const uint8_t *gst, size_t n, uint8_t *dxt_out, size_t out_cap, int scan_mode,
-                int nthreads) {
+static int decode_image(const uint8_t *gst, size_t n, uint8_t *out, size_t out_cap, int scan_mode, int nthreads,
+                        int rgb) {
   decode_ctx *c = (decode_ctx *)calloc(1, sizeof(decode_ctx));
   if (!c) return GSTO_E_ARG;
   int st = setup_ctx(c, gst, n);
@@ -496,11 +547,12 @@ int gsto_decode(const uint8_t *gst, size_t n, uint8_t *dxt_out, size_t out_cap, 
     free(c);
     return st;
   }
-  if (!dxt_out || out_cap < 8 * (size_t)c->B) {
+  if (!out || out_cap < (rgb ? 48 : 8) * (size_t)c->B) {
     free(c);
     return GSTO_E_ARG;
   }
-  c->dxt = dxt_out;
+  if (rgb) c->rgb = out;
+  else c->dxt = out;
   c->symbols = (uint8_t *)malloc(7 * (size_t)c->B + c->hdr.palette_bytes);
   c->planes = (int8_t *)malloc(6 * (size_t)c->B);
   c->indices = (int32_t *)malloc(4 * (size_t)c->B);
@@ -510,7 +562,7 @@ int gsto_decode(const uint8_t *gst, size_t n, uint8_t *dxt_out, size_t out_cap, 
     int s1 = parallel_for(c->group_base[4], nthreads, rans_range, c);
     parallel_for(6 * (c->bx / 32) * (c->by / 32), nthreads, wavelet_range, c);
     gsto_scan_indices(c->symbols + c->sec[3].out_off, c->B, c->indices, scan_mode);
-    int s2 = parallel_for(c->by, nthreads, assemble_range, c);
+    int s2 = parallel_for(c->by, nthreads, rgb ? assemble_rgb_range : assemble_range, c);
     st = s1 != GSTO_OK ? s1 : s2;
   }
   free(c->symbols);
@@ -518,6 +570,14 @@ int gsto_decode(const uint8_t *gst, size_t n, uint8_t *dxt_out, size_t out_cap, 
   free(c->indices);
   free(c);
   return st;
+}
+
+int gsto_decode(const uint8_t *gst, size_t n, uint8_t *dxt_out, size_t out_cap, int scan_mode, int nthreads) {
+  return decode_image(gst, n, dxt_out, out_cap, scan_mode, nthreads, 0);
+}
+
+int gsto_decode_rgb(const uint8_t *gst, size_t n, uint8_t *rgb_out, size_t out_cap, int scan_mode, int nthreads) {
+  return decode_image(gst, n, rgb_out, out_cap, scan_mode, nthreads, 1);
 }
 
 int gsto_decode_batch(const uint8_t *const *gst, const size_t *lens, int n_streams,

@@ -95,6 +95,10 @@ uint16_t gsto_ycocg_to_565(int y, int co, int cg);
 int gsto_decode(const uint8_t *gst, size_t n, uint8_t *dxt_out, size_t out_cap, int scan_mode,
                 int nthreads);
 
+/* The same decode to 8-bit RGB (codec/assemble.cl:83-129, the reference's
+ * LoadRGB): width*height*3 bytes, raster order, 3 bytes per pixel. */
+int gsto_decode_rgb(const uint8_t *gst, size_t n, uint8_t *rgb_out, size_t out_cap, int scan_mode, int nthreads);
+
 /* The same decode, stopping after the rANS stage: writes the reference's
  * decompressed-symbol buffer (Y planes, chroma planes, palette, index deltas,
  * decoder.cpp:441-461 layout) of 7*B + palette_bytes bytes. */

@@ -319,3 +319,30 @@ def test_batch_autotune_and_tuning_validation(gpu_ctx):
         gpu_ctx.set_option("persistent", 2)
     b.set_tuning(0, 0)
     b.close()
+
+
+def test_load_rgb_matches_oracle(gpu_ctx):
+    # LoadRGB(s): assemble_rgb's pixels (codec/assemble.cl:83-129).  The oracle's
+    # RGB path is checked on the CPU against a plain four-colour DXT1 decode of
+    # its own DXT1 output; here the GPU's RGB output must equal it byte for byte.
+    streams = [golden_stream("test1.gst"), golden_stream("synth768x512_s3.gst")] + \
+        [workloads.encode_image(w, h, 800 + i).stream for i, (w, h) in enumerate([(1024, 512), (512, 1024)])]
+    hdrs, packed = decoder.pack_batch(streams)
+    d_cmp = torch.from_numpy(packed).cuda()
+    total = sum(h.width * h.height * 3 for h in hdrs)
+    d_out = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    decoder.load_rgbs(gpu_ctx, hdrs, d_cmp, d_out)
+    assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
+    out = d_out.cpu().numpy()
+    off = 0
+    for s, h in zip(streams, hdrs):
+        st, ref = oracle.decode_rgb(s, oracle.SCAN_EXACT)
+        assert st == 0
+        assert np.array_equal(out[off:off + ref.size], ref), (h.width, h.height)
+        off += ref.size
+    # single-image form, device-resident
+    one = torch.zeros(hdrs[0].width * hdrs[0].height * 3, dtype=torch.uint8, device="cuda")
+    h0, p0 = decoder.pack_batch(streams[:1])
+    decoder.load_rgb(gpu_ctx, h0[0], torch.from_numpy(p0).cuda(), one)
+    assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
+    assert np.array_equal(one.cpu().numpy(), oracle.decode_rgb(streams[0], oracle.SCAN_EXACT)[1])

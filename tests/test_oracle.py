@@ -250,3 +250,34 @@ def test_histogram_known_answers(ref, golden):
         out = np.zeros_like(counts)
         assert ref.gstref_generate_histogram(counts.ctypes.data, counts.size, c["M"], out.ctypes.data) == 0
         assert out.tolist() == c["expected"]
+
+
+def test_rgb_oracle_is_four_colour_dxt1_decode():
+    # The RGB restatement (assemble.cl:83-129) equals a four-colour DXT1 decode
+    # of the DXT1 blocks the pinned DXT path produces (valid streams keep every
+    # 5:6:5 channel in range, where the two agree).
+    for name in ("test1.gst", "synth768x512_s3.gst"):
+        s = golden_stream(name)
+        st, rgb = oracle.decode_rgb(s, oracle.SCAN_EXACT)
+        st2, dxt = oracle.decode(s, oracle.SCAN_EXACT)
+        assert st == st2 == 0
+        w = int.from_bytes(s[0:4], "little")
+        h = int.from_bytes(s[4:8], "little")
+        blk = dxt.view(np.uint64)
+        e0 = (blk & 0xFFFF).astype(np.int64)
+        e1 = ((blk >> np.uint64(16)) & 0xFFFF).astype(np.int64)
+        sel_word = (blk >> np.uint64(32)).astype(np.uint64)
+
+        def widen(e):
+            r, g, b = (e >> 11) & 31, (e >> 5) & 63, e & 31
+            return np.stack([(r << 3) | (r >> 2), (g << 2) | (g >> 4), (b << 3) | (b >> 2)], -1)
+
+        p0, p1 = widen(e0), widen(e1)
+        pal = np.stack([p0, p1, (2 * p0 + p1) // 3, (p0 + 2 * p1) // 3], 1)
+        bx = w // 4
+        img = np.zeros((h, w, 3), np.uint8)
+        n = np.arange(blk.size)
+        for pix in range(16):
+            sel = ((sel_word >> np.uint64(2 * pix)) & np.uint64(3)).astype(np.int64)
+            img[(n // bx) * 4 + pix // 4, (n % bx) * 4 + pix % 4] = pal[n, sel]
+        assert np.array_equal(img.reshape(-1), rgb), name

@@ -322,12 +322,17 @@ def run_gst(args, rank, world, local):
         for h, d_one, off in batch.views:
             decoder.load_compressed_dxt(ctx, h, d_one, base + off, stream)
 
-    def step_e2e():  # host buffers: pinned H2D, decode, D2H of the DXT1 blocks
+    def step_e2e_serial():  # host buffers: pinned H2D, graph replay, D2H of the DXT1 blocks, one after another
         with torch.cuda.stream(stream):
             batch.d_cmp.copy_(batch.h_cmp, non_blocking=True)
         rb.launch(batch.d_cmp, batch.d_out, stream, graph=True)
         with torch.cuda.stream(stream):
             batch.h_out.copy_(batch.d_out, non_blocking=True)
+
+    chunks = 8
+
+    def step_e2e():  # gst_load_host_dxts: pinned host in/out, copies and decodes of `chunks` runs overlapped
+        decoder.load_host_dxts(ctx, batch.hdrs, batch.h_cmp, batch.h_out, chunks, stream)
 
     peak, peak_kind = measured_peak_hbm()
     barrier(world)
@@ -356,11 +361,22 @@ def run_gst(args, rank, world, local):
     got_pi = batch.d_out.cpu().numpy().view(np.uint64)
     per_image_exact = bool(np.array_equal(got_pi, batch.expected()))
 
-    # e2e through the public API with host buffers
+    # e2e through the public API with host buffers: the pipelined host-to-host
+    # call, its chunk count chosen by timing 1 to 8 outside the timed steps
+    best = None
+    for c in (1, 2, 3, 4, 5, 6, 8):
+        chunks = c
+        t_c, _ = time_steps(step_e2e, 3, 2, stream, flush)
+        if best is None or statistics.mean(t_c) < best[1]:
+            best = (c, statistics.mean(t_c))
+    chunks = best[0]
+    batch.h_out.zero_()
     t_e2e, _ = time_steps(step_e2e, args.steps, args.warmup, stream, flush)
     e2e_total = max_over_ranks(sum(t_e2e), world)
     e2e_value = world * batch.pixels * args.steps / (e2e_total / 1e3) / 1e6
+    stream.synchronize()
     e2e_exact = bool(np.array_equal(batch.h_out.numpy().view(np.uint64), batch.expected()))
+    t_ser, _ = time_steps(step_e2e_serial, max(3, args.steps // 2), args.warmup, stream, flush)
 
     line = {
         "metric": METRIC,
@@ -419,6 +435,8 @@ def run_gst(args, rank, world, local):
             "h2d_bytes_per_step": int(batch.h_cmp.numel()),
             "d2h_bytes_per_step": int(batch.out_bytes),
             "bit_exact": e2e_exact,
+            "call": f"gst_load_host_dxts, {chunks} chunks (pinned host layout in, pinned DXT1 out)",
+            "serial_ms_per_step": round(statistics.mean(t_ser), 4),
         },
         "encode_seconds": round(encode_s, 1),
     }

@@ -117,6 +117,17 @@ struct gst_ctx {
   cudaEvent_t ev[kMaxTimedKernels + 1] = {};
   int timed_kernels = 0;
   const char *timed_names[kMaxTimedKernels] = {};
+  // Pipelined host-to-host decode (gst_load_host_dxts): device mirrors of the
+  // caller's pinned input and output, and its copy-in / decode / copy-out
+  // streams with one event pair per chunk.
+  uint8_t *hs_cmp_d = nullptr;
+  size_t hs_cmp_cap = 0;
+  uint8_t *hs_out_d = nullptr;
+  size_t hs_out_cap = 0;
+  cudaStream_t hs_in = nullptr, hs_comp = nullptr, hs_out = nullptr;
+  cudaEvent_t hs_start = nullptr, hs_done = nullptr;
+  cudaEvent_t hs_copied[kPlanRing] = {}, hs_decoded[kPlanRing] = {};
+  bool hs_used = false;
 };
 
 namespace gst {
@@ -245,12 +256,12 @@ PlanLayout plan_layout(const gst_header *hdrs, int n) {
 // Writes the plan (L.bytes) for n images whose compressed data sit in the
 // reference's layout: codec/decoder.cpp:132-149 and demo/photos_sf.cpp:753-791
 // (offsets page, then 4n frequency tables, then each image's four sections),
-// and whose DXT1 blocks go back to back.  With stream_at, image i is instead a
-// whole GST stream (header, tables, sections) at device address stream_at[i],
-// and with out_at its blocks go to device address out_at[i]; the kernels then
-// get null compressed and output bases.
-void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph, const uint64_t *stream_at,
-                const uint64_t *out_at, uint32_t out_block_bytes) {
+// and whose DXT1 blocks go back to back.  With freq_at / body_at, image i's
+// four frequency tables and first section are instead at those device
+// addresses, and with out_at its blocks go to device address out_at[i]; the
+// kernels then get null compressed and output bases.
+void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph, const uint64_t *freq_at,
+                const uint64_t *body_at, const uint64_t *out_at, uint32_t out_block_bytes) {
   memset(ph, 0, L.bytes);
   GstPlanHead *head = reinterpret_cast<GstPlanHead *>(ph);
   head->n_images = uint32_t(n);
@@ -267,8 +278,8 @@ void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph,
     const gst_header &h = hdrs[i];
     GstImageDesc &d = imgs[i];
     const uint32_t B = uint32_t(image_blocks(h));
-    d.freq_off = stream_at ? stream_at[i] + 28 : page + size_t(i) * 4 * kFreqTableBytes;
-    d.body_off = stream_at ? stream_at[i] + 28 + 4 * kFreqTableBytes : body;
+    d.freq_off = freq_at ? freq_at[i] : page + size_t(i) * 4 * kFreqTableBytes;
+    d.body_off = body_at ? body_at[i] : body;
     d.sym_off = scratch_off + L.lay[i].sym;
     d.chunk_off = scratch_off + L.lay[i].chunk;
     d.gsum_off = scratch_off + L.lay[i].gsum;
@@ -326,7 +337,7 @@ gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8
   PlanBuf *pb = nullptr;
   st = acquire_plan(ctx, L.bytes, stream, cap, &pb);
   if (st != GST_OK) return st;
-  write_plan(L, hdrs, n, pb->h, nullptr, nullptr, rgb ? 48 : 8);
+  write_plan(L, hdrs, n, pb->h, nullptr, nullptr, nullptr, rgb ? 48 : 8);
   GstPlanView view = plan_view(L, pb->d, ctx->status_d);
   view.image_err = nullptr;  // the context reports per call
   view.rgb = rgb ? 1 : 0;
@@ -464,6 +475,16 @@ void gst_destroy(gst_ctx *ctx) {
   for (auto &e : ctx->ev)
     if (e) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  cudaFree(ctx->hs_cmp_d);
+  cudaFree(ctx->hs_out_d);
+  for (cudaStream_t s : {ctx->hs_in, ctx->hs_comp, ctx->hs_out})
+    if (s) cudaStreamDestroy(s);
+  for (cudaEvent_t e : {ctx->hs_start, ctx->hs_done})
+    if (e) cudaEventDestroy(e);
+  for (int k = 0; k < kPlanRing; ++k) {
+    if (ctx->hs_copied[k]) cudaEventDestroy(ctx->hs_copied[k]);
+    if (ctx->hs_decoded[k]) cudaEventDestroy(ctx->hs_decoded[k]);
+  }
   delete ctx;
 }
 
@@ -619,6 +640,146 @@ gst_status gst_load_rgb(gst_ctx *ctx, const gst_header *hdr, const void *d_cmp, 
   return gst_load_rgbs(ctx, hdr, 1, d_cmp, d_out, stream);
 }
 
+gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const void *h_cmp, void *h_out,
+                              int chunks, void *stream) {
+  if (!ctx || !hdrs || n <= 0 || !h_cmp || !h_out || chunks < 0) return GST_E_ARG;
+  for (int i = 0; i < n; ++i) {
+    gst_status st = check_header(hdrs[i]);
+    if (st != GST_OK) return st;
+  }
+  if (chunks == 0) chunks = std::min(n, 8);
+  chunks = std::min(std::min(chunks, n), kPlanRing);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t caller = static_cast<cudaStream_t>(stream);
+  if (capturing(caller)) return GST_E_ARG;  // host memory paths are not captured
+  if (!ctx->hs_in) {
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->hs_in, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->hs_comp, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->hs_out, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->hs_start, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->hs_done, cudaEventDisableTiming);
+    for (int k = 0; k < kPlanRing && e == cudaSuccess; ++k) {
+      e = cudaEventCreateWithFlags(&ctx->hs_copied[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->hs_decoded[k], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  // Where each image's tables, sections and blocks are (the reference's
+  // layout, codec/decoder.cpp:430-476), and the chunk boundaries: contiguous
+  // runs of images whose block counts grow as 1, 1, 2, 4, ... so that the
+  // first copy out starts early and every later chunk is decoded while the
+  // copies out before it run.
+  const size_t page = offsets_page_bytes(n);
+  std::vector<uint64_t> body(n + 1), out(n + 1);
+  body[0] = page + size_t(n) * 4 * kFreqTableBytes;
+  out[0] = 0;
+  uint64_t blocks = 0;
+  for (int i = 0; i < n; ++i) {
+    body[i + 1] = body[i] + section_bytes(hdrs[i]);
+    out[i + 1] = out[i] + 8 * image_blocks(hdrs[i]);
+    blocks += image_blocks(hdrs[i]);
+  }
+  std::vector<double> bound(chunks);  // cumulative fraction of the blocks at the end of chunk k
+  double wsum = 0;
+  for (int k = 0; k < chunks; ++k) wsum += k < 2 ? 1.0 : double(1u << (k - 1));
+  for (int k = 0, acc_w = 0; k < chunks; ++k) {
+    acc_w += k < 2 ? 1 : int(1u << (k - 1));
+    bound[k] = double(acc_w) / wsum;
+  }
+  std::vector<int> cut(1, 0);
+  uint64_t acc = 0;
+  for (int i = 0; i < n; ++i) {
+    acc += image_blocks(hdrs[i]);
+    const int k = int(cut.size()) - 1;  // the chunk image i belongs to
+    const int left_images = n - (i + 1), left_chunks = chunks - int(cut.size());
+    if (left_chunks > 0 && left_images >= left_chunks &&
+        (double(acc) >= bound[k] * double(blocks) || left_images == left_chunks))
+      cut.push_back(i + 1);
+  }
+  cut.push_back(n);
+  const int nc = int(cut.size()) - 1;
+  gst_status st = grow_device(&ctx->hs_cmp_d, &ctx->hs_cmp_cap, body[n]);
+  if (st == GST_OK) st = grow_device(&ctx->hs_out_d, &ctx->hs_out_cap, out[n]);
+  if (st != GST_OK) return st;
+  size_t scratch = 0;
+  std::vector<PlanLayout> lay(nc);
+  for (int c = 0; c < nc; ++c) {
+    lay[c] = plan_layout(hdrs + cut[c], cut[c + 1] - cut[c]);
+    scratch = std::max(scratch, lay[c].scratch_bytes);
+  }
+  // A previous call's copies out of the mirrors must be done before this
+  // call overwrites them.
+  cudaEventRecord(ctx->hs_start, caller);
+  cudaStreamWaitEvent(ctx->hs_in, ctx->hs_start, 0);
+  if (ctx->hs_used) cudaStreamWaitEvent(ctx->hs_in, ctx->hs_done, 0);
+  cudaStreamWaitEvent(ctx->hs_comp, ctx->hs_start, 0);
+  cudaStreamWaitEvent(ctx->hs_out, ctx->hs_start, 0);
+  st = acquire_scratch(ctx, scratch, ctx->hs_comp, false);
+  if (st != GST_OK) return st;
+  const uint8_t *hc = static_cast<const uint8_t *>(h_cmp);
+  uint8_t *ho = static_cast<uint8_t *>(h_out);
+  cudaError_t e = cudaSuccess;
+  // The three passes are enqueued one after another (every copy in, then every
+  // decode, then every copy out) so that copies sharing a copy engine queue in
+  // the order they can run: a copy out never holds up a later copy in, and
+  // each chunk's plan travels with its data instead of behind later chunks.
+  // 1. Copy in each chunk's tables, sections (two contiguous ranges) and plan.
+  PlanBuf *pbs[kPlanRing] = {};
+  for (int c = 0; c < nc && e == cudaSuccess; ++c) {
+    const int i0 = cut[c], i1 = cut[c + 1], m = i1 - i0;
+    const size_t t0 = page + size_t(i0) * 4 * kFreqTableBytes, t1 = page + size_t(i1) * 4 * kFreqTableBytes;
+    e = cudaMemcpyAsync(ctx->hs_cmp_d + t0, hc + t0, t1 - t0, cudaMemcpyHostToDevice, ctx->hs_in);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(ctx->hs_cmp_d + body[i0], hc + body[i0], body[i1] - body[i0], cudaMemcpyHostToDevice,
+                          ctx->hs_in);
+    if (e != cudaSuccess) break;
+    std::vector<uint64_t> fa(m), ba(m), oa(m);
+    for (int k = 0; k < m; ++k) {
+      fa[k] = reinterpret_cast<uint64_t>(ctx->hs_cmp_d + page + size_t(i0 + k) * 4 * kFreqTableBytes);
+      ba[k] = reinterpret_cast<uint64_t>(ctx->hs_cmp_d + body[i0 + k]);
+      oa[k] = reinterpret_cast<uint64_t>(ctx->hs_out_d + out[i0 + k]);
+    }
+    st = acquire_plan(ctx, lay[c].bytes, ctx->hs_in, false, &pbs[c]);
+    if (st != GST_OK) return st;
+    write_plan(lay[c], hdrs + i0, m, pbs[c]->h, fa.data(), ba.data(), oa.data());
+    e = cudaMemcpyAsync(pbs[c]->d, pbs[c]->h, lay[c].bytes, cudaMemcpyHostToDevice, ctx->hs_in);
+    if (e == cudaSuccess) e = cudaEventRecord(pbs[c]->copied, ctx->hs_in);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->hs_copied[c], ctx->hs_in);
+  }
+  // 2. Decode each chunk once it is in.
+  for (int c = 0; c < nc && e == cudaSuccess; ++c) {
+    e = cudaStreamWaitEvent(ctx->hs_comp, ctx->hs_copied[c], 0);
+    if (e != cudaSuccess) break;
+    GstPlanView view = plan_view(lay[c], pbs[c]->d, ctx->status_d);
+    view.image_err = nullptr;
+    e = launch_decode(nullptr, ctx->scratch, nullptr, view, ctx->hs_comp, &ctx->last_launches, nullptr, ctx->tuning,
+                      ctx->timed_names);
+    if (e == cudaSuccess) e = cudaEventRecord(pbs[c]->done, ctx->hs_comp);
+    pbs[c]->stream = ctx->hs_comp;
+    pbs[c]->used = true;
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->hs_decoded[c], ctx->hs_comp);
+  }
+  // 3. Copy each chunk's blocks out once decoded.
+  for (int c = 0; c < nc && e == cudaSuccess; ++c) {
+    const int i0 = cut[c], i1 = cut[c + 1];
+    e = cudaStreamWaitEvent(ctx->hs_out, ctx->hs_decoded[c], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(ho + out[i0], ctx->hs_out_d + out[i0], out[i1] - out[i0], cudaMemcpyDeviceToHost,
+                          ctx->hs_out);
+  }
+  if (e != cudaSuccess) return cuda_status(e);
+  cudaEventRecord(ctx->scratch_done, ctx->hs_comp);
+  ctx->scratch_stream = ctx->hs_comp;
+  ctx->scratch_used = true;
+  // hs_done: the last copy out, after every decode (the copy-out stream
+  // waited for each chunk's decode in turn).
+  e = cudaEventRecord(ctx->hs_done, ctx->hs_out);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(caller, ctx->hs_done, 0);
+  ctx->hs_used = true;
+  return cuda_status(e);
+}
+
 gst_status gst_decompress_dxt(gst_ctx *ctx, const uint8_t *gst, size_t len, uint8_t *dxt_out, size_t out_cap) {
   if (!ctx || !gst || !dxt_out) return GST_E_ARG;
   gst_header h;
@@ -711,7 +872,7 @@ gst_status gst_batch_create(gst_ctx *ctx, const gst_header *hdrs, int n, gst_bat
   b->compressed_bytes = gst_batch_layout_bytes(hdrs, n);
   for (int i = 0; i < n; ++i) b->out_bytes += size_t(image_blocks(hdrs[i])) * 8;
   std::vector<uint8_t> plan(b->layout.bytes);
-  write_plan(b->layout, hdrs, n, plan.data(), nullptr, nullptr);
+  write_plan(b->layout, hdrs, n, plan.data(), nullptr, nullptr, nullptr);
   cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&b->plan_d), b->layout.bytes);
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(&b->scratch), std::max<size_t>(b->layout.scratch_bytes, 256));
   if (e == cudaSuccess) e = cudaMemcpy(b->plan_d, plan.data(), b->layout.bytes, cudaMemcpyHostToDevice);

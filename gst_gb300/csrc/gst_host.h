@@ -45,8 +45,8 @@ struct PlanLayout {
 };
 PlanLayout plan_layout(const gst_header *hdrs, int n);
 // out_block_bytes: output bytes per block, 8 (DXT1) or 48 (RGB8).
-void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph, const uint64_t *stream_at,
-                const uint64_t *out_at, uint32_t out_block_bytes = 8);
+void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph, const uint64_t *freq_at,
+                const uint64_t *body_at, const uint64_t *out_at, uint32_t out_block_bytes = 8);
 GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d);
 
 int ctx_device(const gst_ctx *ctx);

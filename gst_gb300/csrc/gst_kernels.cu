@@ -410,6 +410,32 @@ __global__ void __launch_bounds__(128, MINB) gst_rans_kernel(const uint8_t *__re
 }
 
 // ---------------------------------------------------------------------------
+// C's truncating u / 4 and u / 2 for signed u, as floor division of u plus
+// (divisor - 1) when u < 0.  The sign (-1 or 0) comes from a high multiply
+// and the correction from a multiply-add, so two of the three instructions
+// issue to the FMA pipe; the integer ALU pipe keeps the shift.
+__device__ __forceinline__ int32_t trunc_div4(int32_t u) {
+  int32_t sgn, v;
+  asm("mul.hi.s32 %0, %1, 2;" : "=r"(sgn) : "r"(u));          // -1 if u < 0, else 0 (|u| < 2^30)
+  asm("mad.lo.s32 %0, %1, -3, %2;" : "=r"(v) : "r"(sgn), "r"(u));
+  return v >> 2;
+}
+__device__ __forceinline__ int32_t trunc_div2(int32_t u) {
+  int32_t sgn, v;
+  asm("mul.hi.s32 %0, %1, 2;" : "=r"(sgn) : "r"(u));
+  asm("mad.lo.s32 %0, %1, -1, %2;" : "=r"(v) : "r"(sgn), "r"(u));
+  return v >> 1;
+}
+
+// Byte (SEL & 7) of w sign-extended to 32 bits: a byte permute whose upper
+// selector nibbles have the sign-replicate bit set (prmt's default mode).
+template <uint32_t SEL>
+__device__ __forceinline__ int32_t sext_byte(uint32_t w) {
+  uint32_t d;
+  asm("prmt.b32 %0, %1, 0, %2;" : "=r"(d) : "r"(w), "n"(SEL));
+  return static_cast<int32_t>(d);
+}
+
 // Inverse 5/3 lifting of one line of length L in place, with the arithmetic of
 // inverse_wavelet.cl:28-64 (NormalizeIndex mirroring; C division).
 template <int L>
@@ -422,12 +448,12 @@ __device__ __forceinline__ void inv53_line(int32_t *p, int step) {
   for (int x = 0; x < mid; ++x) {
     const int prev = mid + (x > 0 ? x - 1 : 0);  // mid + NormalizeIndex(2x-1, L)/2
     const int next = mid + x;                    // mid + NormalizeIndex(2x+1, L)/2
-    d[2 * x] = s[x] - (s[prev] + s[next] + 2) / 4;
+    d[2 * x] = s[x] - trunc_div4(s[prev] + s[next] + 2);
   }
 #pragma unroll
   for (int x = 0; x < mid; ++x) {
     const int nx = (2 * x + 2 < L) ? 2 * x + 2 : L - 2;  // NormalizeIndex(2x+2, L)
-    d[2 * x + 1] = s[mid + x] + (d[2 * x] + d[nx]) / 2;
+    d[2 * x + 1] = s[mid + x] + trunc_div2(d[2 * x] + d[nx]);
   }
 #pragma unroll
   for (int k = 0; k < L; ++k) p[k * step] = d[k];
@@ -556,13 +582,19 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
               static_cast<uint32_t>(ld_sym<COH>(chunk_pref + (p0 >> 5)));
   }
 
-  // 3. Coefficients to int32 (byte - 128), rows of pitch kPlanePitch.
+  // 3. Coefficients to int32 (byte - 128), rows of pitch kPlanePitch: the
+  //    byte with its top bit flipped, sign-extended by one byte permute.
   auto unpack = [&](uint4 cv, int chunk) {
     const int p = chunk >> 6, q = chunk & 63;  // plane, 16-byte chunk in the plane's block
     int32_t *dst = pl + p * kPlaneWords + (q >> 1) * kPlanePitch + (q & 1) * 16;
-    const uint32_t w[4] = {cv.x, cv.y, cv.z, cv.w};
+    const uint32_t w[4] = {cv.x ^ 0x80808080u, cv.y ^ 0x80808080u, cv.z ^ 0x80808080u, cv.w ^ 0x80808080u};
 #pragma unroll
-    for (int k = 0; k < 16; ++k) dst[k] = static_cast<int32_t>((w[k >> 2] >> (8 * (k & 3))) & 0xFFu) - 128;
+    for (int k = 0; k < 4; ++k) {
+      dst[4 * k + 0] = sext_byte<0x8880u>(w[k]);
+      dst[4 * k + 1] = sext_byte<0x9991u>(w[k]);
+      dst[4 * k + 2] = sext_byte<0xAAA2u>(w[k]);
+      dst[4 * k + 3] = sext_byte<0xBBB3u>(w[k]);
+    }
   };
 #pragma unroll
   for (int k = 0; k < kChunks; ++k)

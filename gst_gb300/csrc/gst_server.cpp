@@ -14,7 +14,7 @@
 //     compressed input is freed at once, the DXT1 output stays resident until
 //     the caller releases it.
 // Every image keeps its own GST stream and output region: the plan carries
-// absolute device addresses (write_plan with stream_at/out_at), so a batch
+// absolute device addresses (write_plan with freq_at/body_at/out_at), so a batch
 // needs no packing on the device.
 #include <cuda_runtime.h>
 
@@ -109,7 +109,7 @@ struct Slot {
   size_t err_off = 0;            // per-image error words in the plan, copied back into plan_h
   std::vector<uint64_t> ids;
   std::vector<gst_header> hdrs;
-  std::vector<uint64_t> stream_at, out_at;
+  std::vector<uint64_t> freq_at, body_at, out_at;
   bool busy = false;
   uint64_t t_done = 0;
   struct gst_server *srv = nullptr;
@@ -203,7 +203,8 @@ gst_status grow(uint8_t **dev_p, uint8_t **host_p, size_t *cap, size_t need) {
 bool gst_server::launch(Slot &s, std::unique_lock<std::mutex> &lk) {
   s.ids.clear();
   s.hdrs.clear();
-  s.stream_at.clear();
+  s.freq_at.clear();
+  s.body_at.clear();
   s.out_at.clear();
   size_t scratch = 0;
   const int cap = cfg.max_batch_images;
@@ -216,7 +217,8 @@ bool gst_server::launch(Slot &s, std::unique_lock<std::mutex> &lk) {
     r.t_launch = now();
     s.ids.push_back(r.id);
     s.hdrs.push_back(r.hdr);
-    s.stream_at.push_back(reinterpret_cast<uint64_t>(dev + r.in_off));
+    s.freq_at.push_back(reinterpret_cast<uint64_t>(dev + r.in_off + 28));
+    s.body_at.push_back(reinterpret_cast<uint64_t>(dev + r.in_off + 28 + 4 * kFreqTableBytes));
     s.out_at.push_back(reinterpret_cast<uint64_t>(dev + r.out_off));
     admitted.pop_front();
   }
@@ -247,7 +249,7 @@ bool gst_server::launch(Slot &s, std::unique_lock<std::mutex> &lk) {
   }
   cudaError_t e = cudaSuccess;
   if (st == GST_OK) {
-    write_plan(L, s.hdrs.data(), n, s.plan_h, s.stream_at.data(), s.out_at.data());
+    write_plan(L, s.hdrs.data(), n, s.plan_h, s.freq_at.data(), s.body_at.data(), s.out_at.data());
     for (auto &c : copies) {
       e = cudaMemcpyAsync(dev + c.second.first, host + c.first, c.second.second, cudaMemcpyHostToDevice, s.stream);
       if (e != cudaSuccess) break;

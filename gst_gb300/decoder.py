@@ -41,6 +41,7 @@ EXPORTED_SYMBOLS = (
     "gst_init", "gst_destroy", "gst_initialize_decoder", "gst_parse_header",
     "gst_required_scratch", "gst_preallocate", "gst_free_decompressor",
     "gst_decompress_dxt", "gst_load_compressed_dxt", "gst_load_compressed_dxts", "gst_load_rgb", "gst_load_rgbs",
+    "gst_load_host_dxts",
     "gst_batch_layout_bytes", "gst_pack_batch", "gst_decode_rans_groups",
     "gst_batch_create", "gst_batch_destroy", "gst_batch_device_bytes", "gst_batch_launch",
     "gst_batch_graph_launch", "gst_batch_autotune", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
@@ -141,6 +142,7 @@ def load_library() -> ctypes.CDLL:
         "gst_load_compressed_dxt": (I, [P, HP, P, P, P]),
         "gst_load_compressed_dxts": (I, [P, HP, I, P, P, P]),
         "gst_load_rgb": (I, [P, HP, P, P, P]),
+        "gst_load_host_dxts": (I, [P, HP, I, P, P, I, P]),
         "gst_load_rgbs": (I, [P, HP, I, P, P, P]),
         "gst_batch_layout_bytes": (S, [HP, I]),
         "gst_pack_batch": (I, [ctypes.POINTER(P), ctypes.POINTER(S), I, P, S]),
@@ -335,6 +337,15 @@ def load_compressed_dxts(ctx: GPUContext, hdrs: Sequence[GenTCHeader], cmp_data,
     arr = (GenTCHeader * len(hdrs))(*hdrs)
     _check(load_library().gst_load_compressed_dxts(ctx.handle, arr, len(hdrs), _ptr(cmp_data), _ptr(output),
                                                    _stream(stream)), "gst_load_compressed_dxts")
+
+
+def load_host_dxts(ctx: GPUContext, hdrs: Sequence[GenTCHeader], h_cmp, h_out, chunks: int = 0,
+                   stream=None) -> None:
+    """gst_load_host_dxts: pinned host layout in, pinned host DXT1 out, with the
+    copies in, decodes and copies out of `chunks` runs of images overlapped."""
+    arr = (GenTCHeader * len(hdrs))(*hdrs)
+    _check(load_library().gst_load_host_dxts(ctx.handle, arr, len(hdrs), _ptr(h_cmp), _ptr(h_out), int(chunks),
+                                             _stream(stream)), "gst_load_host_dxts")
 
 
 def load_rgbs(ctx: GPUContext, hdrs: Sequence[GenTCHeader], cmp_data, output, stream=None) -> None:

@@ -114,6 +114,19 @@ gst_status gst_load_rgb(gst_ctx *ctx, const gst_header *hdr, const void *d_cmp, 
 gst_status gst_load_rgbs(gst_ctx *ctx, const gst_header *hdrs, int n, const void *d_cmp, void *d_out,
                          void *stream);
 
+/* Pipelined host-to-host LoadCompressedDXTs (the streaming form of
+ * demo/photos_sf.cpp:688-830, no counterpart API in the reference): h_cmp is
+ * the reference's layout (as for gst_load_compressed_dxts) and h_out the
+ * DXT1 output, both in pinned host memory (cudaMallocHost / cudaHostAlloc).
+ * The n images are split into `chunks` (0 = up to 8) contiguous runs of about
+ * equal block counts; each run's tables and sections are copied in, decoded
+ * and copied out on three internal streams, so that copies in, decodes and
+ * copies out of different runs overlap.  Enqueued after the work already on
+ * `stream`, and `stream` waits for the last copy out: h_out is complete once
+ * `stream` reaches that point.  Calls on one context run one after another. */
+gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const void *h_cmp, void *h_out,
+                              int chunks, void *stream);
+
 /* Resident batches (the serving and benchmark form of LoadCompressedDXTs):
  * gst_batch_create builds the batch's work plan once, uploads it and reserves
  * the batch's own scratch (gst_batch_device_bytes in total), so that

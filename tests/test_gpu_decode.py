@@ -346,3 +346,22 @@ def test_load_rgb_matches_oracle(gpu_ctx):
     decoder.load_rgb(gpu_ctx, h0[0], torch.from_numpy(p0).cuda(), one)
     assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
     assert np.array_equal(one.cpu().numpy(), oracle.decode_rgb(streams[0], oracle.SCAN_EXACT)[1])
+
+
+@pytest.mark.parametrize("chunks", [1, 3, 8])
+def test_load_host_dxts_pipelined(gpu_ctx, chunks):
+    # Pinned host layout in, pinned host DXT1 out, chunks overlapped on three
+    # streams; twice in a row (the device mirrors are reused).
+    imgs = [workloads.encode_image(w, h, 840 + i) for i, (w, h) in
+            enumerate([(1024, 512), (512, 512), (2048, 1024), (512, 2048), (1024, 1024)])]
+    hdrs, packed = decoder.pack_batch([im.stream for im in imgs])
+    want = np.concatenate([im.blocks for im in imgs])
+    h_cmp = torch.from_numpy(packed).pin_memory()
+    h_out = torch.zeros(sum(h.dxt_bytes for h in hdrs), dtype=torch.uint8).pin_memory()
+    s = torch.cuda.Stream()
+    for _ in range(2):
+        h_out.zero_()
+        decoder.load_host_dxts(gpu_ctx, hdrs, h_cmp, h_out, chunks, s)
+        s.synchronize()
+        assert decoder.sync_status(gpu_ctx, s) == decoder.GST_OK
+        assert np.array_equal(h_out.numpy().view(np.uint64), want)

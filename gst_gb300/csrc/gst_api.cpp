@@ -112,6 +112,8 @@ struct gst_ctx {
   size_t out_h_cap = 0;
   int last_launches = 0;
   GstTuning tuning;  // rANS launch configuration of the context's calls and untuned batches
+  uint64_t wait_limit_ns = 0;  // persistent tile wait bound (0: the kernel's 2 s)
+  bool inject_drop_rans = false;  // fault injection for tests: persistent launches without their rANS items
   // Instrumentation: events around each kernel of the last decode call.
   bool profiling = false;
   cudaEvent_t ev[kMaxTimedKernels + 1] = {};
@@ -217,7 +219,10 @@ gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, const
   if (e != cudaSuccess) return cuda_status(e);
   if (!cap) cudaEventRecord(pb->copied, stream);
   cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
-  e = launch_decode(d_cmp, d_scratch, d_out, view, stream, &ctx->last_launches, ev, ctx->tuning, ctx->timed_names);
+  GstPlanView v = view;
+  v.wait_limit_ns = ctx->wait_limit_ns;
+  if (ctx->inject_drop_rans && ctx->tuning.persistent && v.sync) v.n_rans = 0;
+  e = launch_decode(d_cmp, d_scratch, d_out, v, stream, &ctx->last_launches, ev, ctx->tuning, ctx->timed_names);
   ctx->timed_kernels = ev ? ctx->last_launches : 0;
   if (e != cudaSuccess) return cuda_status(e);
   if (!cap) {
@@ -968,6 +973,16 @@ gst_status gst_set_option(gst_ctx *ctx, const char *name, int value) {
   if (strcmp(name, "persistent") == 0) {
     if (value != 0 && value != 1) return GST_E_ARG;
     ctx->tuning.persistent = value;
+    return GST_OK;
+  }
+  if (strcmp(name, "persistent_wait_us") == 0) {
+    if (value < 0 || value > 2000000) return GST_E_ARG;
+    ctx->wait_limit_ns = uint64_t(value) * 1000u;
+    return GST_OK;
+  }
+  if (strcmp(name, "inject_drop_rans") == 0) {
+    if (value != 0 && value != 1) return GST_E_ARG;
+    ctx->inject_drop_rans = value != 0;
     return GST_OK;
   }
   return GST_E_ARG;

@@ -410,23 +410,6 @@ __global__ void __launch_bounds__(128, MINB) gst_rans_kernel(const uint8_t *__re
 }
 
 // ---------------------------------------------------------------------------
-// C's truncating u / 4 and u / 2 for signed u, as floor division of u plus
-// (divisor - 1) when u < 0.  The sign (-1 or 0) comes from a high multiply
-// and the correction from a multiply-add, so two of the three instructions
-// issue to the FMA pipe; the integer ALU pipe keeps the shift.
-__device__ __forceinline__ int32_t trunc_div4(int32_t u) {
-  int32_t sgn, v;
-  asm("mul.hi.s32 %0, %1, 2;" : "=r"(sgn) : "r"(u));          // -1 if u < 0, else 0 (|u| < 2^30)
-  asm("mad.lo.s32 %0, %1, -3, %2;" : "=r"(v) : "r"(sgn), "r"(u));
-  return v >> 2;
-}
-__device__ __forceinline__ int32_t trunc_div2(int32_t u) {
-  int32_t sgn, v;
-  asm("mul.hi.s32 %0, %1, 2;" : "=r"(sgn) : "r"(u));
-  asm("mad.lo.s32 %0, %1, -1, %2;" : "=r"(v) : "r"(sgn), "r"(u));
-  return v >> 1;
-}
-
 // Byte (SEL & 7) of w sign-extended to 32 bits: a byte permute whose upper
 // selector nibbles have the sign-replicate bit set (prmt's default mode).
 template <uint32_t SEL>
@@ -448,12 +431,12 @@ __device__ __forceinline__ void inv53_line(int32_t *p, int step) {
   for (int x = 0; x < mid; ++x) {
     const int prev = mid + (x > 0 ? x - 1 : 0);  // mid + NormalizeIndex(2x-1, L)/2
     const int next = mid + x;                    // mid + NormalizeIndex(2x+1, L)/2
-    d[2 * x] = s[x] - trunc_div4(s[prev] + s[next] + 2);
+    d[2 * x] = s[x] - (s[prev] + s[next] + 2) / 4;
   }
 #pragma unroll
   for (int x = 0; x < mid; ++x) {
     const int nx = (2 * x + 2 < L) ? 2 * x + 2 : L - 2;  // NormalizeIndex(2x+2, L)
-    d[2 * x + 1] = s[mid + x] + trunc_div2(d[2 * x] + d[nx]);
+    d[2 * x + 1] = s[mid + x] + (d[2 * x] + d[nx]) / 2;
   }
 #pragma unroll
   for (int k = 0; k < L; ++k) p[k * step] = d[k];
@@ -676,8 +659,8 @@ __device__ __forceinline__ uint64_t global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // a tile waits at most 2 s for its image
-constexpr uint32_t kWaitLimitSpins = 1u << 24;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // default: a tile waits at most 2 s for its image
+constexpr uint32_t kWaitLimitSpins = 1u << 24;   // and at most this many polls
 
 __host__ __device__ constexpr size_t persistent_smem_bytes(uint32_t stage_words) {
   return rans_smem_bytes(stage_words) > kTileSmemBytes ? rans_smem_bytes(stage_words) : kTileSmemBytes;
@@ -715,10 +698,11 @@ __global__ void __launch_bounds__(128, 8) gst_persistent_kernel(const uint8_t *_
         uint32_t ok = 1;
         if (ld_acquire(ready + it.image) < need) {
           const uint64_t t0 = global_ns();
+          const uint64_t limit = plan.wait_limit_ns ? plan.wait_limit_ns : kWaitLimitNs;
           for (uint32_t spin = 0;; ++spin) {
             __nanosleep(256);
             if (ld_acquire(ready + it.image) >= need) break;
-            if (spin > kWaitLimitSpins || global_ns() - t0 > kWaitLimitNs) {
+            if (spin > kWaitLimitSpins || global_ns() - t0 > limit) {
               ok = 0;
               flag_error(plan.err, image_err, kErrTimeout);
               break;

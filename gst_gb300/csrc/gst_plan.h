@@ -98,6 +98,7 @@ struct GstPlanView {
   // Persistent kernel (may be null otherwise): [0] work-queue head, [1] CTAs
   // finished, [4 + i] groups of image i decoded.  Every launch leaves them 0.
   uint32_t *sync;
+  uint64_t wait_limit_ns;  // bound of a persistent tile's wait for its image (0: 2 s)
   uint32_t n_images;
   uint32_t rgb;  // 1: the tiles write RGB8 pixels (48 bytes per block) instead of DXT1
   uint32_t n_rans, n_tiles;

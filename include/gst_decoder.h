@@ -234,6 +234,12 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
  *                         (a tile waits, bounded, for its image's groups;
  *                         GST_E_TIMEOUT from gst_sync_status if it gave up).
  *                         gst_decode_rans_groups always uses the rANS kernel.
+ *   "persistent_wait_us"  bound of a persistent tile's wait for its image,
+ *                         microseconds (0 = 2 s, at most 2,000,000).
+ *   "inject_drop_rans"    fault injection for tests, 0 (default) or 1: the
+ *                         context's persistent launches leave out their rANS
+ *                         items, so every tile waits until its bound and the
+ *                         call reports GST_E_TIMEOUT; the decode is void.
  * Invalid values and unknown names return GST_E_ARG.  They apply to the
  * context's calls and to resident batches without a tuning of their own;
  * such batches re-capture their graph after a change. */

@@ -365,3 +365,26 @@ def test_load_host_dxts_pipelined(gpu_ctx, chunks):
         s.synchronize()
         assert decoder.sync_status(gpu_ctx, s) == decoder.GST_OK
         assert np.array_equal(h_out.numpy().view(np.uint64), want)
+
+
+def test_persistent_wait_times_out_and_context_survives():
+    # Fault injection on the host: the persistent launch leaves out its rANS
+    # items, so every tile's bounded wait runs out (1 ms here) and the call
+    # reports GST_E_TIMEOUT; the context then decodes normally.
+    ctx = decoder.GPUContext(0)
+    try:
+        im = workloads.encode_image(512, 512, 860)
+        hdrs, packed = decoder.pack_batch([im.stream])
+        d_cmp = torch.from_numpy(packed).cuda()
+        d_out = torch.zeros(hdrs[0].dxt_bytes, dtype=torch.uint8, device="cuda")
+        ctx.set_option("persistent", 1)
+        ctx.set_option("persistent_wait_us", 1000)
+        ctx.set_option("inject_drop_rans", 1)
+        decoder.load_compressed_dxts(ctx, hdrs, d_cmp, d_out)
+        assert decoder.sync_status(ctx) == decoder.GST_E_TIMEOUT
+        ctx.set_option("inject_drop_rans", 0)
+        decoder.load_compressed_dxts(ctx, hdrs, d_cmp, d_out)
+        assert decoder.sync_status(ctx) == decoder.GST_OK
+        assert np.array_equal(d_out.cpu().numpy().view(np.uint64), im.blocks)
+    finally:
+        ctx.close()

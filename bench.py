@@ -212,10 +212,12 @@ class Batch:
         return np.concatenate([im.blocks for im in self.images])
 
 
-def time_steps(fn, steps, warmup, stream, flush, ctx=None):
+def time_steps(fn, steps, warmup, stream, flush, ctx=None, clear=None):
     """Runs fn() warmup + steps times; returns per-step device ms (CUDA events
     on `stream`, L2 flushed before each step outside the events) and the
-    per-kernel ms of each step."""
+    per-kernel ms of each step.  `clear` (a tensor) is zeroed before every
+    step outside the events, so that the output checked after the last step
+    is that step's own work."""
     import torch
     kern = []
     for _ in range(warmup):
@@ -224,6 +226,8 @@ def time_steps(fn, steps, warmup, stream, flush, ctx=None):
     times = []
     for _ in range(steps):
         with torch.cuda.stream(stream):
+            if clear is not None:
+                clear.zero_()
             flush.zero_()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
@@ -283,8 +287,9 @@ def run_only(args, local):
         rb = decoder.ResidentBatch(ctx, b.hdrs)
         tuning = tune(rb, b, stream, args)
         fn = lambda: rb.launch(b.d_cmp, b.d_out, stream, graph=True)  # noqa: E731
-        t, _ = time_steps(fn, args.steps, args.warmup, stream, flush)
+        t, _ = time_steps(fn, args.steps, args.warmup, stream, flush, clear=b.d_out)
         ok = bool(np.array_equal(b.d_out.cpu().numpy().view(np.uint64), b.expected()))
+        ok = ok and decoder.sync_status(ctx, stream) == decoder.GST_OK
         units = b.pixels
         rb.close()
     ctx.close()
@@ -337,7 +342,7 @@ def run_gst(args, rank, world, local):
     peak, peak_kind = measured_peak_hbm()
     barrier(world)
     with ClockSampler(local) as clocks:
-        times, _ = time_steps(step_batched, args.steps, args.warmup, stream, flush)
+        times, _ = time_steps(step_batched, args.steps, args.warmup, stream, flush, clear=batch.d_out)
     clock = clocks.summary()
     stream.synchronize()
     got = batch.d_out.cpu().numpy().view(np.uint64)
@@ -356,7 +361,7 @@ def run_gst(args, rank, world, local):
     dominant = max(ksum.items(), key=lambda kv: kv[1]["share"])[0] if ksum else None
 
     # per-image path
-    t_img, _ = time_steps(step_per_image, max(3, args.steps // 4), 2, stream, flush)
+    t_img, _ = time_steps(step_per_image, max(3, args.steps // 4), 2, stream, flush, clear=batch.d_out)
     per_image_ms = statistics.mean(t_img)
     got_pi = batch.d_out.cpu().numpy().view(np.uint64)
     per_image_exact = bool(np.array_equal(got_pi, batch.expected()))
@@ -371,7 +376,7 @@ def run_gst(args, rank, world, local):
             best = (c, statistics.mean(t_c))
     chunks = best[0]
     batch.h_out.zero_()
-    t_e2e, _ = time_steps(step_e2e, args.steps, args.warmup, stream, flush)
+    t_e2e, _ = time_steps(step_e2e, args.steps, args.warmup, stream, flush, clear=batch.h_out)
     e2e_total = max_over_ranks(sum(t_e2e), world)
     e2e_value = world * batch.pixels * args.steps / (e2e_total / 1e3) / 1e6
     stream.synchronize()
@@ -460,8 +465,9 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
         rb = decoder.ResidentBatch(ctx, b.hdrs)
         tuning = tune(rb, b, stream, args)
         fn = lambda b=b, rb=rb: rb.launch(b.d_cmp, b.d_out, stream, graph=True)  # noqa: E731
-        t, _ = time_steps(fn, steps, 3, stream, flush)
+        t, _ = time_steps(fn, steps, 3, stream, flush, clear=b.d_out)
         ok = bool(np.array_equal(b.d_out.cpu().numpy().view(np.uint64), b.expected()))
+        ok = ok and decoder.sync_status(ctx, stream) == decoder.GST_OK
         ctx.set_profiling(True)
         _, k = time_steps(lambda b=b, rb=rb: rb.launch(b.d_cmp, b.d_out, stream), 3, 1, stream, flush, ctx)
         ctx.set_profiling(False)

@@ -315,7 +315,7 @@ void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph,
 }
 
 GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) {
-  GstPlanView view;
+  GstPlanView view = {};  // every field: wait_limit_ns 0 is the kernel's default bound
   view.err = status_d;
   view.images = reinterpret_cast<const GstImageDesc *>(plan_d + L.off_images);
   view.rans = reinterpret_cast<const GstRansItem *>(plan_d + L.off_rans);
@@ -413,9 +413,10 @@ bool valid_tuning(int blocks_per_sm, int stage_words, int persistent = 0) {
 cudaError_t batch_launch_locked(gst_batch *b, const void *d_cmp, void *d_out, cudaStream_t st, const GstTuning &t,
                                 cudaEvent_t *ev) {
   gst_ctx *ctx = b->ctx;
-  return launch_decode(static_cast<const uint8_t *>(d_cmp), b->scratch, static_cast<uint8_t *>(d_out),
-                       plan_view(b->layout, b->plan_d, ctx->status_d), st, &ctx->last_launches, ev, t,
-                       ctx->timed_names);
+  GstPlanView view = plan_view(b->layout, b->plan_d, ctx->status_d);
+  view.wait_limit_ns = ctx->wait_limit_ns;
+  return launch_decode(static_cast<const uint8_t *>(d_cmp), b->scratch, static_cast<uint8_t *>(d_out), view, st,
+                       &ctx->last_launches, ev, t, ctx->timed_names);
 }
 
 }  // namespace
@@ -1010,9 +1011,10 @@ gst_status gst_batch_autotune(gst_batch *b, const void *d_cmp, void *d_out, void
   gst_ctx *ctx = b->ctx;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (capturing(st)) return GST_E_ARG;
-  // Two kernels: CTAs per SM x staging depth, the deepest stages that the
-  // shared memory of that many CTAs per SM holds and shallower ones.  The
-  // persistent kernel: its tile buffers fit 2040-word stages at 8 CTAs per SM.
+  // Two kernels: CTAs of 128 threads per SM x staging depth, the deepest
+  // stages that the shared memory of that many CTAs per SM holds and
+  // shallower ones.  The persistent kernel (8 CTAs of 128 threads per SM):
+  // its tile buffers hold 2040-word stages.
   static const GstTuning kCandidates[] = {
       {16, 520, 0}, {12, 520, 0}, {12, 1016, 0}, {8, 1528, 0}, {8, 2040, 0}, {8, 2816, 0},
       {8, 1016, 1}, {8, 2040, 1},

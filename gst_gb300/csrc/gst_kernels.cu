@@ -42,6 +42,10 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 
 // Error bits go to the call's status word and, where the plan has them, to the
 // image's own word (so that a batch can report per image).
+// Barrier `id` over `n` threads (a multiple of 32): id 0 over the whole CTA is
+// __syncthreads; the persistent kernel's two rANS halves use ids 1 and 2.
+__device__ __forceinline__ void bar_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
 __device__ __forceinline__ void flag_error(uint32_t *err, uint32_t *image_err, uint32_t bits) {
   atomicOr(err, bits);
   if (image_err) atomicOr(image_err, bits);
@@ -58,13 +62,14 @@ __device__ __forceinline__ void flag_error(uint32_t *err, uint32_t *image_err, u
 // Built without searching: each symbol with freq > 0 marks its first slot,
 // and since those first slots increase with x, a running maximum of the marks
 // over the slots gives every slot's symbol.  Entry = (freq << 11 | x << 24) -
-// cum + s, from one per-symbol word.  Requires blockDim.x == 128; `work` is
-// 3 KB of shared scratch (per-symbol words, slot marks) that is free again on
-// return.  Returns false (block-uniformly) if the frequencies do not sum to
-// 2048.
+// cum + s, from one per-symbol word.  Run by 128 threads (t = 0..127) that
+// synchronise on named barrier BAR; `work` is 3 KB of shared scratch
+// (per-symbol words, slot marks) that is free again on return.  Returns false
+// (uniformly over the 128 threads) if the frequencies do not sum to 2048.
+template <int BAR>
 __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t *tbl, uint32_t *wred,
-                                   uint8_t *work) {
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+                                   uint8_t *work, int t) {
+  const int lane = t & 31, warp = t >> 5;
   uint32_t *sym_word = reinterpret_cast<uint32_t *>(work);  // 256
   uint8_t *marks = work + 1024;                             // 2048
   reinterpret_cast<uint4 *>(marks)[t] = make_uint4(0, 0, 0, 0);
@@ -76,7 +81,7 @@ __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t 
     if (lane >= d) v += n;
   }
   if (lane == 31) wred[warp] = v;
-  __syncthreads();
+  bar_sync(BAR, 128);
   uint32_t woff = 0;
 #pragma unroll
   for (int w = 0; w < 4; ++w) woff += (w < warp) ? wred[w] : 0u;
@@ -89,7 +94,7 @@ __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t 
     if (f0) marks[c0] = static_cast<uint8_t>(x0);
     if (f1) marks[c1] = static_cast<uint8_t>(x1);
   }
-  __syncthreads();
+  bar_sync(BAR, 128);
   if (total != kTableSize) return false;
   // Thread t owns slots [16t, 16t + 16): running maximum within, then an
   // exclusive maximum over the preceding threads.
@@ -110,7 +115,7 @@ __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t 
   if (lane == 31) wred[4 + warp] = incl;
   uint32_t excl = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
   if (lane == 0) excl = 0;
-  __syncthreads();
+  bar_sync(BAR, 128);
 #pragma unroll
   for (int w = 0; w < 3; ++w)
     if (w < warp) excl = max(excl, wred[4 + w]);
@@ -122,7 +127,7 @@ __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t 
   dst[1] = make_uint4(e[4], e[5], e[6], e[7]);
   dst[2] = make_uint4(e[8], e[9], e[10], e[11]);
   dst[3] = make_uint4(e[12], e[13], e[14], e[15]);
-  __syncthreads();
+  bar_sync(BAR, 128);
   return true;
 }
 
@@ -380,19 +385,22 @@ __device__ __forceinline__ void rans_group(const uint8_t *__restrict__ cmp, uint
 }
 
 // One rANS work item: ngroups <= 4 groups of one section, group first_group + w
-// decoded by warp w.  The CTA is 128 threads; all of them return.
+// decoded by warp w of a group of 128 threads (t = 0..127) that owns the
+// shared memory at `smem` (rans_smem_bytes(stage_words)) and named barrier
+// BAR; all of them return.
+template <int BAR>
 __device__ __forceinline__ void rans_item(const uint8_t *__restrict__ cmp, uint8_t *__restrict__ scratch,
                                           uint32_t *err, uint32_t *image_err, uint32_t *counter,
                                           const GstImageDesc &im, uint32_t section, uint32_t first_group,
-                                          uint32_t ngroups, uint32_t ns, uint32_t stage_words) {
-  extern __shared__ __align__(16) uint8_t smem_raw[];
-  RansHead &sm = *reinterpret_cast<RansHead *>(smem_raw);
+                                          uint32_t ngroups, uint32_t ns, uint32_t stage_words, uint8_t *smem,
+                                          int t) {
+  RansHead &sm = *reinterpret_cast<RansHead *>(smem);
   const uint16_t *freqs = reinterpret_cast<const uint16_t *>(cmp + im.freq_off + kFreqTableBytes * section);
-  const bool table_ok = build_decode_table(freqs, sm.tbl, sm.wred, smem_raw + kStageOffset);
-  if (!table_ok && threadIdx.x == 0) flag_error(err, image_err, kErrTable);
-  const uint32_t warp = threadIdx.x >> 5;
+  const bool table_ok = build_decode_table<BAR>(freqs, sm.tbl, sm.wred, smem + kStageOffset, t);
+  if (!table_ok && t == 0) flag_error(err, image_err, kErrTable);
+  const uint32_t warp = static_cast<uint32_t>(t) >> 5;
   if (warp < ngroups) {
-    uint16_t *stage = reinterpret_cast<uint16_t *>(smem_raw + kStageOffset) + warp * (stage_words + 8);
+    uint16_t *stage = reinterpret_cast<uint16_t *>(smem + kStageOffset) + warp * (stage_words + 8);
     rans_group(cmp, scratch, err, image_err, counter, im, section, first_group + warp, ns, table_ok, sm.tbl, stage,
                stage_words);
   }
@@ -404,9 +412,11 @@ __device__ __forceinline__ void rans_item(const uint8_t *__restrict__ cmp, uint8
 template <int MINB>
 __global__ void __launch_bounds__(128, MINB) gst_rans_kernel(const uint8_t *__restrict__ cmp,
                                                              uint8_t *__restrict__ scratch, GstPlanView plan) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
   const GstRansItem it = plan.rans[blockIdx.x];
-  rans_item(cmp, scratch, plan.err, plan.image_err ? plan.image_err + it.image : nullptr, plan.counters + it.image,
-            plan.images[it.image], it.section, it.first_group, it.ngroups, it.streams, plan.stage_words);
+  rans_item<0>(cmp, scratch, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
+               plan.counters + it.image, plan.images[it.image], it.section, it.first_group, it.ngroups, it.streams,
+               plan.stage_words, smem_raw, threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -649,6 +659,8 @@ __global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict
 // before the tile and is held by a running CTA that never waits, so the
 // waits end whether or not all CTAs are resident.  The last CTA to finish
 // re-arms the queue and the counters, so a resident plan can be relaunched.
+// (CTAs of 256 threads taking rANS items in pairs measured slower: at 48
+// registers they spill, at 64 only four fit per SM.)
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
   uint32_t v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -661,14 +673,16 @@ __device__ __forceinline__ uint64_t global_ns() {
 }
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // default: a tile waits at most 2 s for its image
 constexpr uint32_t kWaitLimitSpins = 1u << 24;   // and at most this many polls
+constexpr int kPersistentThreads = 128;
 
 __host__ __device__ constexpr size_t persistent_smem_bytes(uint32_t stage_words) {
   return rans_smem_bytes(stage_words) > kTileSmemBytes ? rans_smem_bytes(stage_words) : kTileSmemBytes;
 }
 
-__global__ void __launch_bounds__(128, 8) gst_persistent_kernel(const uint8_t *__restrict__ cmp,
-                                                                uint8_t *__restrict__ scratch,
-                                                                uint8_t *__restrict__ out, GstPlanView plan) {
+__global__ void __launch_bounds__(kPersistentThreads, 8) gst_persistent_kernel(const uint8_t *__restrict__ cmp,
+                                                                               uint8_t *__restrict__ scratch,
+                                                                               uint8_t *__restrict__ out,
+                                                                               GstPlanView plan) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   __shared__ uint32_t item_s, ok_s;
   uint32_t *queue = plan.sync, *exits = plan.sync + 1, *ready = plan.sync + 4;
@@ -681,9 +695,9 @@ __global__ void __launch_bounds__(128, 8) gst_persistent_kernel(const uint8_t *_
     if (item >= n_items) break;
     if (item < plan.n_rans) {
       const GstRansItem it = plan.rans[item];
-      rans_item(cmp, scratch, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
-                plan.counters + it.image, plan.images[it.image], it.section, it.first_group, it.ngroups, it.streams,
-                plan.stage_words);
+      rans_item<0>(cmp, scratch, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
+                   plan.counters + it.image, plan.images[it.image], it.section, it.first_group, it.ngroups,
+                   it.streams, plan.stage_words, smem_raw, threadIdx.x);
       __syncthreads();
       if (threadIdx.x == 0) {
         __threadfence();
@@ -712,7 +726,9 @@ __global__ void __launch_bounds__(128, 8) gst_persistent_kernel(const uint8_t *_
         ok_s = ok;
       }
       __syncthreads();
-      if (ok_s) tile_work<128, true>(scratch, out, plan.err, image_err, im, it.tile, reinterpret_cast<int32_t *>(smem_raw));
+      if (ok_s)
+        tile_work<kPersistentThreads, true>(scratch, out, plan.err, image_err, im, it.tile,
+                                            reinterpret_cast<int32_t *>(smem_raw));
     }
   }
   if (threadIdx.x == 0) {
@@ -758,10 +774,10 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gst_persistent_kernel, 128, smem);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gst_persistent_kernel, kPersistentThreads, smem);
     if (e != cudaSuccess) return e;
     const uint32_t grid = std::min<uint32_t>(plan.n_rans + plan.n_tiles, uint32_t(std::max(1, sms * per_sm)));
-    gst_persistent_kernel<<<grid, 128, smem, stream>>>(d_cmp, d_scratch, d_out, plan);
+    gst_persistent_kernel<<<grid, kPersistentThreads, smem, stream>>>(d_cmp, d_scratch, d_out, plan);
     if (names) names[*launches] = "gst_persistent_kernel";
     ++*launches;
     if (ev) cudaEventRecord(ev[*launches], stream);
@@ -840,9 +856,10 @@ __global__ void __launch_bounds__(128) gst_rans_static_kernel(const uint8_t *__r
   }
   const uint32_t first = b * kGroupsPerRansCta;
   const uint32_t ngroups = min(kGroupsPerRansCta, im.sec_groups[section] - first);
+  extern __shared__ __align__(16) uint8_t smem_raw[];
   uint32_t *err = reinterpret_cast<uint32_t *>(base);
-  rans_item(cmp, base + kStaticHeaderBytes, err, nullptr, err + 1, im, section, first, ngroups, kStreamsPerGroup,
-            kDefaultStageWords);
+  rans_item<0>(cmp, base + kStaticHeaderBytes, err, nullptr, err + 1, im, section, first, ngroups,
+               kStreamsPerGroup, kDefaultStageWords, smem_raw, threadIdx.x);
 }
 
 // gst_tile_kernel for a single image whose descriptor arrives by value; the

@@ -222,7 +222,8 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
  * sizes are fixed, codec/decoder.cpp:166-417).  Known names:
  *   "rans_blocks_per_sm"  register budget of the rANS kernel in CTAs of 128
  *                         threads per SM: 1-9 (eight, 64 registers), 10-13
- *                         (twelve, default) or 14-16 (sixteen).
+ *                         (twelve, default) or 14-16 (sixteen).  The
+ *                         persistent kernel always runs 8 per SM.
  *   "rans_stage_words"    16-bit renormalisation words each warp stages in
  *                         shared memory: a multiple of 8 in [520, 2816];
  *                         default 1016.  Deeper stages re-stage less often

@@ -213,14 +213,12 @@ __device__ __forceinline__ uint32_t mul_hi(uint32_t a, uint32_t b) {
 //   e' = e mod 2^24 (the freq << 11 term cancels), and the slot's byte offset
 //   4x - 8192 q, all as multiply-adds.  Renormalising lanes read consecutive
 //   words below the read pointer, the lowest lane the lowest address
-//   (ans_decode.cl:133-140); lane l's word lies popc(renormalising lanes >= l)
-//   words below the pointer.  Every lane prefetches, off the dependency chain,
-//   the word d = l (d = 32 for lane 0) below the pointer, so a shuffle from
-//   lane (d mod 32) hands each renormalising lane its word.
+//   (ans_decode.cl:133-140): lane l's word lies popc(renormalising lanes >= l)
+//   words below the pointer, and only those lanes load it from the stage.
 // For a valid stream the read pointer never goes below the staged words; a
 // malformed one is caught at the end of a 16-step run (the pointer is then
-// clamped so that every prefetch stays inside the CTA's shared memory) or by
-// the final pointer.
+// clamped so that every read stays inside the CTA's shared memory) or by the
+// final pointer.
 template <bool INDEX>
 __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, uint32_t lo, uint32_t top,
                                              const uint32_t *__restrict__ tbl, uint16_t *stage, uint32_t stage_words,
@@ -237,7 +235,6 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
   uint32_t x = active ? reinterpret_cast<const uint32_t *>(sec + top)[lane] : kRansL;
   int ptr = static_cast<int>(top >> 1);      // word index of the section
   uint32_t s2 = 2u * (ptr - sbase16);        // byte offset of word ptr in the stage
-  const uint32_t pre_off = 0u - 2u * static_cast<uint32_t>(lane == 0 ? 32 : lane);
   const uint32_t ge = ~lanemask_lt();
   bool bad = false;
   uint32_t total_sym = 0;
@@ -261,7 +258,6 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
     uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      const uint32_t pre = *reinterpret_cast<const uint16_t *>(stage_bytes + static_cast<int>(s2 + pre_off));
       const uint32_t qm = mad_hi(x, 1u << 21, 0u - 2048u);                          // q - 2048
       const uint32_t off = mad_lo(qm, 0u - 8192u, mad_lo(x, 4u, 0u - (1u << 24)));  // 4 (x mod 2048)
       const uint32_t e = *reinterpret_cast<const uint32_t *>(tbl_bytes + off);
@@ -269,8 +265,11 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
       x = mad_lo(mul_hi(ec, 1u << 21), qm, ec);
       const bool need = active && x < kRansL;
       const uint32_t m = __ballot_sync(0xFFFFFFFFu, need);
-      const uint32_t v = __shfl_sync(0xFFFFFFFFu, pre, __popc(m & ge));
-      if (need) x = mad_lo(x, 65536u, v);
+      if (need) {
+        const uint32_t depth2 = 2u * static_cast<uint32_t>(__popc(m & ge));
+        const uint32_t v = *reinterpret_cast<const uint16_t *>(stage_bytes + static_cast<int>(s2 - depth2));
+        x = mad_lo(x, 65536u, v);
+      }
       s2 = mad_lo(static_cast<uint32_t>(__popc(m)), 0u - 2u, s2);
       // Steps 16k..16k+15 are positions 255-16k .. 240-16k of this stream
       // (ans_decode.cl:154-155 stores the symbols in reverse).

@@ -431,11 +431,8 @@ __device__ __forceinline__ int32_t sext_byte(uint32_t w) {
 // Inverse 5/3 lifting of one line of length L in place, with the arithmetic of
 // inverse_wavelet.cl:28-64 (NormalizeIndex mirroring; C division).
 template <int L>
-__device__ __forceinline__ void inv53_line(int32_t *p, int step) {
+__device__ __forceinline__ void inv53_lift(const int32_t (&s)[L], int32_t (&d)[L]) {
   constexpr int mid = L / 2;
-  int32_t s[L], d[L];
-#pragma unroll
-  for (int k = 0; k < L; ++k) s[k] = p[k * step];
 #pragma unroll
   for (int x = 0; x < mid; ++x) {
     const int prev = mid + (x > 0 ? x - 1 : 0);  // mid + NormalizeIndex(2x-1, L)/2
@@ -447,12 +444,35 @@ __device__ __forceinline__ void inv53_line(int32_t *p, int step) {
     const int nx = (2 * x + 2 < L) ? 2 * x + 2 : L - 2;  // NormalizeIndex(2x+2, L)
     d[2 * x + 1] = s[mid + x] + (d[2 * x] + d[nx]) / 2;
   }
+}
+
+template <int L>
+__device__ __forceinline__ void inv53_line(int32_t *p, int step) {
+  int32_t s[L], d[L];
+#pragma unroll
+  for (int k = 0; k < L; ++k) s[k] = p[k * step];
+  inv53_lift<L>(s, d);
 #pragma unroll
   for (int k = 0; k < L; ++k) p[k * step] = d[k];
 }
 
+// The 16 coefficients (byte - 128) of a 16-byte chunk: the byte with its top
+// bit flipped, sign-extended by one byte permute.
+__device__ __forceinline__ void unpack16(uint4 cv, int32_t *dst) {
+  const uint32_t w[4] = {cv.x ^ 0x80808080u, cv.y ^ 0x80808080u, cv.z ^ 0x80808080u, cv.w ^ 0x80808080u};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    dst[4 * k + 0] = sext_byte<0x8880u>(w[k]);
+    dst[4 * k + 1] = sext_byte<0x9991u>(w[k]);
+    dst[4 * k + 2] = sext_byte<0xAAA2u>(w[k]);
+    dst[4 * k + 3] = sext_byte<0xBBB3u>(w[k]);
+  }
+}
+
 constexpr int kPlanePitch = 33;  // row pitch in words: rows and columns both bank-conflict free
-constexpr int kPlaneWords = 32 * kPlanePitch;
+// Planes 16 banks apart, so that half-warps working on two planes at once do
+// not collide.
+constexpr int kPlaneWords = 32 * kPlanePitch + 16;
 
 // One level over the top-left L x L of all six planes: rows, then columns;
 // NT threads take the 6L lines of each pass.
@@ -541,7 +561,7 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
                                           uint32_t tile, int32_t *pl) {
   constexpr int kWarps = NT / 32;
   constexpr int kRows = 32 / kWarps;            // block rows a warp assembles
-  constexpr int kChunks = (384 + NT - 1) / NT;  // 16-byte plane chunks a thread loads
+  constexpr int kOwn = (192 + NT - 1) / NT;     // coefficient rows (of the six planes) a thread owns
   const size_t B = static_cast<size_t>(im.bx) * im.by;
   const uint32_t tx = tile % im.tiles_x, ty = tile / im.tiles_x;
   const uint8_t *sym = scratch + im.sym_off;
@@ -549,15 +569,24 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
 
   // 1. The tile's 1024 coefficients of plane p are the tile-th 1024-byte run of
   //    the plane (inverse_wavelet.cl:79-104); planes Y1 Y2 Co1 Cg1 Co2 Cg2 are
-  //    consecutive B-byte runs of the decoded Y and chroma sections: 384
-  //    16-byte chunks.
+  //    consecutive B-byte runs of the decoded Y and chroma sections.  A thread
+  //    owns whole coefficient rows (line l: plane 2 (w mod 3) + lane / 16, row
+  //    16 (w / 3) + lane mod 16, w = l / 32, so "row < 16" is warp-uniform) and
+  //    keeps their 32 bytes in registers: only rows < 16, columns < 16 -- the
+  //    part levels 2..16 work on -- go to shared memory before level 32.
   const uint8_t *tile_base = sym + static_cast<size_t>(tile) * 1024;
-  uint4 c[kChunks];
+  uint4 raw_lo[kOwn], raw_hi[kOwn];
 #pragma unroll
-  for (int k = 0; k < kChunks; ++k) {
-    const int chunk = t + k * NT;
-    c[k] = make_uint4(0, 0, 0, 0);
-    if (chunk < 384) c[k] = ld_sym<COH>(reinterpret_cast<const uint4 *>(tile_base + (chunk >> 6) * B) + (chunk & 63));
+  for (int k = 0; k < kOwn; ++k) {
+    const int l = t + k * NT;
+    raw_lo[k] = raw_hi[k] = make_uint4(0, 0, 0, 0);
+    if (l < 192) {
+      const int w = l >> 5, ln = l & 31;
+      const int p = 2 * (w % 3) + (ln >> 4), r = 16 * (w / 3) + (ln & 15);
+      const uint4 *row = reinterpret_cast<const uint4 *>(tile_base + p * B + r * 32);
+      raw_lo[k] = ld_sym<COH>(row);
+      raw_hi[k] = ld_sym<COH>(row + 1);
+    }
   }
 
   // 2. Palette indices of the rows this thread assembles (rows warp + kWarps i,
@@ -574,23 +603,21 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
               static_cast<uint32_t>(ld_sym<COH>(chunk_pref + (p0 >> 5)));
   }
 
-  // 3. Coefficients to int32 (byte - 128), rows of pitch kPlanePitch: the
-  //    byte with its top bit flipped, sign-extended by one byte permute.
-  auto unpack = [&](uint4 cv, int chunk) {
-    const int p = chunk >> 6, q = chunk & 63;  // plane, 16-byte chunk in the plane's block
-    int32_t *dst = pl + p * kPlaneWords + (q >> 1) * kPlanePitch + (q & 1) * 16;
-    const uint32_t w[4] = {cv.x ^ 0x80808080u, cv.y ^ 0x80808080u, cv.z ^ 0x80808080u, cv.w ^ 0x80808080u};
+  // 3. The top-left 16x16 of each plane to int32 shared memory (pitch
+  //    kPlanePitch), byte - 128.
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      dst[4 * k + 0] = sext_byte<0x8880u>(w[k]);
-      dst[4 * k + 1] = sext_byte<0x9991u>(w[k]);
-      dst[4 * k + 2] = sext_byte<0xAAA2u>(w[k]);
-      dst[4 * k + 3] = sext_byte<0xBBB3u>(w[k]);
+  for (int k = 0; k < kOwn; ++k) {
+    const int l = t + k * NT;
+    if (l < 96) {  // rows < 16
+      const int w = l >> 5, ln = l & 31;
+      const int p = 2 * w + (ln >> 4), r = ln & 15;
+      int32_t v[16];
+      unpack16(raw_lo[k], v);
+      int32_t *dst = pl + p * kPlaneWords + r * kPlanePitch;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) dst[j] = v[j];
     }
-  };
-#pragma unroll
-  for (int k = 0; k < kChunks; ++k)
-    if (t + k * NT < 384) unpack(c[k], t + k * NT);
+  }
 
   // 4. Finish the index prefix sums (warp scans) and start the palette gathers.
   const uint32_t *pal = reinterpret_cast<const uint32_t *>(sym + im.sec_out[2]);
@@ -610,12 +637,37 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
   }
   __syncthreads();
 
-  // 5. Five levels of the inverse 5/3 wavelet.
+  // 5. Five levels of the inverse 5/3 wavelet.  Level 32's row pass takes each
+  //    row from its owner: columns < 16 from shared memory for rows < 16,
+  //    everything else straight from the row's bytes in registers.
   inv53_level<2, NT>(pl);
   inv53_level<4, NT>(pl);
   inv53_level<8, NT>(pl);
   inv53_level<16, NT>(pl);
-  inv53_level<32, NT>(pl);
+#pragma unroll
+  for (int k = 0; k < kOwn; ++k) {
+    const int l = t + k * NT;
+    if (l < 192) {
+      const int w = l >> 5, ln = l & 31;
+      const int p = 2 * (w % 3) + (ln >> 4), r = 16 * (w / 3) + (ln & 15);
+      int32_t *row = pl + p * kPlaneWords + r * kPlanePitch;
+      int32_t s[32], d[32];
+      if (w < 3) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) s[j] = row[j];
+      } else {
+        unpack16(raw_lo[k], s);
+      }
+      unpack16(raw_hi[k], s + 16);
+      inv53_lift<32>(s, d);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) row[j] = d[j];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int c = threadIdx.x; c < 6 * 32; c += NT) inv53_line<32>(pl + (c >> 5) * kPlaneWords + (c & 31), kPlanePitch);
+  __syncthreads();
 
   // 6. YCoCg667 -> RGB565 endpoints and whole 8-byte DXT1 blocks (or the
   //    blocks' pixels).
@@ -641,7 +693,7 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
 }
 
 template <bool RGB>
-__global__ void __launch_bounds__(256) gst_tile_kernel(const uint8_t *__restrict__ scratch, uint8_t *__restrict__ out,
+__global__ void __launch_bounds__(256, 8) gst_tile_kernel(const uint8_t *__restrict__ scratch, uint8_t *__restrict__ out,
                                                        GstPlanView plan) {
   __shared__ int32_t pl[6 * kPlaneWords];
   const GstTileItem it = plan.tiles[blockIdx.x];

@@ -561,7 +561,11 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
                                           uint32_t tile, int32_t *pl) {
   constexpr int kWarps = NT / 32;
   constexpr int kRows = 32 / kWarps;            // block rows a warp assembles
-  constexpr int kOwn = (192 + NT - 1) / NT;     // coefficient rows (of the six planes) a thread owns
+  // With at least 192 threads every thread owns at most one coefficient row
+  // and keeps it in registers until level 32; with fewer, the coefficients
+  // all go to shared memory first (two rows per thread would spill).
+  constexpr bool kRegRows = NT >= 192;
+  constexpr int kOwn = kRegRows ? 1 : (384 + NT - 1) / NT;  // rows owned, or 16-byte chunks loaded
   const size_t B = static_cast<size_t>(im.bx) * im.by;
   const uint32_t tx = tile % im.tiles_x, ty = tile / im.tiles_x;
   const uint8_t *sym = scratch + im.sym_off;
@@ -580,12 +584,14 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
   for (int k = 0; k < kOwn; ++k) {
     const int l = t + k * NT;
     raw_lo[k] = raw_hi[k] = make_uint4(0, 0, 0, 0);
-    if (l < 192) {
+    if (kRegRows && l < 192) {
       const int w = l >> 5, ln = l & 31;
       const int p = 2 * (w % 3) + (ln >> 4), r = 16 * (w / 3) + (ln & 15);
       const uint4 *row = reinterpret_cast<const uint4 *>(tile_base + p * B + r * 32);
       raw_lo[k] = ld_sym<COH>(row);
       raw_hi[k] = ld_sym<COH>(row + 1);
+    } else if (!kRegRows && l < 384) {  // chunk l: plane l / 64, row (l % 64) / 2, half l % 2
+      raw_lo[k] = ld_sym<COH>(reinterpret_cast<const uint4 *>(tile_base + (l >> 6) * B) + (l & 63));
     }
   }
 
@@ -608,12 +614,18 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
 #pragma unroll
   for (int k = 0; k < kOwn; ++k) {
     const int l = t + k * NT;
-    if (l < 96) {  // rows < 16
+    int32_t v[16];
+    if (kRegRows && l < 96) {  // rows < 16
       const int w = l >> 5, ln = l & 31;
       const int p = 2 * w + (ln >> 4), r = ln & 15;
-      int32_t v[16];
       unpack16(raw_lo[k], v);
       int32_t *dst = pl + p * kPlaneWords + r * kPlanePitch;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) dst[j] = v[j];
+    } else if (!kRegRows && l < 384) {  // every chunk
+      unpack16(raw_lo[k], v);
+      const int q = l & 63;
+      int32_t *dst = pl + (l >> 6) * kPlaneWords + (q >> 1) * kPlanePitch + (q & 1) * 16;
 #pragma unroll
       for (int j = 0; j < 16; ++j) dst[j] = v[j];
     }
@@ -644,6 +656,9 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
   inv53_level<4, NT>(pl);
   inv53_level<8, NT>(pl);
   inv53_level<16, NT>(pl);
+  if constexpr (!kRegRows) {
+    inv53_level<32, NT>(pl);
+  } else {
 #pragma unroll
   for (int k = 0; k < kOwn; ++k) {
     const int l = t + k * NT;
@@ -668,6 +683,7 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
 #pragma unroll
   for (int c = threadIdx.x; c < 6 * 32; c += NT) inv53_line<32>(pl + (c >> 5) * kPlaneWords + (c & 31), kPlanePitch);
   __syncthreads();
+  }
 
   // 6. YCoCg667 -> RGB565 endpoints and whole 8-byte DXT1 blocks (or the
   //    blocks' pixels).

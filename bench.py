@@ -43,6 +43,16 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "decoded Mpix/s & DXT1 GB/s, batched vs per-image, bit-exact; p50/p99 latency"
+
+# DRAM bytes (read + write) per launch of each kernel on the 64-image batch,
+# from one `ncu --set full --clock-control none` capture of each kernel of the
+# current build (ncu flushes the caches before each replay, so these are
+# cold-cache bytes: the tile kernel's reads are the rANS kernel's symbols,
+# which in an unprofiled launch stay in L2).
+NCU_TRAFFIC_BATCHED = {
+    "gst_rans_kernel": 14.19e6 + 5.66e6,
+    "gst_tile_kernel": 40.27e6 + 3.74e6,
+}
 FLUSH_BYTES = 256 << 20
 
 
@@ -430,7 +440,9 @@ def run_gst(args, rank, world, local):
             "unit": "GB/s",
             "frac": round(batch.alg_bytes / (ms_per_step / 1e3) / 1e9 / peak, 4),
             "peak_source": f"{peak_kind} hbm_gbs",
-            "traffic": None,
+            "traffic": NCU_TRAFFIC_BATCHED.get(dominant),
+            "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of the dominant kernel, one cold-cache "
+                            "ncu capture per launch; null where no capture of that kernel was made",
             "algorithmic_bytes_per_launch": batch.alg_bytes,
             "dominant_kernel": dominant,
             "kernels": {k: {"avg_ms": round(v["avg_ms"], 4), "share": round(v["share"], 3)} for k, v in ksum.items()},

@@ -41,7 +41,7 @@ gst_status check_header(const gst_header &h) {
   const uint64_t B = px / 16;
   if (B >= (1u << 28)) return GST_E_FORMAT;
   if (h.palette_bytes == 0 || h.palette_bytes % kSymsPerGroup) return GST_E_FORMAT;
-  if (7 * B + h.palette_bytes >= (1ull << 32)) return GST_E_FORMAT;
+  if (8 * B + h.palette_bytes >= (1ull << 32)) return GST_E_FORMAT;
   const uint32_t lens[4] = {h.y_cmp_sz, h.chroma_cmp_sz, h.palette_sz, h.indices_sz};
   const uint64_t syms[4] = {2 * B, 4 * B, h.palette_bytes, B};
   for (int i = 0; i < 4; ++i) {
@@ -60,7 +60,7 @@ ScratchLayout scratch_layout(const gst_header &h) {
   const uint64_t B = image_blocks(h);
   ScratchLayout s;
   s.sym = 0;
-  s.chunk = align_up(7 * B + h.palette_bytes, kAlign);
+  s.chunk = align_up(8 * B + h.palette_bytes, kAlign);  // index section: 2 bytes per block
   s.gsum = s.chunk + align_up(B / 32 * 4, kAlign);
   s.total = s.gsum + align_up(2 * (B / kSymsPerGroup) * 4, kAlign);
   return s;

@@ -199,9 +199,13 @@ __device__ __forceinline__ uint32_t mul_hi(uint32_t a, uint32_t b) {
 
 // Decodes one group: ns <= 32 interleaved streams of 256 symbols whose final
 // states sit at [top, hi) and whose renormalisation words fill [lo, top) of
-// the section `sec` (ans_decode.cl:25-74).  Lane l is stream l.  When INDEX,
-// also returns the lane's suffix sums of (symbol - 128) after 32, 64, ..., 256
-// steps in suf[] (the palette-index deltas).
+// the section `sec` (ans_decode.cl:25-74).  Lane l is stream l, its 256
+// symbols go to out[0..255].  When INDEX (the palette-index deltas
+// d = symbol - 128), out instead receives 256 int16: for position k of the
+// stream, the sum of d over the positions after k within k's 32-position
+// chunk (decode order runs backwards, so that is the chunk's running sum when
+// k is decoded); and suf[m] returns the sum of d over the last 32(m + 1)
+// positions.
 //
 // The top stage_words words of [lo, top) are staged in shared memory; every 16
 // steps, if the next 16 steps could read below the staged words, the warp
@@ -237,7 +241,7 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
   uint32_t s2 = 2u * (ptr - sbase16);        // byte offset of word ptr in the stage
   const uint32_t ge = ~lanemask_lt();
   bool bad = false;
-  uint32_t total_sym = 0;
+  int32_t crun = 0, tot = 0;  // INDEX: running sum within the chunk, and over the chunks done
   int32_t s0 = 0, s1 = 0, s2_ = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0;
 #pragma unroll 1
   for (int k = 0; k < 16; ++k) {
@@ -256,6 +260,8 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
       s2 = 0;
     }
     uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+    uint32_t ew[8];  // INDEX: 16 int16 partial sums, slot 15 - j for step j
+    if (INDEX && !(k & 1)) crun = 0;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       const uint32_t qm = mad_hi(x, 1u << 21, 0u - 2048u);                          // q - 2048
@@ -273,17 +279,32 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
       s2 = mad_lo(static_cast<uint32_t>(__popc(m)), 0u - 2u, s2);
       // Steps 16k..16k+15 are positions 255-16k .. 240-16k of this stream
       // (ans_decode.cl:154-155 stores the symbols in reverse).
-      if (j < 4) w3 = __byte_perm(w3, e, 0x2107);
-      else if (j < 8) w2 = __byte_perm(w2, e, 0x2107);
-      else if (j < 12) w1 = __byte_perm(w1, e, 0x2107);
-      else w0 = __byte_perm(w0, e, 0x2107);
-      if (INDEX) total_sym = mad_hi(e, 256u, total_sym);
+      if constexpr (INDEX) {
+        const uint32_t part = static_cast<uint32_t>(crun) & 0xFFFFu;
+        crun += static_cast<int32_t>(e >> 24) - 128;
+        if (j & 1) ew[7 - (j >> 1)] |= part;  // slot 15 - j, even: low half
+        else ew[7 - (j >> 1)] = part << 16;   // odd slot: high half
+      } else {
+        if (j < 4) w3 = __byte_perm(w3, e, 0x2107);
+        else if (j < 8) w2 = __byte_perm(w2, e, 0x2107);
+        else if (j < 12) w1 = __byte_perm(w1, e, 0x2107);
+        else w0 = __byte_perm(w0, e, 0x2107);
+      }
     }
     ptr = static_cast<int>(s2 >> 1) + sbase16;
-    if (active) *reinterpret_cast<uint4 *>(out + 240 - 16 * k) = make_uint4(w0, w1, w2, w3);
+    if constexpr (INDEX) {
+      if (active) {
+        uint4 *o = reinterpret_cast<uint4 *>(out + 2 * (240 - 16 * k));
+        o[0] = make_uint4(ew[0], ew[1], ew[2], ew[3]);
+        o[1] = make_uint4(ew[4], ew[5], ew[6], ew[7]);
+      }
+    } else {
+      if (active) *reinterpret_cast<uint4 *>(out + 240 - 16 * k) = make_uint4(w0, w1, w2, w3);
+    }
     if (INDEX && (k & 1)) {
       const int mm = k >> 1;
-      const int32_t v = static_cast<int32_t>(total_sym) - 4096 * (mm + 1);
+      tot += crun;
+      const int32_t v = tot;
       s0 = mm == 0 ? v : s0;
       s1 = mm == 1 ? v : s1;
       s2_ = mm == 2 ? v : s2_;
@@ -321,8 +342,9 @@ __device__ __forceinline__ void rans_group(const uint8_t *__restrict__ cmp, uint
   const bool group_ok = table_ok && (hi & 3u) == 0 && (lo & 3u) == 0 && hi <= len && lo <= len &&
                         hi >= lo + 4u * ns;
   const bool is_index = section == 3;
-  uint8_t *out = scratch + im.sym_off + im.sec_out[section] + static_cast<size_t>(g) * ns * kSymsPerStream +
-                 static_cast<size_t>(lane) * kSymsPerStream;
+  // Index sections store 2 bytes per position (decode_group<true>).
+  const size_t pos = static_cast<size_t>(g) * ns * kSymsPerStream + static_cast<size_t>(lane) * kSymsPerStream;
+  uint8_t *out = scratch + im.sym_off + im.sec_out[section] + (is_index ? 2 * pos : pos);
 
   int32_t suf[8];
   if (group_ok) {
@@ -336,8 +358,9 @@ __device__ __forceinline__ void rans_group(const uint8_t *__restrict__ cmp, uint
 
   if (!is_index) return;
   // Palette-index prefix sums (codec/decode_indices.cl computes them with a
-  // multi-pass 128-wide scan; here: per 32-block chunk within the group, and
-  // per group below).
+  // multi-pass 128-wide scan; here: the prefix through the end of each
+  // 32-block chunk within the group, and per group below; a block's index is
+  // then group prefix + chunk prefix - its partial sum from decode_group).
   const int32_t T = group_ok ? suf[7] : 0;  // this lane's 256 deltas
   int32_t incl = T;
 #pragma unroll
@@ -349,7 +372,7 @@ __device__ __forceinline__ void rans_group(const uint8_t *__restrict__ cmp, uint
     const int32_t lane_off = incl - T;
     int32_t pre[8];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) pre[c] = lane_off + T - suf[7 - c];
+    for (int c = 0; c < 8; ++c) pre[c] = lane_off + T - (c < 7 ? suf[6 - c] : 0);
     int32_t *chunk = reinterpret_cast<int32_t *>(scratch + im.chunk_off) + static_cast<size_t>(g) * 256 + lane * 8;
     reinterpret_cast<int4 *>(chunk)[0] = make_int4(pre[0], pre[1], pre[2], pre[3]);
     reinterpret_cast<int4 *>(chunk)[1] = make_int4(pre[4], pre[5], pre[6], pre[7]);
@@ -596,15 +619,17 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
   }
 
   // 2. Palette indices of the rows this thread assembles (rows warp + kWarps i,
-  //    column lane): loads first, so that they overlap the wavelet.
+  //    column lane): group prefix + prefix through the block's 32-block chunk
+  //    - the sum of the deltas after the block in its chunk.  Loads first, so
+  //    that they overlap the wavelet.
   const int32_t *chunk_pref = reinterpret_cast<const int32_t *>(scratch + im.chunk_off);
   const int32_t *gpref = reinterpret_cast<const int32_t *>(scratch + im.gsum_off) + im.sec_groups[3];
-  const uint8_t *deltas = sym + im.sec_out[3];
+  const int16_t *partial = reinterpret_cast<const int16_t *>(sym + im.sec_out[3]);
   uint32_t d[kRows], base[kRows];
 #pragma unroll
   for (int i = 0; i < kRows; ++i) {
     const uint32_t p0 = (ty * 32 + warp + kWarps * i) * im.bx + tx * 32;  // first block of the row segment
-    d[i] = static_cast<uint32_t>(ld_sym<COH>(deltas + p0 + lane)) - 128u;
+    d[i] = static_cast<uint32_t>(static_cast<int32_t>(ld_sym<COH>(partial + p0 + lane)));
     base[i] = static_cast<uint32_t>(ld_sym<COH>(gpref + (p0 >> 13))) +
               static_cast<uint32_t>(ld_sym<COH>(chunk_pref + (p0 >> 5)));
   }
@@ -631,18 +656,13 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
     }
   }
 
-  // 4. Finish the index prefix sums (warp scans) and start the palette gathers.
+  // 4. The palette gathers.
   const uint32_t *pal = reinterpret_cast<const uint32_t *>(sym + im.sec_out[2]);
   uint32_t word[kRows];
   bool bad = false;
 #pragma unroll
   for (int i = 0; i < kRows; ++i) {
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, d[i], o);
-      if (lane >= o) d[i] += n;
-    }
-    const uint32_t idx = base[i] + d[i];
+    const uint32_t idx = base[i] - d[i];
     word[i] = 0;
     if (idx < im.palette_words) word[i] = ld_sym<COH>(pal + idx);
     else bad = true;
@@ -889,7 +909,7 @@ namespace gst {
 // loads the library until the process exits.
 //
 // Limits and rules (also stated in include/gst_decoder.h):
-//  * kStaticScratchBytes (4 MiB) bounds the image: 256 + 7*B + palette_bytes
+//  * kStaticScratchBytes (4 MiB) bounds the image: 256 + 8*B + palette_bytes
 //    + B/8 + 8*B/8192 bytes must fit (B = w*h/16); that is at most 2048x2048
 //    with a typical palette.  Larger images are rejected with GST_E_ARG before
 //    anything is enqueued.
@@ -992,7 +1012,7 @@ extern "C" gst_status gst_load_compressed_dxt_static(const gst_header *hdr, cons
   }
   // Scratch inside the static array: symbols, chunk prefixes, group sums.
   auto up = [](uint64_t x) { return (x + 255) / 256 * 256; };
-  const uint64_t sym_bytes = up(7 * B + h.palette_bytes), chunk_bytes = up(B / 32 * 4);
+  const uint64_t sym_bytes = up(8 * B + h.palette_bytes), chunk_bytes = up(B / 32 * 4);
   const uint64_t gsum_bytes = up(2 * (B / kSymsPerGroup) * 4);
   if (kStaticHeaderBytes + sym_bytes + chunk_bytes + gsum_bytes > kStaticScratchBytes) return GST_E_ARG;
 

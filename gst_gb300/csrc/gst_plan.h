@@ -53,7 +53,7 @@ constexpr uint32_t kErrTimeout = 16u;    // a bounded wait of the persistent ker
 struct alignas(16) GstImageDesc {
   uint64_t freq_off;    // bytes from the compressed base to this image's 4 tables
   uint64_t body_off;    // bytes from the compressed base to its first section body
-  uint64_t sym_off;     // scratch: decoded symbols, 7*B + palette_bytes
+  uint64_t sym_off;     // scratch: decoded symbols, 8*B + palette_bytes (index section 2 B/block)
   uint64_t out_off;     // output: DXT1 blocks, 8*B bytes
   uint64_t chunk_off;   // scratch: int32 exclusive prefix per 32-block chunk, B/32
   uint64_t gsum_off;    // scratch: int32 index-group sums, then their exclusive prefix

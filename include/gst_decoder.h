@@ -170,7 +170,7 @@ gst_status gst_batch_set_tuning(gst_batch *batch, int blocks_per_sm, int stage_w
  * allocates).  Input and output are the caller's, as for
  * gst_load_compressed_dxt; the scratch is a 4 MiB array built into the library,
  * held by every GPU that loads the library until the process exits.
- *   - Limit: the image's scratch (256 + 7*B + palette_bytes + B/8 + B/1024
+ *   - Limit: the image's scratch (256 + 8*B + palette_bytes + B/8 + B/1024
  *     bytes, B = width*height/16) must fit in 4 MiB -- about 2048x2048;
  *     larger images return GST_E_ARG and nothing is enqueued.
  *   - All calls share that array and leave their data in it: each call clears

@@ -250,7 +250,8 @@ PlanLayout plan_layout(const gst_header *hdrs, int n) {
   L.off_images = align_up(sizeof(GstPlanHead), 128);
   L.off_rans = L.off_images + sizeof(GstImageDesc) * n;
   L.off_tiles = align_up(L.off_rans + sizeof(GstRansItem) * L.n_rans, 16);
-  L.off_counters = align_up(L.off_tiles + sizeof(GstTileItem) * L.n_tiles, 16);
+  L.off_order = align_up(L.off_tiles + sizeof(GstTileItem) * L.n_tiles, 16);
+  L.off_counters = align_up(L.off_order + 4 * size_t(L.n_rans), 16);
   L.off_image_err = L.off_counters + 4 * size_t(n);
   L.off_sync = align_up(L.off_image_err + 4 * size_t(n), 16);
   L.bytes = align_up(L.off_sync + 16 + 4 * size_t(n), 16);
@@ -312,6 +313,18 @@ void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph,
     scratch_off += L.lay[i].total;
     out_off += uint64_t(out_block_bytes) * B;
   }
+  // The rANS kernel's launch order, longest first: items of sections with more
+  // compressed bytes per group (more renormalisation words, more re-staging)
+  // start first, so that the launch does not end on a few long items.  (The
+  // persistent kernel keeps image order, so that images finish one after
+  // another and their tiles can start early.)
+  uint32_t *order = reinterpret_cast<uint32_t *>(ph + L.off_order);
+  for (uint32_t k = 0; k < ri; ++k) order[k] = k;
+  auto cost = [&](uint32_t k) {
+    const GstImageDesc &d = imgs[rans[k].image];
+    return uint64_t(d.sec_len[rans[k].section]) * 16 / std::max<uint32_t>(1u, d.sec_groups[rans[k].section]);
+  };
+  std::stable_sort(order, order + ri, [&](uint32_t a, uint32_t b) { return cost(a) > cost(b); });
 }
 
 GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) {
@@ -322,6 +335,7 @@ GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) 
   view.tiles = L.n_tiles ? reinterpret_cast<const GstTileItem *>(plan_d + L.off_tiles) : nullptr;
   view.counters = reinterpret_cast<uint32_t *>(plan_d + L.off_counters);
   view.image_err = reinterpret_cast<uint32_t *>(plan_d + L.off_image_err);
+  view.rans_order = reinterpret_cast<const uint32_t *>(plan_d + L.off_order);
   view.sync = reinterpret_cast<uint32_t *>(plan_d + L.off_sync);
   view.n_images = uint32_t(L.n_images);
   view.rgb = 0;

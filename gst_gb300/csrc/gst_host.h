@@ -37,7 +37,7 @@ ScratchLayout scratch_layout(const gst_header &h);
 
 // Where everything of a plan for these headers goes.
 struct PlanLayout {
-  size_t off_images, off_rans, off_tiles, off_counters, off_image_err, off_sync, bytes;
+  size_t off_images, off_rans, off_tiles, off_order, off_counters, off_image_err, off_sync, bytes;
   int n_images;
   uint32_t n_rans, n_tiles;
   size_t scratch_bytes;

@@ -435,7 +435,7 @@ template <int MINB>
 __global__ void __launch_bounds__(128, MINB) gst_rans_kernel(const uint8_t *__restrict__ cmp,
                                                              uint8_t *__restrict__ scratch, GstPlanView plan) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
-  const GstRansItem it = plan.rans[blockIdx.x];
+  const GstRansItem it = plan.rans[plan.rans_order ? plan.rans_order[blockIdx.x] : blockIdx.x];
   rans_item<0>(cmp, scratch, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
                plan.counters + it.image, plan.images[it.image], it.section, it.first_group, it.ngroups, it.streams,
                plan.stage_words, smem_raw, threadIdx.x);

@@ -95,6 +95,7 @@ struct GstPlanView {
   const GstTileItem *tiles;
   uint32_t *counters;   // one per image (index-group completion count)
   uint32_t *image_err;  // one per image (error bits), or null
+  const uint32_t *rans_order;  // the rANS kernel's CTA b takes rans[rans_order[b]] (null: rans[b])
   // Persistent kernel (may be null otherwise): [0] work-queue head, [1] CTAs
   // finished, [4 + i] groups of image i decoded.  Every launch leaves them 0.
   uint32_t *sync;

@@ -515,6 +515,24 @@ __device__ __forceinline__ void inv53_level(int32_t *pl) {
   __syncthreads();
 }
 
+// The same over the first NG threads of the CTA only (threadIdx.x < NG), which
+// synchronise on named barrier BAR.
+template <int L, int NG, int BAR>
+__device__ __forceinline__ void inv53_level_group(int32_t *pl) {
+#pragma unroll
+  for (int t = threadIdx.x; t < 6 * L; t += NG) {
+    const int p = t / L, r = t % L;
+    inv53_line<L>(pl + p * kPlaneWords + r * kPlanePitch, 1);
+  }
+  bar_sync(BAR, NG);
+#pragma unroll
+  for (int t = threadIdx.x; t < 6 * L; t += NG) {
+    const int p = t / L, c = t % L;
+    inv53_line<L>(pl + p * kPlaneWords + c, kPlanePitch);
+  }
+  bar_sync(BAR, NG);
+}
+
 // assemble.cl:39-62: YCoCg667 -> RGB565 on int values of signed chars.
 __device__ __forceinline__ uint32_t ycocg_to_565(int y, int co, int cg) {
   const int t = y - cg / 2;
@@ -634,25 +652,20 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
               static_cast<uint32_t>(ld_sym<COH>(chunk_pref + (p0 >> 5)));
   }
 
-  // 3. The top-left 16x16 of each plane to int32 shared memory (pitch
-  //    kPlanePitch), byte - 128.
+  // 3. (fewer than 192 threads) All coefficients to int32 shared memory
+  //    (pitch kPlanePitch), byte - 128.
+  if constexpr (!kRegRows) {
 #pragma unroll
-  for (int k = 0; k < kOwn; ++k) {
-    const int l = t + k * NT;
-    int32_t v[16];
-    if (kRegRows && l < 96) {  // rows < 16
-      const int w = l >> 5, ln = l & 31;
-      const int p = 2 * w + (ln >> 4), r = ln & 15;
-      unpack16(raw_lo[k], v);
-      int32_t *dst = pl + p * kPlaneWords + r * kPlanePitch;
+    for (int k = 0; k < kOwn; ++k) {
+      const int l = t + k * NT;
+      if (l < 384) {
+        int32_t v[16];
+        unpack16(raw_lo[k], v);
+        const int q = l & 63;
+        int32_t *dst = pl + (l >> 6) * kPlaneWords + (q >> 1) * kPlanePitch + (q & 1) * 16;
 #pragma unroll
-      for (int j = 0; j < 16; ++j) dst[j] = v[j];
-    } else if (!kRegRows && l < 384) {  // every chunk
-      unpack16(raw_lo[k], v);
-      const int q = l & 63;
-      int32_t *dst = pl + (l >> 6) * kPlaneWords + (q >> 1) * kPlanePitch + (q & 1) * 16;
-#pragma unroll
-      for (int j = 0; j < 16; ++j) dst[j] = v[j];
+        for (int j = 0; j < 16; ++j) dst[j] = v[j];
+      }
     }
   }
 
@@ -667,42 +680,53 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
     if (idx < im.palette_words) word[i] = ld_sym<COH>(pal + idx);
     else bad = true;
   }
-  __syncthreads();
 
-  // 5. Five levels of the inverse 5/3 wavelet.  Level 32's row pass takes each
-  //    row from its owner: columns < 16 from shared memory for rows < 16,
-  //    everything else straight from the row's bytes in registers.
-  inv53_level<2, NT>(pl);
-  inv53_level<4, NT>(pl);
-  inv53_level<8, NT>(pl);
-  inv53_level<16, NT>(pl);
+  // 5. Five levels of the inverse 5/3 wavelet.
   if constexpr (!kRegRows) {
+    __syncthreads();
+    inv53_level<2, NT>(pl);
+    inv53_level<4, NT>(pl);
+    inv53_level<8, NT>(pl);
+    inv53_level<16, NT>(pl);
     inv53_level<32, NT>(pl);
   } else {
-#pragma unroll
-  for (int k = 0; k < kOwn; ++k) {
-    const int l = t + k * NT;
-    if (l < 192) {
-      const int w = l >> 5, ln = l & 31;
-      const int p = 2 * (w % 3) + (ln >> 4), r = 16 * (w / 3) + (ln & 15);
+    // Levels 2..16 touch only the top-left 16x16 of each plane, rows 0..15,
+    // whose owners are warps 0-2: they run those levels among themselves
+    // (named barrier 1) and then level 32's row pass of their rows.  Rows
+    // 16..31 (warps 3-5) are untouched coefficients until level 32, so their
+    // owners run level 32's row pass at once, straight from registers, while
+    // the small levels run.  Then level 32's column pass over the CTA.
+    int32_t sv[32], dv[32];
+    if (t < 96) {
+      const int p = 2 * warp + (lane >> 4), r = lane & 15;
       int32_t *row = pl + p * kPlaneWords + r * kPlanePitch;
-      int32_t s[32], d[32];
-      if (w < 3) {
+      unpack16(raw_lo[0], sv);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) s[j] = row[j];
-      } else {
-        unpack16(raw_lo[k], s);
-      }
-      unpack16(raw_hi[k], s + 16);
-      inv53_lift<32>(s, d);
+      for (int j = 0; j < 16; ++j) row[j] = sv[j];
+      bar_sync(1, 96);
+      inv53_level_group<2, 96, 1>(pl);
+      inv53_level_group<4, 96, 1>(pl);
+      inv53_level_group<8, 96, 1>(pl);
+      inv53_level_group<16, 96, 1>(pl);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) row[j] = d[j];
+      for (int j = 0; j < 16; ++j) sv[j] = row[j];
+      unpack16(raw_hi[0], sv + 16);
+      inv53_lift<32>(sv, dv);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) row[j] = dv[j];
+    } else if (t < 192) {
+      const int w = warp - 3, p = 2 * w + (lane >> 4), r = 16 + (lane & 15);
+      int32_t *row = pl + p * kPlaneWords + r * kPlanePitch;
+      unpack16(raw_lo[0], sv);
+      unpack16(raw_hi[0], sv + 16);
+      inv53_lift<32>(sv, dv);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) row[j] = dv[j];
     }
-  }
-  __syncthreads();
+    __syncthreads();
 #pragma unroll
-  for (int c = threadIdx.x; c < 6 * 32; c += NT) inv53_line<32>(pl + (c >> 5) * kPlaneWords + (c & 31), kPlanePitch);
-  __syncthreads();
+    for (int c = threadIdx.x; c < 6 * 32; c += NT) inv53_line<32>(pl + (c >> 5) * kPlaneWords + (c & 31), kPlanePitch);
+    __syncthreads();
   }
 
   // 6. YCoCg667 -> RGB565 endpoints and whole 8-byte DXT1 blocks (or the

@@ -34,8 +34,8 @@ _ref = None
 def build(force: bool = False) -> Path:
     if force or not ORACLE_LIB.exists() or ORACLE_LIB.stat().st_mtime < max(
             ORACLE_SRC.stat().st_mtime, ORACLE_HDR.stat().st_mtime):
-        subprocess.run([os.environ.get("CC", "gcc"), "-std=c11", "-O2", "-shared", "-fPIC", "-pthread",
-                        str(ORACLE_SRC), "-o", str(ORACLE_LIB)], check=True)
+        subprocess.run([os.environ.get("CC", "gcc"), "-std=c11", "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-pthread",
+                        str(ORACLE_SRC), "-o", str(ORACLE_LIB), "-lm"], check=True)
     return ORACLE_LIB
 
 
@@ -64,6 +64,11 @@ def load() -> ctypes.CDLL:
         lib.gsto_decode_rgb.argtypes = [P, S, P, S, I, I]
         lib.gsto_decode_symbols.argtypes = [P, S, P, S, I]
         lib.gsto_section_search.argtypes = [P, U32, U32]
+        lib.gsto_normalize.argtypes = [P, I, I, P]
+        lib.gsto_encode_section.argtypes = [P, S, P, S, ctypes.POINTER(S)]
+        lib.gsto_encode_section_bound.argtypes = [S]
+        lib.gsto_encode_section_bound.restype = S
+        lib.gsto_encode_stream.argtypes = [U32, U32, U32, P, P, P, P, P, S, ctypes.POINTER(S)]
         lib.gsto_section_search.restype = U32
         _lib = lib
     return _lib
@@ -154,3 +159,42 @@ def scan_indices(deltas: np.ndarray, mode: int) -> np.ndarray:
     out = np.zeros(d.size, dtype=np.int32)
     lib.gsto_scan_indices(d.ctypes.data, d.size, out.ctypes.data, mode)
     return out
+
+
+def normalize(counts, M: int = 2048) -> tuple[int, np.ndarray]:
+    """ans::GenerateHistogram restated -> (status, normalized frequencies)."""
+    lib = load()
+    c = np.ascontiguousarray(counts, dtype=np.uint32)
+    out = np.zeros(max(c.size, 1), dtype=np.uint32)
+    st = lib.gsto_normalize(c.ctypes.data, c.size, M, out.ctypes.data)
+    return int(st), out[: c.size]
+
+
+def encode_section(symbols: np.ndarray) -> tuple[int, bytes]:
+    """ByteEncoder::EncodeBytes restated -> (status, section bytes)."""
+    lib = load()
+    x = np.ascontiguousarray(symbols, dtype=np.uint8)
+    cap = int(lib.gsto_encode_section_bound(x.size))
+    out = np.zeros(max(cap, 1), dtype=np.uint8)
+    n = ctypes.c_size_t()
+    st = lib.gsto_encode_section(x.ctypes.data, x.size, out.ctypes.data, cap, ctypes.byref(n))
+    return int(st), out[: n.value].tobytes()
+
+
+def split_symbols(width: int, height: int, palette_bytes: int, symbols: np.ndarray):
+    """The decompressed-symbol buffer (decoder.cpp:441-461 layout) as its four sections."""
+    B = width * height // 16
+    s = np.ascontiguousarray(symbols, dtype=np.uint8)
+    return s[: 2 * B], s[2 * B: 6 * B], s[6 * B: 6 * B + palette_bytes], s[6 * B + palette_bytes: 7 * B + palette_bytes]
+
+
+def encode_stream(width: int, height: int, palette_bytes: int, y, chroma, palette, indices) -> tuple[int, bytes]:
+    """codec/encoder.cpp:122-144 restated: a GST stream from its four symbol sections."""
+    lib = load()
+    secs = [np.ascontiguousarray(a, dtype=np.uint8) for a in (y, chroma, palette, indices)]
+    cap = 28 + sum(int(lib.gsto_encode_section_bound(a.size)) for a in secs)
+    out = np.zeros(cap, dtype=np.uint8)
+    n = ctypes.c_size_t()
+    st = lib.gsto_encode_stream(width, height, palette_bytes, *(a.ctypes.data for a in secs), out.ctypes.data, cap,
+                                ctypes.byref(n))
+    return int(st), out[: n.value].tobytes()

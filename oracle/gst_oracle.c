@@ -9,6 +9,7 @@
  */
 #include "gst_oracle.h"
 
+#include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -613,4 +614,227 @@ uint32_t gsto_section_search(const uint32_t *oo, uint32_t num_offsets, uint32_t 
     x = (high + low) >> 1;
   }
   return x;
+}
+
+/* ========================================================================= */
+/* Encoder stages.                                                           */
+
+/* A candidate of the frequency correction: ans/histogram.cpp:10-19 (Symbol). */
+typedef struct {
+  int symbol;
+  double rank;
+} gsto_ranked;
+
+/* The binary heap of the C++ library with comparator std::greater<Symbol>
+ * (a min-heap on rank), as GCC's libstdc++ implements it (bits/stl_heap.h:
+ * __push_heap, __adjust_heap, __make_heap, __pop_heap -- the SGI STL sift
+ * procedure).  The tie order of ans/histogram.cpp:84-110 depends on it. */
+static void heap_sift_up(gsto_ranked *h, long hole, long top, gsto_ranked v) {
+  long parent = (hole - 1) / 2;
+  while (hole > top && h[parent].rank > v.rank) {
+    h[hole] = h[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  h[hole] = v;
+}
+
+static void heap_adjust(gsto_ranked *h, long hole, long len, gsto_ranked v) {
+  const long top = hole;
+  long child = hole;
+  while (child < (len - 1) / 2) {
+    child = 2 * (child + 1);
+    if (h[child].rank > h[child - 1].rank) child--; /* on equal ranks the right child moves up */
+    h[hole] = h[child];
+    hole = child;
+  }
+  if ((len & 1) == 0 && child == (len - 2) / 2) {
+    child = 2 * (child + 1);
+    h[hole] = h[child - 1];
+    hole = child - 1;
+  }
+  heap_sift_up(h, hole, top, v);
+}
+
+static void heap_make(gsto_ranked *h, long len) {
+  if (len < 2) return;
+  for (long parent = (len - 2) / 2;; --parent) {
+    heap_adjust(h, parent, len, h[parent]);
+    if (parent == 0) return;
+  }
+}
+
+/* Moves the minimum to h[len-1]; the heap keeps len-1 entries. */
+static void heap_pop(gsto_ranked *h, long len) {
+  if (len < 2) return;
+  const gsto_ranked v = h[len - 1];
+  h[len - 1] = h[0];
+  heap_adjust(h, 0, len - 1, v);
+}
+
+/* h[len-1] joins the heap of len-1 entries. */
+static void heap_push(gsto_ranked *h, long len) { heap_sift_up(h, len - 1, 0, h[len - 1]); }
+
+/* ans/histogram.cpp:25-29 (GetFreqChange). */
+static double freq_change(int count, int new_count, int sign) {
+  return log2((double)new_count / (double)(new_count + sign)) * (double)count;
+}
+
+/* ans/histogram.cpp:40-121 */
+int gsto_normalize(const uint32_t *counts, int n, int M, uint32_t *out) {
+  if (M <= 0 || n < 0 || (n > 0 && (!counts || !out))) return GSTO_E_ARG;
+  uint32_t usum = 0; /* fold_sum: std::accumulate in uint32, then int */
+  for (int i = 0; i < n; ++i) usum += counts[i];
+  const int sum = (int)usum;
+  for (int i = 0; i < n; ++i) {
+    if (counts[i] == 0) {
+      out[i] = 0;
+      continue;
+    }
+    const uint32_t scaled = counts[i] * (uint32_t)M; /* uint32 product, wraps as the reference's */
+    const double from_scaled = (double)((float)scaled / (float)sum);
+    const int down = (int)from_scaled;
+    const int v = (from_scaled * from_scaled <= (double)(down * (down + 1))) ? down : down + 1;
+    out[i] = (uint32_t)(v > 1 ? v : 1);
+  }
+  uint32_t hsum = 0;
+  for (int i = 0; i < n; ++i) hsum += out[i];
+  int correction = M - (int)hsum;
+  if (correction == 0) return GSTO_OK;
+  if (correction == M) return GSTO_E_ARG;
+  const int sign = correction > 0 ? 1 : -1;
+  gsto_ranked *h = (gsto_ranked *)malloc(sizeof(gsto_ranked) * (size_t)(n > 0 ? n : 1));
+  if (!h) return GSTO_E_ARG;
+  long len = 0;
+  for (int i = 0; i < n; ++i) {
+    if (counts[i] == 0) continue;
+    if (out[i] > 1 || correction > 0) {
+      h[len].symbol = i;
+      h[len].rank = freq_change((int)counts[i], (int)out[i], sign);
+      ++len;
+    }
+  }
+  heap_make(h, len);
+  int status = GSTO_OK;
+  while (correction != 0) {
+    if (len == 0) {
+      status = GSTO_E_ARG;
+      break;
+    }
+    heap_pop(h, len);
+    const int i = h[--len].symbol;
+    out[i] = (uint32_t)((int)out[i] + sign);
+    correction -= sign;
+    if (out[i] > 1 || sign == 1) {
+      h[len].symbol = i;
+      h[len].rank = freq_change((int)counts[i], (int)out[i], sign);
+      heap_push(h, ++len);
+    }
+  }
+  free(h);
+  return status;
+}
+
+size_t gsto_encode_section_bound(size_t n) {
+  const size_t G = n / GSTO_SYMS_PER_GROUP;
+  /* at most one 16-bit word per symbol (the state drops below 2^15 after
+   * one shift, ans/encode.cpp:62-66), a 2-byte pad and the 32 states */
+  return GSTO_FREQ_BYTES + 4 * G + G * (2 * GSTO_SYMS_PER_GROUP + 2 + 4 * GSTO_STREAMS_PER_GROUP);
+}
+
+/* ans/encode.cpp:224-259 over one group (EncodeInterleaved with 32 encoders of
+ * ans/encode.cpp:39-69), then codec/entropy.cpp:213-229's 4-byte alignment
+ * (two zero bytes in front).  Returns the group's byte count. */
+static size_t encode_group(const uint8_t *sym, const uint32_t F[256], const uint32_t C[256], uint8_t *out,
+                           uint16_t *words) {
+  uint32_t state[GSTO_STREAMS_PER_GROUP];
+  for (int s = 0; s < GSTO_STREAMS_PER_GROUP; ++s) state[s] = GSTO_RANS_L; /* k * M */
+  size_t nw = 0;
+  for (int i = 0; i < GSTO_SYMS_PER_STREAM; ++i) {
+    for (int s = 0; s < GSTO_STREAMS_PER_GROUP; ++s) {
+      const uint32_t x = sym[s * GSTO_SYMS_PER_STREAM + i];
+      uint32_t st = state[s];
+      const uint32_t upper = (1u << 16) * 16u * F[x]; /* b * k * F */
+      while (st >= upper) {
+        words[nw++] = (uint16_t)(st & 0xFFFF);
+        st >>= 16;
+      }
+      state[s] = (st / F[x]) * GSTO_TABLE_SIZE + C[x] + (st % F[x]);
+    }
+  }
+  const size_t pad = (nw & 1) ? 2 : 0;
+  uint8_t *p = out;
+  if (pad) {
+    p[0] = p[1] = 0;
+    p += 2;
+  }
+  for (size_t k = 0; k < nw; ++k, p += 2) wr16(p, words[k]);
+  for (int s = 0; s < GSTO_STREAMS_PER_GROUP; ++s, p += 4) wr32(p, state[s]);
+  return (size_t)(p - out);
+}
+
+/* codec/entropy.cpp:174-265 */
+int gsto_encode_section(const uint8_t *in, size_t n, uint8_t *out, size_t cap, size_t *out_len) {
+  if (!in || !out || !out_len || n == 0 || n % GSTO_SYMS_PER_GROUP) return GSTO_E_ARG;
+  if (n > 0xFFFFFFFFu || cap < gsto_encode_section_bound(n)) return GSTO_E_ARG;
+  uint32_t counts[256] = {0};
+  for (size_t i = 0; i < n; ++i) counts[in[i]]++;
+  int nz = 0;
+  for (int i = 0; i < 256; ++i)
+    if (counts[i]) nz = i + 1;
+  uint32_t F[256] = {0}, C[256] = {0};
+  if (gsto_normalize(counts, nz, GSTO_TABLE_SIZE, F) != GSTO_OK) return GSTO_E_ARG;
+  for (int i = 1; i < 256; ++i) C[i] = C[i - 1] + F[i - 1];
+  const size_t G = n / GSTO_SYMS_PER_GROUP;
+  for (int i = 0; i < 256; ++i) wr16(out + 2 * i, (uint16_t)F[i]);
+  uint8_t *offs = out + GSTO_FREQ_BYTES;
+  uint8_t *p = offs + 4 * G;
+  uint16_t *words = (uint16_t *)malloc(sizeof(uint16_t) * GSTO_SYMS_PER_GROUP);
+  if (!words) return GSTO_E_ARG;
+  uint32_t cum = (uint32_t)(4 * G);
+  for (size_t g = 0; g < G; ++g) {
+    const size_t sz = encode_group(in + g * GSTO_SYMS_PER_GROUP, F, C, p, words);
+    cum += (uint32_t)sz;
+    wr32(offs + 4 * g, cum);
+    p += sz;
+  }
+  free(words);
+  *out_len = (size_t)(p - out); /* already a multiple of 4 (entropy.cpp:261-262) */
+  return GSTO_OK;
+}
+
+/* codec/encoder.cpp:122-144 */
+int gsto_encode_stream(uint32_t w, uint32_t h, uint32_t palette_bytes, const uint8_t *y, const uint8_t *chroma,
+                       const uint8_t *palette, const uint8_t *indices, uint8_t *out, size_t cap, size_t *out_len) {
+  if (!out || !out_len || w == 0 || h == 0 || w % 4 || h % 4) return GSTO_E_ARG;
+  const size_t B = (size_t)(w / 4) * (h / 4);
+  const uint8_t *src[4] = {y, chroma, palette, indices};
+  const size_t nsym[4] = {2 * B, 4 * B, palette_bytes, B};
+  size_t need = GSTO_HEADER_BYTES;
+  for (int k = 0; k < 4; ++k) {
+    if (!src[k] || nsym[k] == 0 || nsym[k] % GSTO_SYMS_PER_GROUP) return GSTO_E_ARG;
+    need += gsto_encode_section_bound(nsym[k]);
+  }
+  if (cap < need) return GSTO_E_ARG;
+  uint8_t *tmp = (uint8_t *)malloc(gsto_encode_section_bound(4 * B > palette_bytes ? 4 * B : palette_bytes));
+  if (!tmp) return GSTO_E_ARG;
+  uint32_t sizes[4];
+  uint8_t *body = out + GSTO_HEADER_BYTES + 4 * GSTO_FREQ_BYTES;
+  for (int k = 0; k < 4; ++k) {
+    size_t len = 0;
+    const int st = gsto_encode_section(src[k], nsym[k], tmp, gsto_encode_section_bound(nsym[k]), &len);
+    if (st != GSTO_OK) {
+      free(tmp);
+      return st;
+    }
+    memcpy(out + GSTO_HEADER_BYTES + k * GSTO_FREQ_BYTES, tmp, GSTO_FREQ_BYTES);
+    memcpy(body, tmp + GSTO_FREQ_BYTES, len - GSTO_FREQ_BYTES);
+    body += len - GSTO_FREQ_BYTES;
+    sizes[k] = (uint32_t)(len - GSTO_FREQ_BYTES);
+  }
+  free(tmp);
+  const uint32_t hdr[7] = {w, h, palette_bytes, sizes[0], sizes[1], sizes[2], sizes[3]};
+  for (int i = 0; i < 7; ++i) wr32(out + 4 * i, hdr[i]);
+  *out_len = (size_t)(body - out);
+  return GSTO_OK;
 }

@@ -8,12 +8,17 @@
  * smoke check and the CPU-baseline leg of bench.py may call it, and only as the
  * checker or the timed CPU baseline; the product never links it.
  *
+ * It also restates the encoder stages that the GPU encoder runs
+ * (ans/histogram.cpp, ans/encode.cpp, codec/entropy.cpp, codec/encoder.cpp).
+ *
  * Parity is pinned (tests/test_oracle.py) against:
  *   - the reference encoder's DXTImage::PhysicalBlocks() on the streams it
  *     wrote (codec/test/codec_test.cpp:36-48), committed as tests/golden/;
  *   - the reference's own ans::DecodeInterleaved and GenTC::InverseWavelet2D,
  *     compiled from the reference sources by oracle/build_ref.sh;
- *   - the known answers of ans/ans_ocl_test.cpp and codec/test/wavelet_test.cpp.
+ *   - the known answers of ans/ans_ocl_test.cpp and codec/test/wavelet_test.cpp;
+ *   - for the encoder stages, the reference's own ans::GenerateHistogram and
+ *     ByteEncoder outputs (tests/golden/golden.json) and its encoder's streams.
  */
 #ifndef GST_ORACLE_H
 #define GST_ORACLE_H
@@ -108,6 +113,36 @@ int gsto_decode_symbols(const uint8_t *gst, size_t n, uint8_t *symbols, size_t c
  * are written back to back in input order. */
 int gsto_decode_batch(const uint8_t *const *gst, const size_t *lens, int n_streams,
                       uint8_t *dxt_out, size_t out_cap, int scan_mode, int nthreads);
+
+/* --- encoder stages (the checker of the GPU encoder) ----------------------- */
+
+/* ans/histogram.cpp:40-121 (ans::GenerateHistogram) for n counts and target sum
+ * M: the float-scaled first guess per symbol, then the heap correction that
+ * moves the sum to M one unit at a time, cheapest rank first.  Equal ranks
+ * resolve in the order of the C++ library's binary heap (std::make_heap /
+ * std::pop_heap / std::push_heap with std::greater), the sift procedure of the
+ * SGI STL that GCC's libstdc++ keeps; it is restated here in C.  Ranks use the
+ * C library's log2, as the reference does.  Returns GSTO_E_ARG for M <= 0 or
+ * all-zero counts (the reference asserts). */
+int gsto_normalize(const uint32_t *counts, int n, int M, uint32_t *out);
+
+/* codec/entropy.cpp:174-265 (ByteEncoder::EncodeBytes) with ans/encode.cpp:56-69
+ * and 224-259 (rANS_Encoder::Encode, ans::EncodeInterleaved) at the OpenCL
+ * settings of ans/ans_ocl_encode.cpp (M = 2^11, k = 2^4, b = 2^16), 32 streams
+ * of 256 symbols per group: the 512-byte frequency table, the u32 group end
+ * offsets, then the groups.  n must be a positive multiple of 8192.  A section
+ * holding only byte 0 (the reference's encoder refuses a one-entry frequency
+ * vector, ans/ans_utils.h:43-47) encodes with F[0] = 2048. */
+int gsto_encode_section(const uint8_t *in, size_t n, uint8_t *out, size_t cap, size_t *out_len);
+
+/* Upper bound of gsto_encode_section's output for n symbols. */
+size_t gsto_encode_section_bound(size_t n);
+
+/* codec/encoder.cpp:122-144: one GST stream from its four symbol sections
+ * (Y planes 2B, chroma planes 4B, palette padded to palette_bytes, index
+ * deltas B; B = w*h/16). */
+int gsto_encode_stream(uint32_t w, uint32_t h, uint32_t palette_bytes, const uint8_t *y, const uint8_t *chroma,
+                       const uint8_t *palette, const uint8_t *indices, uint8_t *out, size_t cap, size_t *out_len);
 
 /* ans_decode.cl:97-143 section lookup (ans_decode_multiple), for tests: returns
  * the section x the work-group at `wg` is assigned to by the kernel's search. */

@@ -16,8 +16,10 @@ Nothing here is needed at test time; the tests read the committed outputs:
   ans/ans_ocl_test.cpp:157-345 (same frequency vectors, stream counts and
   srand(0)/rand() symbol draws), the decode tables of :64-155, the histogram
   known answers of ans/histogram_test.cpp:85-103, the 4x4 inverse wavelet known
-  answer of codec/test/wavelet_test.cpp:129-158, and SHA-256 digests of the
-  reference encoder's DXT1 blocks and of its ByteEncoder sections.
+  answer of codec/test/wavelet_test.cpp:129-158, ans::GenerateHistogram on
+  seeded count vectors (ties, uint32 wrap, large corrections), and SHA-256
+  digests of the reference encoder's DXT1 blocks and of its ByteEncoder
+  sections.
 
 Usage: python tests/golden/make_golden.py
 """
@@ -105,7 +107,7 @@ def main() -> None:
     if not oracle.build_ref():
         raise SystemExit("reference sources not available; cannot regenerate fixtures")
     ref = oracle.load_ref()
-    gold: dict = {"streams": {}, "rans": [], "tables": [], "histograms": [], "sections": []}
+    gold: dict = {"streams": {}, "rans": [], "tables": [], "histograms": [], "histogram_stress": [], "sections": []}
 
     # --- whole streams from the reference encoder -------------------------------
     s, blocks = ref_compress_file(ref, REF_TEST_IMAGE)
@@ -220,9 +222,15 @@ def main() -> None:
                       ([3, 2, 1, 4, 3], 2048), ([12, 14, 17, 1, 1, 2, 372], 2048)):
         gold["histograms"].append({"counts": counts, "M": M, "expected": ref_histogram(ref, counts, M)})
 
-    # --- ByteEncoder sections: digests the project's encoder must reproduce -------
-    for seed, kind, n_groups in ((21, "laplace1", 1), (22, "laplace6", 3), (23, "laplace20", 2),
-                                 (24, "uniform", 2), (25, "two_symbols", 1)):
+    # --- GenerateHistogram on count vectors with ties, uint32 wrap and large
+    #     corrections: pins the heap order of the frequency correction ---------
+    for seed, kind, M in HISTOGRAM_CASES:
+        counts = histogram_input(seed, kind)
+        gold["histogram_stress"].append({"seed": seed, "kind": kind, "M": M,
+                                         "expected": ref_histogram(ref, counts, M)})
+
+    # --- ByteEncoder sections: digests the project's encoders must reproduce ------
+    for seed, kind, n_groups in SECTION_CASES:
         x = section_input(seed, kind, n_groups)
         assert ref.gstref_encode_bytes(x.tobytes(), x.size, buf, cap, ctypes.byref(n)) == 0
         gold["sections"].append({"seed": seed, "kind": kind, "n_groups": n_groups, "bytes": int(n.value),
@@ -237,6 +245,14 @@ def main() -> None:
     print("wrote", sorted(p.name for p in HERE.iterdir()))
 
 
+SECTION_CASES = ((21, "laplace1", 1), (22, "laplace6", 3), (23, "laplace20", 2), (24, "uniform", 2),
+                 (25, "two_symbols", 1), (26, "seven_symbols", 2), (27, "rare_tail", 3), (28, "one_symbol", 1),
+                 (29, "skewed", 2), (30, "wrap255", 1), (31, "rare_group", 4), (32, "laplace6", 70))
+
+HISTOGRAM_KINDS = ("small_values", "spike", "equal", "wrap", "laplace", "large")
+HISTOGRAM_CASES = tuple((100 + i, HISTOGRAM_KINDS[i % 6], 2048 if i % 5 else 4096 - 97 * i) for i in range(36))
+
+
 def section_input(seed: int, kind: str, n_groups: int) -> np.ndarray:
     """Seeded input bytes of one ByteEncoder section (shared with the tests)."""
     rng = np.random.default_rng(seed)
@@ -248,7 +264,49 @@ def section_input(seed: int, kind: str, n_groups: int) -> np.ndarray:
         return rng.integers(0, 256, n).astype(np.uint8)
     if kind == "two_symbols":
         return np.where(rng.random(n) < 0.9, 128, 131).astype(np.uint8)
+    if kind == "seven_symbols":  # equal counts: the frequency correction meets ties
+        return rng.choice(np.array([3, 40, 77, 128, 129, 200, 254], np.uint8), n)
+    if kind == "rare_tail":  # a Laplace body plus 60 symbols that occur once or twice
+        x = (np.rint(rng.laplace(0, 4, n)).astype(np.int64) % 256).astype(np.uint8)
+        pos = rng.choice(n, 90, replace=False)
+        x[pos] = rng.integers(60, 200, 90).astype(np.uint8)
+        return x
+    if kind == "one_symbol":
+        return np.full(n, 77, np.uint8)
+    if kind == "skewed":  # 99.9 % one byte
+        return np.where(rng.random(n) < 0.999, 128, rng.integers(0, 256, n)).astype(np.uint8)
+    if kind == "wrap255":  # symbols 0 and 255 both present (256 table entries)
+        return (np.rint(rng.laplace(0, 2, n)).astype(np.int64) % 256).astype(np.uint8)
+    if kind == "rare_group":  # one group made only of the section's rarest symbols (one word per symbol)
+        x = np.full(n, 128, np.uint8)
+        x[: n // 2] = (np.rint(rng.laplace(0, 1, n // 2)).astype(np.int64) % 256).astype(np.uint8)
+        x[n - 8192:] = rng.integers(0, 256, 8192).astype(np.uint8)
+        return x
     raise ValueError(kind)
+
+
+def histogram_input(seed: int, kind: str) -> np.ndarray:
+    """Seeded count vectors for the GenerateHistogram cases (shared with the tests)."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(2, 257))
+    if kind == "small_values":
+        c = rng.choice([1, 2, 3, 5, 8], size=n)
+    elif kind == "spike":
+        c = rng.integers(0, 4, size=n)
+        c[rng.integers(0, n)] = rng.integers(1, 10**6)
+    elif kind == "equal":
+        c = np.full(n, int(rng.integers(1, 50)))
+    elif kind == "wrap":  # counts * M overflow uint32 in the reference's product
+        c = rng.integers(0, 3, size=n) * int(rng.integers(2_100_000, 3_000_000))
+    elif kind == "laplace":
+        c = np.round(np.exp(-np.abs(np.arange(n) - n / 2) / rng.uniform(1, 30)) * rng.integers(100, 10**7))
+    elif kind == "large":
+        c = rng.integers(0, 5_000_000, size=n)
+    else:
+        raise ValueError(kind)
+    c = np.asarray(c, np.int64)
+    c[-1] = max(c[-1], 1)
+    return c.astype(np.uint32)
 
 
 if __name__ == "__main__":

@@ -130,6 +130,7 @@ struct gst_ctx {
   cudaEvent_t hs_start = nullptr, hs_done = nullptr;
   cudaEvent_t hs_copied[kPlanRing] = {}, hs_decoded[kPlanRing] = {};
   bool hs_used = false;
+  gst::host::EncodeState *enc = nullptr;  // encoder calls (gst_encode_api.cpp)
 };
 
 namespace gst {
@@ -390,6 +391,10 @@ gst_status read_device_status(gst_ctx *ctx, cudaStream_t stream) {
 namespace gst {
 namespace host {
 int ctx_device(const gst_ctx *ctx) { return ctx->device; }
+std::mutex &ctx_mutex(gst_ctx *ctx) { return ctx->mu; }
+EncodeState *&ctx_encode_state(gst_ctx *ctx) { return ctx->enc; }
+uint32_t *ctx_status(gst_ctx *ctx) { return ctx->status_d; }
+uint64_t ctx_wait_limit_ns(gst_ctx *ctx) { return ctx->wait_limit_ns; }
 GstTuning ctx_tuning(gst_ctx *ctx) {
   std::lock_guard<std::mutex> lock(ctx->mu);
   return ctx->tuning;
@@ -479,6 +484,7 @@ void gst_destroy(gst_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
+  gst::host::destroy_encode_state(ctx->enc);
   cudaFree(ctx->scratch);
   cudaFree(ctx->status_d);
   for (auto &pb : ctx->plans) {

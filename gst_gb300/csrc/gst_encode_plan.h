@@ -1,0 +1,77 @@
+// gst_encode_plan.h -- device-visible plan of one GPU encode call (shared by
+// gst_encode.cu and gst_encode_api.cpp).  Internal to the library.
+//
+// An encode call takes S sections of symbols (each a positive multiple of
+// 8192 bytes) grouped into U units.  A unit is either one ByteEncoder section
+// (codec/entropy.cpp:174-265: 512-byte frequency table, u32 group end offsets,
+// groups) or one GST stream of four sections (codec/encoder.cpp:122-144:
+// 28-byte header, the four frequency tables, then the four section bodies).
+// Units are written back to back.  Every group of every section gets a global
+// index in output order; a group's bytes land at
+//     out + section.grp_fixed + (bytes of all groups before it),
+// the last term coming from the encode kernel's decoupled look-back over group
+// sizes, so the whole output is placed in one pass.
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+#include <vector_types.h>
+
+namespace gst {
+
+constexpr uint32_t kHeaderBytes = 28;         // GenTCHeader, codec/codec_base.h:9-20
+constexpr uint32_t kEncMaxWords = 8192;       // 16-bit words per group: at most one per symbol
+constexpr uint32_t kEncHistChunk = 32768;     // symbols per histogram CTA
+constexpr uint32_t kEncLogTableLen = 2050;    // log2(n / (n +- 1)) for n in [0, 2049]
+constexpr uint32_t kEncMaxGroupBytes = 2 * kEncMaxWords + 2 + 4 * 32;
+
+struct EncSection {
+  const uint8_t *sym;   // the section's symbols (16-byte aligned)
+  uint64_t grp_fixed;   // fixed bytes before the section's first group (see above)
+  uint64_t tbl_fixed;   // frequency table at out + tbl_fixed + (group bytes before group tbl_group)
+  uint32_t n_groups;
+  uint32_t first_group;
+  uint32_t tbl_group;
+  uint32_t unit;
+};
+
+struct EncUnit {
+  uint64_t fixed_before;  // fixed bytes of all earlier units
+  uint64_t fixed_bytes;   // this unit's own fixed bytes (header, tables, group offsets)
+  uint32_t first_group, end_group;
+  uint32_t first_section, n_sections;
+  uint32_t width, height, palette_bytes;
+  uint32_t is_stream;  // 1: GST stream of four sections; 0: one ByteEncoder section
+};
+
+struct EncChunk {
+  uint32_t section, start, len;  // len: a multiple of 8192
+};
+
+// Look-back status word of a group: flag in bits 62-63, byte count below.
+constexpr uint64_t kEncFlagAggregate = 1ull << 62;
+constexpr uint64_t kEncFlagInclusive = 2ull << 62;
+constexpr uint64_t kEncValueMask = (1ull << 62) - 1;
+
+struct EncPlanView {
+  const EncSection *sections;
+  const EncUnit *units;
+  const EncChunk *chunks;
+  const uint32_t *group_section;
+  // scratch, zeroed before each call: counts, status, ticket
+  uint32_t *counts;               // [S][256]
+  unsigned long long *status;     // [G]
+  uint32_t *ticket;
+  // scratch written by the kernels
+  uint4 *tables;                  // [S][256] encode entries
+  uint16_t *freqs;                // [S][256] normalised frequencies
+  const double *log2_plus;        // log2(n / (n + 1)), n in [0, 2049]
+  const double *log2_minus;       // log2(n / (n - 1)), n in [0, 2049] (n = 0, 1 unused)
+  uint8_t *out;
+  unsigned long long *offsets;    // [U + 1]: unit starts, then the total
+  uint32_t *err;
+  uint64_t wait_limit_ns;
+  uint32_t n_sections, n_units, n_groups, n_chunks;
+};
+
+}  // namespace gst

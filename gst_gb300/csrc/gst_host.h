@@ -6,12 +6,22 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <vector>
 
 #include "gst_decoder.h"
+#include "gst_encode_plan.h"
 #include "gst_plan.h"
 
 namespace gst {
+
+// gst_encode.cu
+// Enqueues the encoder kernels of one plan (histogram, normalisation, rANS
+// encode, tables); normalize_only runs the normalisation alone on counts
+// already in place.
+cudaError_t launch_encode(const EncPlanView &v, int sm_count, cudaStream_t stream, bool normalize_only,
+                          int *launches);
+size_t encode_rans_smem_bytes();
 
 // gst_kernels.cu
 // Enqueues the kernels of one plan; names (may be null) receives the name of
@@ -51,6 +61,16 @@ GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d);
 
 int ctx_device(const gst_ctx *ctx);
 GstTuning ctx_tuning(gst_ctx *ctx);
+
+// Context state of the encoder calls (gst_encode_api.cpp), created on first use.
+struct EncodeState;
+void destroy_encode_state(EncodeState *s);
+std::mutex &ctx_mutex(gst_ctx *ctx);
+EncodeState *&ctx_encode_state(gst_ctx *ctx);
+uint32_t *ctx_status(gst_ctx *ctx);
+uint64_t ctx_wait_limit_ns(gst_ctx *ctx);
+// Waits for `stream` and turns the device error bits into a status (clears them).
+gst_status read_device_status(gst_ctx *ctx, cudaStream_t stream);
 
 }  // namespace host
 }  // namespace gst

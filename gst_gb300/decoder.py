@@ -49,6 +49,9 @@ EXPORTED_SYMBOLS = (
     "gst_status_string",
     "gst_server_create", "gst_server_destroy", "gst_server_now_ns", "gst_server_submit", "gst_server_poll",
     "gst_server_read", "gst_server_release", "gst_server_read_stats",
+    # include/gst_encode.h
+    "gst_encode_section_bound", "gst_encode_stream_bound", "gst_encode_bytes", "gst_encode_streams",
+    "gst_compress_symbols", "gst_encode_normalize",
 )
 
 
@@ -84,6 +87,13 @@ class ServerStats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class StreamSymbols(ctypes.Structure):
+    """gst_stream_symbols: the four symbol sections of one image (device pointers)."""
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("palette_bytes", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("d_y", ctypes.c_void_p), ("d_chroma", ctypes.c_void_p),
+                ("d_palette", ctypes.c_void_p), ("d_indices", ctypes.c_void_p)]
 
 
 class GenTCHeader(ctypes.Structure):
@@ -169,6 +179,12 @@ def load_library() -> ctypes.CDLL:
         "gst_server_read": (I, [P, ctypes.c_uint64, P, S]),
         "gst_server_release": (I, [P, ctypes.c_uint64]),
         "gst_server_read_stats": (I, [P, ctypes.POINTER(ServerStats), I]),
+        "gst_encode_section_bound": (S, [S]),
+        "gst_encode_stream_bound": (S, [U32, U32, U32]),
+        "gst_encode_bytes": (I, [P, I, ctypes.POINTER(P), ctypes.POINTER(S), P, S, P, P]),
+        "gst_encode_streams": (I, [P, ctypes.POINTER(StreamSymbols), I, P, S, P, P]),
+        "gst_compress_symbols": (I, [P, U32, U32, U32, P, P, S, ctypes.POINTER(S)]),
+        "gst_encode_normalize": (I, [P, P, I, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

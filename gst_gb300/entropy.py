@@ -1,0 +1,80 @@
+"""The GPU encoder stages (include/gst_encode.h) from Python.
+
+Mirrors the reference's entropy-coding interfaces: ``normalize_frequencies``
+is ans::ocl::NormalizeFrequencies (ans/ans_ocl_encode.cpp:6-8),
+``encode_bytes`` is ByteEncoder::EncodeBytes (codec/entropy.cpp:174-265) for
+many sections at once, ``encode_streams`` / ``compress_symbols`` assemble GST
+streams as GenTC::CompressDXTImage does (codec/encoder.cpp:122-144).  Device
+buffers are torch CUDA tensors (or raw pointers); everything runs through the
+CUDA kernels of libgst_gb300.so, with no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Sequence
+
+import numpy as np
+
+from .decoder import GPUContext, StreamSymbols, _check, _ptr, _stream, load_library
+
+SYMS_PER_GROUP = 8192
+
+
+def section_bound(n_symbols: int) -> int:
+    return int(load_library().gst_encode_section_bound(n_symbols))
+
+
+def stream_bound(width: int, height: int, palette_bytes: int) -> int:
+    return int(load_library().gst_encode_stream_bound(width, height, palette_bytes))
+
+
+def normalize_frequencies(ctx: GPUContext, counts) -> np.ndarray:
+    """GenerateHistogram(counts, 2048) on the GPU (blocking)."""
+    c = np.ascontiguousarray(counts, dtype=np.uint32)
+    out = np.zeros(c.size, dtype=np.uint32)
+    _check(load_library().gst_encode_normalize(ctx.handle, c.ctypes.data, c.size, out.ctypes.data),
+           "gst_encode_normalize")
+    return out
+
+
+def encode_bytes(ctx: GPUContext, sections: Sequence, out, offsets, stream=None) -> None:
+    """Enqueues EncodeBytes for every device section (uint8, multiples of 8192)
+    into `out`; `offsets` (int64, len(sections) + 1) receives the section starts
+    and the total."""
+    lib = load_library()
+    n = len(sections)
+    ptrs = (ctypes.c_void_p * n)(*[_ptr(s) for s in sections])
+    sizes = (ctypes.c_size_t * n)(*[int(s.numel()) for s in sections])
+    _check(lib.gst_encode_bytes(ctx.handle, n, ptrs, sizes, _ptr(out), int(out.numel()), _ptr(offsets),
+                                _stream(stream)), "gst_encode_bytes")
+
+
+def stream_symbols(width: int, height: int, palette_bytes: int, symbols) -> StreamSymbols:
+    """The four sections of a device buffer in the decompressed-symbol layout."""
+    B = width * height // 16
+    base = _ptr(symbols)
+    return StreamSymbols(width, height, palette_bytes, 0, base, base + 2 * B, base + 6 * B,
+                         base + 6 * B + palette_bytes)
+
+
+def encode_streams(ctx: GPUContext, images: Sequence[StreamSymbols], out, offsets, stream=None) -> None:
+    """Enqueues one GST stream per image into `out`; `offsets` (int64,
+    len(images) + 1) receives the stream starts and the total."""
+    lib = load_library()
+    arr = (StreamSymbols * len(images))(*images)
+    _check(lib.gst_encode_streams(ctx.handle, arr, len(images), _ptr(out), int(out.numel()), _ptr(offsets),
+                                  _stream(stream)), "gst_encode_streams")
+
+
+def compress_symbols(ctx: GPUContext, width: int, height: int, palette_bytes: int, symbols: np.ndarray) -> bytes:
+    """Host-to-host: one GST stream from a decompressed-symbol buffer (blocking)."""
+    lib = load_library()
+    s = np.ascontiguousarray(symbols, dtype=np.uint8)
+    cap = stream_bound(width, height, palette_bytes)
+    if cap == 0:
+        raise ValueError("dimensions the decoder would reject")
+    out = np.zeros(cap, dtype=np.uint8)
+    n = ctypes.c_size_t()
+    _check(lib.gst_compress_symbols(ctx.handle, width, height, palette_bytes, s.ctypes.data, out.ctypes.data, cap,
+                                    ctypes.byref(n)), "gst_compress_symbols")
+    return out[: n.value].tobytes()

@@ -1,5 +1,5 @@
-"""The C ABI library: it loads, exports every symbol include/gst_decoder.h
-declares, and its host-side logic (stream validation, batch layout, error
+"""The C ABI library: it loads, exports every symbol include/gst_decoder.h and
+include/gst_encode.h declare, and its host-side logic (stream validation, batch layout, error
 reporting without a GPU) behaves as documented.  No kernel runs here."""
 import ctypes
 import re
@@ -13,8 +13,10 @@ from gst_gb300.decoder import GST_E_ARG, GST_E_CUDA, GST_E_FORMAT, GST_OK
 
 
 def header_functions():
-    text = (ROOT / "include" / "gst_decoder.h").read_text()
-    return sorted(set(re.findall(r"^\s*(?:[\w\s\*]+?)\b(gst_\w+)\s*\(", text, re.M)))
+    names = set()
+    for h in sorted((ROOT / "include").glob("*.h")):
+        names |= set(re.findall(r"^\s*(?:[\w\s\*]+?)\b(gst_\w+)\s*\(", h.read_text(), re.M))
+    return sorted(names)
 
 
 def test_library_exports_every_declared_symbol():

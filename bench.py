@@ -64,7 +64,7 @@ def parse_args():
     p.add_argument("--impl", choices=("gst", "reference"), default="gst")
     p.add_argument("--skip-extra", action="store_true", help="headline workload only")
     p.add_argument("--cpu-sample", type=int, default=16, help="images of the batch the CPU baseline decodes")
-    p.add_argument("--only", choices=("batched", "large", "plain", "rans", "serving"),
+    p.add_argument("--only", choices=("batched", "large", "plain", "rans", "serving", "encode"),
                    help="time one workload's decode call only (a small command for profilers)")
     p.add_argument("--rans-blocks-per-sm", type=int, default=0,
                    help="fix the rANS kernel's CTAs of 128 threads per SM (8, 12 or 16) instead of autotuning")
@@ -73,6 +73,8 @@ def parse_args():
     p.add_argument("--serve-seconds", type=float, default=2.0,
                    help="length of each open-loop serving run (the serving config names 60 s)")
     p.add_argument("--serve-rates", default="1000,5000,20000", help="Poisson arrival rates, requests/s")
+    p.add_argument("--encode-hist-match", type=int, default=0, choices=(0, 1),
+                   help="encoder byte counts: merge equal lanes before the atomic (1) or not (0)")
     p.add_argument("--rans-stage-words", type=int, default=1016,
                    help="staging depth with --rans-blocks-per-sm (a multiple of 8 in [520, 2816])")
     return p.parse_args()
@@ -278,6 +280,11 @@ def run_only(args, local):
         out = serving(ctx, args)
         ctx.close()
         return {"only": "serving", **out}
+    if args.only == "encode":
+        ctx.set_option("encode_hist_match", args.encode_hist_match)
+        out = encode_workloads(ctx, stream, flush, device, measured_peak_hbm()[0], args.steps, args.warmup)
+        ctx.close()
+        return {"only": "encode", **out}
     if args.only == "rans":
         sec = workloads.rans_section()
         if args.rans_blocks_per_sm:  # fixed configuration (profiler command lines)
@@ -472,6 +479,8 @@ def run_gst(args, rank, world, local):
         line["serving"] = serving(ctx, args)
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(images[: args.cpu_sample])
+        if not args.skip_extra:
+            line["cpu_baseline"]["encode"] = cpu_baseline_encode(images[: args.cpu_sample])
     rb.close()
     ctx.close()
     return line
@@ -505,6 +514,7 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
             "gst_bytes": b.gst_bytes, "bit_exact": ok, "rans_tuning": tuning,
         }
         rb.close()
+    out.update(encode_workloads(ctx, stream, flush, device, peak, steps, 3))
     sec = workloads.rans_section()
     t, ok, rtuning = time_rans_section(ctx, sec, device, stream, flush, steps, 3)
     alg = len(sec.section) + sec.symbols.size
@@ -516,6 +526,85 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
         "bits_per_symbol": round(8 * (len(sec.section) - 512) / sec.symbols.size, 3), "bit_exact": ok,
         "rans_tuning": rtuning,
     }
+    return out
+
+
+def device_symbols(ctx, stream_bytes: bytes, device):
+    """A stream's decompressed-symbol buffer (Y planes, chroma planes, palette,
+    index deltas; codec/decoder.cpp:441-461) on the device, through the CUDA
+    rANS stage (the encoder workloads' inputs)."""
+    import torch
+    from gst_gb300 import decoder
+    h = decoder.parse_header(stream_bytes)
+    B = h.width * h.height // 16
+    nsyms = (2 * B, 4 * B, h.palette_bytes, B)
+    lens = (h.y_cmp_sz, h.chroma_cmp_sz, h.palette_sz, h.indices_sz)
+    out = torch.empty(7 * B + h.palette_bytes, dtype=torch.uint8, device=device)
+    body, at = 28 + 2048, 0
+    for k in range(4):
+        d_f = torch.from_numpy(np.frombuffer(stream_bytes[28 + 512 * k:28 + 512 * (k + 1)], np.uint8).copy()).to(device)
+        d_b = torch.from_numpy(np.frombuffer(stream_bytes[body:body + lens[k]], np.uint8).copy()).to(device)
+        decoder.decode_rans_groups(ctx, d_f, d_b, lens[k], nsyms[k] // 8192, 32, out[at:at + nsyms[k]])
+        body += lens[k]
+        at += nsyms[k]
+    assert decoder.sync_status(ctx) == decoder.GST_OK
+    return out
+
+
+def encode_workloads(ctx, stream, flush, device, peak, steps, warmup):
+    """The encoder stages (include/gst_encode.h): the symbol sections of the
+    64-image batch and of the 8192x8192 texture encoded back into their GST
+    streams, device-resident, one gst_encode_streams call per step (host plan
+    + four kernels), output checked byte for byte against the streams; then
+    the host-to-host call (gst_compress_symbols) on the 8192x8192 texture."""
+    import torch
+    from gst_gb300 import decoder, entropy, workloads
+    out = {}
+    for name, imgs in (("encode_batched_64", workloads.batched(64)), ("encode_large_8192", [workloads.large()])):
+        syms = [device_symbols(ctx, im.stream, device) for im in imgs]
+        hdrs = [decoder.parse_header(im.stream) for im in imgs]
+        descs = [entropy.stream_symbols(h.width, h.height, h.palette_bytes, s) for h, s in zip(hdrs, syms)]
+        cap = sum(entropy.stream_bound(h.width, h.height, h.palette_bytes) for h in hdrs)
+        d_out = torch.zeros(cap, dtype=torch.uint8, device=device)
+        d_offs = torch.zeros(len(imgs) + 1, dtype=torch.int64, device=device)
+        fn = lambda descs=descs, d_out=d_out, d_offs=d_offs: entropy.encode_streams(ctx, descs, d_out, d_offs, stream)  # noqa: E731
+        t, _ = time_steps(fn, steps, warmup, stream, flush, clear=d_out)
+        ok = decoder.sync_status(ctx, stream) == decoder.GST_OK
+        o = d_offs.cpu().numpy()
+        host = d_out[: int(o[-1])].cpu().numpy().tobytes()
+        ok = ok and all(host[o[i]:o[i + 1]] == im.stream for i, im in enumerate(imgs))
+        ctx.set_profiling(True)
+        _, k = time_steps(fn, 3, 1, stream, flush, ctx)
+        ctx.set_profiling(False)
+        ks = kernel_summary(k)
+        ms = statistics.mean(t)
+        n_sym = sum(int(s.numel()) for s in syms)
+        comp = sum(len(im.stream) for im in imgs)
+        px = sum(im.pixels for im in imgs)
+        rk = ks.get("gst_enc_rans_kernel", {}).get("avg_ms", 0.0)
+        out[name] = {
+            "value": round(n_sym / (ms / 1e3) / 1e9, 3), "unit": "Gsym/s",
+            "mpix_s": round(px / (ms / 1e3) / 1e6, 1), "ms_per_call": round(ms, 4),
+            "p50_ms": round(float(np.percentile(t, 50)), 4), "p99_ms": round(float(np.percentile(t, 99)), 4),
+            "symbols": n_sym, "gst_bytes": comp,
+            "gbs": round((n_sym + comp) / (ms / 1e3) / 1e9, 1),
+            "hbm_frac": round((n_sym + comp) / (ms / 1e3) / 1e9 / peak, 4),
+            "kernels": {kk: round(v["avg_ms"], 4) for kk, v in ks.items()},
+            "rans_kernel_gsym_s": round(n_sym / (rk / 1e3) / 1e9, 3) if rk else None,
+            "byte_exact": bool(ok),
+        }
+        if name == "encode_large_8192":
+            h = hdrs[0]
+            host_sym = syms[0].cpu().numpy()
+            entropy.compress_symbols(ctx, h.width, h.height, h.palette_bytes, host_sym)
+            e2e = []
+            for _ in range(5):
+                t0 = time.perf_counter()
+                s2 = entropy.compress_symbols(ctx, h.width, h.height, h.palette_bytes, host_sym)
+                e2e.append((time.perf_counter() - t0) * 1e3)
+            out[name]["e2e"] = {"ms": round(statistics.median(e2e), 3),
+                                "value": round(n_sym / (statistics.median(e2e) / 1e3) / 1e9, 3), "unit": "Gsym/s",
+                                "h2d_bytes": n_sym, "d2h_bytes": len(s2), "byte_exact": s2 == imgs[0].stream}
     return out
 
 
@@ -606,6 +695,30 @@ def cpu_baseline(images):
     return {"value": round(px / dt / 1e6, 2), "unit": "Mpix/s", "cores": threads, "kind": "port",
             "sample": f"first {len(images)} images of the batched workload ({px / 1e6:.1f} Mpix), oracle decode "
                       f"with {threads} threads, {dt:.2f} s"}
+
+
+def cpu_baseline_encode(images):
+    """The C oracle's encoder stages (restating ByteEncoder::EncodeBytes and the
+    stream assembly) on all host cores, one image per thread, re-encoding the
+    images' symbol sections into their streams."""
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+    threads = os.cpu_count() or 1
+    inputs = []
+    for im in images:
+        w, h, pal = (int.from_bytes(im.stream[i:i + 4], "little") for i in (0, 4, 8))
+        st, sym = oracle.decode_symbols(im.stream, nthreads=threads)
+        assert st == 0
+        inputs.append((w, h, pal, oracle.split_symbols(w, h, pal, sym)))
+    n_sym = sum(7 * (w * h // 16) + pal for w, h, pal, _ in inputs)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        res = list(ex.map(lambda a: oracle.encode_stream(a[0], a[1], a[2], *a[3]), inputs))
+    dt = time.perf_counter() - t0
+    assert all(st == 0 and s == im.stream for (st, s), im in zip(res, images))
+    return {"value": round(n_sym / dt / 1e9, 4), "unit": "Gsym/s", "cores": threads, "kind": "port",
+            "sample": f"symbol sections of the first {len(images)} images of the batched workload "
+                      f"({n_sym / 1e6:.1f} M symbols), oracle encode, {threads} threads, {dt:.2f} s"}
 
 
 def run_reference(args, rank, world):

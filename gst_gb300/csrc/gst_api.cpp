@@ -131,6 +131,7 @@ struct gst_ctx {
   cudaEvent_t hs_copied[kPlanRing] = {}, hs_decoded[kPlanRing] = {};
   bool hs_used = false;
   gst::host::EncodeState *enc = nullptr;  // encoder calls (gst_encode_api.cpp)
+  bool enc_hist_match = false;            // encoder byte counts: merge equal lanes before the atomic
 };
 
 namespace gst {
@@ -395,6 +396,15 @@ std::mutex &ctx_mutex(gst_ctx *ctx) { return ctx->mu; }
 EncodeState *&ctx_encode_state(gst_ctx *ctx) { return ctx->enc; }
 uint32_t *ctx_status(gst_ctx *ctx) { return ctx->status_d; }
 uint64_t ctx_wait_limit_ns(gst_ctx *ctx) { return ctx->wait_limit_ns; }
+cudaEvent_t *ctx_timing_events(gst_ctx *ctx, bool capturing) {
+  return (ctx->profiling && !capturing) ? ctx->ev : nullptr;
+}
+void ctx_set_timed(gst_ctx *ctx, int kernels, int launches) {
+  ctx->timed_kernels = kernels;
+  ctx->last_launches = launches;
+}
+const char **ctx_timed_names(gst_ctx *ctx) { return ctx->timed_names; }
+bool ctx_enc_hist_match(gst_ctx *ctx) { return ctx->enc_hist_match; }
 GstTuning ctx_tuning(gst_ctx *ctx) {
   std::lock_guard<std::mutex> lock(ctx->mu);
   return ctx->tuning;
@@ -999,6 +1009,11 @@ gst_status gst_set_option(gst_ctx *ctx, const char *name, int value) {
   if (strcmp(name, "persistent_wait_us") == 0) {
     if (value < 0 || value > 2000000) return GST_E_ARG;
     ctx->wait_limit_ns = uint64_t(value) * 1000u;
+    return GST_OK;
+  }
+  if (strcmp(name, "encode_hist_match") == 0) {
+    if (value != 0 && value != 1) return GST_E_ARG;
+    ctx->enc_hist_match = value != 0;
     return GST_OK;
   }
   if (strcmp(name, "inject_drop_rans") == 0) {

@@ -267,7 +267,10 @@ gst_status encode_locked(gst_ctx *ctx, EncodeState *st, const std::vector<Sectio
   v.n_units = U;
   v.n_groups = static_cast<uint32_t>(G);
   v.n_chunks = static_cast<uint32_t>(n_chunks);
-  e = launch_encode(v, st->sm_count, stream, false, &st->last_launches);
+  cudaEvent_t *ev = ctx_timing_events(ctx, false);
+  e = launch_encode(v, st->sm_count, stream, false, &st->last_launches, ev, ctx_timed_names(ctx),
+                    ctx_enc_hist_match(ctx));
+  ctx_set_timed(ctx, ev ? st->last_launches : 0, st->last_launches);
   if (e != cudaSuccess) return cuda_status(e);
   cudaEventRecord(st->done, stream);
   st->used = true;

@@ -20,8 +20,8 @@ namespace gst {
 // encode, tables); normalize_only runs the normalisation alone on counts
 // already in place.
 cudaError_t launch_encode(const EncPlanView &v, int sm_count, cudaStream_t stream, bool normalize_only,
-                          int *launches);
-size_t encode_rans_smem_bytes();
+                          int *launches, cudaEvent_t *ev = nullptr, const char **names = nullptr,
+                          bool hist_match = true);
 
 // gst_kernels.cu
 // Enqueues the kernels of one plan; names (may be null) receives the name of
@@ -69,6 +69,12 @@ std::mutex &ctx_mutex(gst_ctx *ctx);
 EncodeState *&ctx_encode_state(gst_ctx *ctx);
 uint32_t *ctx_status(gst_ctx *ctx);
 uint64_t ctx_wait_limit_ns(gst_ctx *ctx);
+// Instrumentation of the context's last call (gst_set_profiling / gst_kernel_times):
+// null when profiling is off or `capturing`.
+cudaEvent_t *ctx_timing_events(gst_ctx *ctx, bool capturing);
+void ctx_set_timed(gst_ctx *ctx, int kernels, int launches);
+const char **ctx_timed_names(gst_ctx *ctx);
+bool ctx_enc_hist_match(gst_ctx *ctx);
 // Waits for `stream` and turns the device error bits into a status (clears them).
 gst_status read_device_status(gst_ctx *ctx, cudaStream_t stream);
 

@@ -237,6 +237,10 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
  *                         gst_decode_rans_groups always uses the rANS kernel.
  *   "persistent_wait_us"  bound of a persistent tile's wait for its image,
  *                         microseconds (0 = 2 s, at most 2,000,000).
+ *   "encode_hist_match"   encoder byte counts (gst_encode.h): 0 (default)
+ *                         issues one shared-memory atomic per byte; 1 merges
+ *                         the lanes of a warp holding the same byte first
+ *                         (a match-any per byte: slower on measured sections).
  *   "inject_drop_rans"    fault injection for tests, 0 (default) or 1: the
  *                         context's persistent launches leave out their rANS
  *                         items, so every tile waits until its bound and the

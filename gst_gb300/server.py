@@ -8,6 +8,7 @@ device until it is released.  This module only submits, polls and releases."""
 from __future__ import annotations
 
 import ctypes
+import gc
 import time
 from dataclasses import dataclass, field
 from typing import Callable, Sequence
@@ -126,7 +127,20 @@ def run_poisson(server: DecodeServer, requests: Sequence[tuple[bytes, np.ndarray
     latency.  Results are released as soon as they are polled, except every
     `verify_every`-th one, which stays on the device until the run is over and
     is then read back and compared with its expected blocks (reading during the
-    run would stall the submitter)."""
+    run would stall the submitter).  Python's cyclic garbage collector is
+    paused for the run (a full collection in a large process stalls the
+    submitter for tens of milliseconds)."""
+    gc_on = gc.isenabled()
+    gc.collect()
+    gc.disable()
+    try:
+        return _run_poisson(server, requests, rate, seconds, seed, verify_every, pick)
+    finally:
+        if gc_on:
+            gc.enable()
+
+
+def _run_poisson(server, requests, rate, seconds, seed, verify_every, pick) -> LoadResult:
     rng = np.random.default_rng(seed)
     n = int(rng.poisson(rate * seconds))
     arrivals = np.sort(rng.uniform(0.0, seconds, n))

@@ -37,6 +37,16 @@ struct EncodeState {
   uint8_t *out_d = nullptr;
   size_t out_cap = 0;
   unsigned long long *offsets_d = nullptr;
+  // endpoint stages (gst_prepare_symbols, gst_compress_dxt)
+  uint8_t *prep_h = nullptr;  // pinned plan staging
+  size_t prep_h_cap = 0;
+  uint8_t *prep_d = nullptr;
+  size_t prep_d_cap = 0;
+  cudaEvent_t prep_done = nullptr;
+  bool prep_used = false;
+  uint8_t *blocks_d = nullptr;
+  size_t blocks_cap = 0;
+  uint32_t *pal_bytes_d = nullptr;
 };
 
 void destroy_encode_state(EncodeState *s) {
@@ -48,6 +58,11 @@ void destroy_encode_state(EncodeState *s) {
   cudaFree(s->in_d);
   cudaFree(s->out_d);
   cudaFree(s->offsets_d);
+  cudaFreeHost(s->prep_h);
+  cudaFree(s->prep_d);
+  cudaFree(s->blocks_d);
+  cudaFree(s->pal_bytes_d);
+  if (s->prep_done) cudaEventDestroy(s->prep_done);
   if (s->done) cudaEventDestroy(s->done);
   if (s->own) cudaStreamDestroy(s->own);
   delete s;
@@ -75,6 +90,8 @@ gst_status get_state(gst_ctx *ctx, EncodeState **out) {
     fill_log2_tables(&t);
     cudaError_t e = cudaDeviceGetAttribute(&n->sm_count, cudaDevAttrMultiProcessorCount, n->device);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&n->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&n->prep_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(&n->pal_bytes_d), sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&n->own, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(&n->log2_d), t.size() * sizeof(double));
     if (e == cudaSuccess) e = cudaMemcpy(n->log2_d, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice);
@@ -278,6 +295,70 @@ gst_status encode_locked(gst_ctx *ctx, EncodeState *st, const std::vector<Sectio
   return GST_OK;
 }
 
+uint64_t palette_capacity(uint32_t w, uint32_t h) {
+  const uint64_t B = uint64_t(w / 4) * (h / 4);
+  return (4 * B + kSymsPerGroup - 1) / kSymsPerGroup * kSymsPerGroup;
+}
+
+struct PrepIn {
+  uint32_t width, height;
+  const uint8_t *blocks;
+  uint8_t *y, *chroma, *palette, *indices;
+};
+
+// Builds and launches the endpoint stages of one call; zeroes the palettes.
+gst_status prepare_locked(EncodeState *st, const std::vector<PrepIn> &imgs, uint32_t *d_palette_bytes,
+                          cudaStream_t stream) {
+  const uint32_t n = static_cast<uint32_t>(imgs.size());
+  uint64_t tiles = 0, chunks = 0;
+  for (const auto &im : imgs) {
+    if (!stream_dims_ok(im.width, im.height, kSymsPerGroup)) return GST_E_ARG;
+    if (!im.blocks || !im.y || !im.chroma || !im.palette || !im.indices) return GST_E_ARG;
+    if (reinterpret_cast<uintptr_t>(im.blocks) % 8) return GST_E_ARG;
+    for (const uint8_t *q : {im.y, im.chroma, im.palette, im.indices})
+      if (reinterpret_cast<uintptr_t>(q) % 16) return GST_E_ARG;
+    const uint64_t B = uint64_t(im.width / 4) * (im.height / 4);
+    tiles += B / 1024;
+    chunks += (B + 8191) / 8192;
+  }
+  if (!d_palette_bytes || reinterpret_cast<uintptr_t>(d_palette_bytes) % 4 || tiles >= (1u << 31)) return GST_E_ARG;
+  const size_t off_chunks = align_up(n * sizeof(EncPrepImage), 16);
+  const size_t off_counts = align_up(off_chunks + chunks * sizeof(EncPrepChunk), 16);
+  const size_t bytes = align_up(off_counts + chunks * sizeof(uint32_t), 16);
+  if (st->prep_used) {
+    const cudaError_t e = cudaEventSynchronize(st->prep_done);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  gst_status r = grow_host(&st->prep_h, &st->prep_h_cap, bytes);
+  if (r == GST_OK) r = grow_dev(&st->prep_d, &st->prep_d_cap, bytes);
+  if (r != GST_OK) return r;
+  memset(st->prep_h, 0, bytes);
+  EncPrepImage *pi = reinterpret_cast<EncPrepImage *>(st->prep_h);
+  EncPrepChunk *pc = reinterpret_cast<EncPrepChunk *>(st->prep_h + off_chunks);
+  uint32_t t = 0, c = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const PrepIn &im = imgs[i];
+    const uint32_t B = (im.width / 4) * (im.height / 4);
+    pi[i] = {reinterpret_cast<const uint64_t *>(im.blocks), im.y, im.chroma, im.palette, im.indices,
+             im.width, im.height, t, 0};
+    t += B / 1024;
+    const uint32_t first = c, count = (B + 8191) / 8192;
+    for (uint32_t k = 0; k < count; ++k, ++c)
+      pc[c] = {i, k * 8192u, std::min<uint32_t>(8192u, B - k * 8192u), first, first + count - 1};
+  }
+  cudaError_t e = cudaMemcpyAsync(st->prep_d, st->prep_h, bytes, cudaMemcpyHostToDevice, stream);
+  for (const auto &im : imgs)
+    if (e == cudaSuccess) e = cudaMemsetAsync(im.palette, 0, palette_capacity(im.width, im.height), stream);
+  if (e == cudaSuccess)
+    e = launch_prepare(reinterpret_cast<const EncPrepImage *>(st->prep_d), n, t,
+                       reinterpret_cast<const EncPrepChunk *>(st->prep_d + off_chunks), c,
+                       reinterpret_cast<uint32_t *>(st->prep_d + off_counts), d_palette_bytes, stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  cudaEventRecord(st->prep_done, stream);
+  st->prep_used = true;
+  return GST_OK;
+}
+
 }  // namespace
 }  // namespace host
 }  // namespace gst
@@ -367,6 +448,77 @@ gst_status gst_compress_symbols(gst_ctx *ctx, uint32_t width, uint32_t height, u
   std::vector<SectionIn> secs = {{d, 2 * B}, {d + 2 * B, 4 * B}, {d + 6 * B, palette_bytes},
                                  {d + 6 * B + palette_bytes, B}};
   std::vector<UnitIn> units = {{true, width, height, palette_bytes, 0, 4}};
+  r = encode_locked(ctx, st, secs, units, st->out_d, st->out_cap, st->offsets_d, st->own);
+  if (r != GST_OK) return r;
+  r = read_device_status(ctx, st->own);
+  if (r != GST_OK) return r;
+  unsigned long long off[2] = {0, 0};
+  e = cudaMemcpy(off, st->offsets_d, sizeof(off), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e);
+  const size_t len = static_cast<size_t>(off[1] - off[0]);
+  if (len > out_cap) return GST_E_ARG;
+  e = cudaMemcpy(gst_out, st->out_d + off[0], len, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e);
+  *out_len = len;
+  return GST_OK;
+}
+
+size_t gst_palette_capacity(uint32_t width, uint32_t height) {
+  if (!stream_dims_ok(width, height, kSymsPerGroup)) return 0;
+  return static_cast<size_t>(palette_capacity(width, height));
+}
+
+gst_status gst_prepare_symbols(gst_ctx *ctx, const gst_symbol_buffers *imgs, int n, uint32_t *d_palette_bytes,
+                               void *stream) {
+  if (!ctx || !imgs || n <= 0) return GST_E_ARG;
+  std::vector<PrepIn> in(n);
+  for (int i = 0; i < n; ++i)
+    in[i] = {imgs[i].width, imgs[i].height, static_cast<const uint8_t *>(imgs[i].d_blocks),
+             static_cast<uint8_t *>(imgs[i].d_y), static_cast<uint8_t *>(imgs[i].d_chroma),
+             static_cast<uint8_t *>(imgs[i].d_palette), static_cast<uint8_t *>(imgs[i].d_indices)};
+  std::lock_guard<std::mutex> lock(ctx_mutex(ctx));
+  cudaSetDevice(ctx_device(ctx));
+  EncodeState *st = nullptr;
+  const gst_status r = get_state(ctx, &st);
+  if (r != GST_OK) return r;
+  return prepare_locked(st, in, d_palette_bytes, static_cast<cudaStream_t>(stream));
+}
+
+gst_status gst_compress_dxt(gst_ctx *ctx, uint32_t width, uint32_t height, const uint64_t *blocks, uint8_t *gst_out,
+                            size_t out_cap, size_t *out_len) {
+  if (!ctx || !blocks || !gst_out || !out_len) return GST_E_ARG;
+  if (!stream_dims_ok(width, height, kSymsPerGroup)) return GST_E_ARG;
+  const uint64_t B = uint64_t(width / 4) * (height / 4);
+  const uint64_t pal_cap = palette_capacity(width, height);
+  std::lock_guard<std::mutex> lock(ctx_mutex(ctx));
+  cudaSetDevice(ctx_device(ctx));
+  EncodeState *st = nullptr;
+  gst_status r = get_state(ctx, &st);
+  if (r != GST_OK) return r;
+  for (cudaEvent_t ev : {st->done, st->prep_done}) {
+    const cudaError_t e = cudaEventSynchronize(ev);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  // device symbol buffer: Y 2B | chroma 4B | indices B | palette (capacity)
+  const size_t sym_bytes = static_cast<size_t>(7 * B + pal_cap);
+  const size_t bound = gst_encode_stream_bound(width, height, static_cast<uint32_t>(std::min<uint64_t>(pal_cap, 0xFFFFE000u)));
+  r = grow_dev(&st->blocks_d, &st->blocks_cap, static_cast<size_t>(8 * B));
+  if (r == GST_OK) r = grow_dev(&st->in_d, &st->in_cap, sym_bytes);
+  if (r == GST_OK) r = grow_dev(&st->out_d, &st->out_cap, bound);
+  if (r != GST_OK) return r;
+  cudaError_t e = cudaMemcpyAsync(st->blocks_d, blocks, static_cast<size_t>(8 * B), cudaMemcpyHostToDevice, st->own);
+  if (e != cudaSuccess) return cuda_status(e);
+  uint8_t *d = st->in_d;
+  const std::vector<PrepIn> in = {{width, height, st->blocks_d, d, d + 2 * B, d + 7 * B, d + 6 * B}};
+  r = prepare_locked(st, in, st->pal_bytes_d, st->own);
+  if (r != GST_OK) return r;
+  uint32_t pal_bytes = 0;
+  e = cudaMemcpyAsync(&pal_bytes, st->pal_bytes_d, sizeof(pal_bytes), cudaMemcpyDeviceToHost, st->own);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st->own);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (pal_bytes == 0 || pal_bytes > pal_cap) return GST_E_CUDA;
+  std::vector<SectionIn> secs = {{d, 2 * B}, {d + 2 * B, 4 * B}, {d + 7 * B, pal_bytes}, {d + 6 * B, B}};
+  std::vector<UnitIn> units = {{true, width, height, pal_bytes, 0, 4}};
   r = encode_locked(ctx, st, secs, units, st->out_d, st->out_cap, st->offsets_d, st->own);
   if (r != GST_OK) return r;
   r = read_device_status(ctx, st->own);

@@ -48,6 +48,21 @@ struct EncChunk {
   uint32_t section, start, len;  // len: a multiple of 8192
 };
 
+// Endpoint stages (gst_prepare.cu): one image's DXT1 blocks in, its four
+// symbol sections out.
+struct EncPrepImage {
+  const uint64_t *blocks;  // width * height / 16 blocks, raster order
+  uint8_t *y, *chroma, *palette, *indices;
+  uint32_t width, height;
+  uint32_t first_tile;  // tiles of earlier images
+  uint32_t pad;
+};
+
+struct EncPrepChunk {  // 8192 blocks (or the image's rest) in raster order
+  uint32_t image, start, len;
+  uint32_t first_chunk, last_chunk;  // the image's chunks
+};
+
 // Look-back status word of a group: flag in bits 62-63, byte count below.
 constexpr uint64_t kEncFlagAggregate = 1ull << 62;
 constexpr uint64_t kEncFlagInclusive = 2ull << 62;

@@ -23,6 +23,13 @@ cudaError_t launch_encode(const EncPlanView &v, int sm_count, cudaStream_t strea
                           int *launches, cudaEvent_t *ev = nullptr, const char **names = nullptr,
                           bool hist_match = true);
 
+// gst_prepare.cu
+// Enqueues the endpoint stages (forward wavelet planes, run palette) of the
+// images of a plan; their palettes must be zeroed beforehand.
+cudaError_t launch_prepare(const EncPrepImage *d_images, uint32_t n_images, uint32_t n_tiles,
+                           const EncPrepChunk *d_chunks, uint32_t n_chunks, uint32_t *d_counts,
+                           uint32_t *d_palette_bytes, cudaStream_t stream);
+
 // gst_kernels.cu
 // Enqueues the kernels of one plan; names (may be null) receives the name of
 // each kernel launched, in order.

@@ -51,7 +51,8 @@ EXPORTED_SYMBOLS = (
     "gst_server_read", "gst_server_release", "gst_server_read_stats",
     # include/gst_encode.h
     "gst_encode_section_bound", "gst_encode_stream_bound", "gst_encode_bytes", "gst_encode_streams",
-    "gst_compress_symbols", "gst_encode_normalize",
+    "gst_compress_symbols", "gst_encode_normalize", "gst_palette_capacity", "gst_prepare_symbols",
+    "gst_compress_dxt",
 )
 
 
@@ -94,6 +95,13 @@ class StreamSymbols(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("palette_bytes", ctypes.c_uint32),
                 ("reserved", ctypes.c_uint32), ("d_y", ctypes.c_void_p), ("d_chroma", ctypes.c_void_p),
                 ("d_palette", ctypes.c_void_p), ("d_indices", ctypes.c_void_p)]
+
+
+class SymbolBuffers(ctypes.Structure):
+    """gst_symbol_buffers: one image's DXT1 blocks in, its four sections out (device pointers)."""
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("d_blocks", ctypes.c_void_p),
+                ("d_y", ctypes.c_void_p), ("d_chroma", ctypes.c_void_p), ("d_palette", ctypes.c_void_p),
+                ("d_indices", ctypes.c_void_p)]
 
 
 class GenTCHeader(ctypes.Structure):
@@ -185,6 +193,9 @@ def load_library() -> ctypes.CDLL:
         "gst_encode_streams": (I, [P, ctypes.POINTER(StreamSymbols), I, P, S, P, P]),
         "gst_compress_symbols": (I, [P, U32, U32, U32, P, P, S, ctypes.POINTER(S)]),
         "gst_encode_normalize": (I, [P, P, I, P]),
+        "gst_palette_capacity": (S, [U32, U32]),
+        "gst_prepare_symbols": (I, [P, ctypes.POINTER(SymbolBuffers), I, P, P]),
+        "gst_compress_dxt": (I, [P, U32, U32, P, P, S, ctypes.POINTER(S)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

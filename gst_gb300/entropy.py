@@ -4,7 +4,9 @@ Mirrors the reference's entropy-coding interfaces: ``normalize_frequencies``
 is ans::ocl::NormalizeFrequencies (ans/ans_ocl_encode.cpp:6-8),
 ``encode_bytes`` is ByteEncoder::EncodeBytes (codec/entropy.cpp:174-265) for
 many sections at once, ``encode_streams`` / ``compress_symbols`` assemble GST
-streams as GenTC::CompressDXTImage does (codec/encoder.cpp:122-144).  Device
+streams as GenTC::CompressDXTImage does (codec/encoder.cpp:122-144);
+``prepare_symbols`` / ``compress_dxt`` run its endpoint stages (YCoCg planes,
+forward wavelet, an index palette) from DXT1 blocks.  Device
 buffers are torch CUDA tensors (or raw pointers); everything runs through the
 CUDA kernels of libgst_gb300.so, with no CPU path.
 """
@@ -15,7 +17,7 @@ from typing import Sequence
 
 import numpy as np
 
-from .decoder import GPUContext, StreamSymbols, _check, _ptr, _stream, load_library
+from .decoder import GPUContext, StreamSymbols, SymbolBuffers, _check, _ptr, _stream, load_library
 
 SYMS_PER_GROUP = 8192
 
@@ -77,4 +79,33 @@ def compress_symbols(ctx: GPUContext, width: int, height: int, palette_bytes: in
     n = ctypes.c_size_t()
     _check(lib.gst_compress_symbols(ctx.handle, width, height, palette_bytes, s.ctypes.data, out.ctypes.data, cap,
                                     ctypes.byref(n)), "gst_compress_symbols")
+    return out[: n.value].tobytes()
+
+
+def palette_capacity(width: int, height: int) -> int:
+    return int(load_library().gst_palette_capacity(width, height))
+
+
+def prepare_symbols(ctx: GPUContext, images: Sequence[tuple], d_palette_bytes, stream=None) -> None:
+    """Enqueues the endpoint stages; images: (width, height, d_blocks, d_y,
+    d_chroma, d_palette, d_indices) with device buffers (uint8 / uint64
+    tensors or pointers); d_palette_bytes: uint32/int32 device array, one per
+    image."""
+    lib = load_library()
+    arr = (SymbolBuffers * len(images))(*[SymbolBuffers(w, h, *(_ptr(b) for b in bufs)) for w, h, *bufs in images])
+    _check(lib.gst_prepare_symbols(ctx.handle, arr, len(images), _ptr(d_palette_bytes), _stream(stream)),
+           "gst_prepare_symbols")
+
+
+def compress_dxt(ctx: GPUContext, width: int, height: int, blocks: np.ndarray) -> bytes:
+    """Host-to-host: DXT1 blocks (uint64, raster order) -> GST stream (blocking)."""
+    lib = load_library()
+    b = np.ascontiguousarray(blocks, dtype=np.uint64)
+    cap = stream_bound(width, height, palette_capacity(width, height))
+    if cap == 0:
+        raise ValueError("dimensions the decoder would reject")
+    out = np.zeros(cap, dtype=np.uint8)
+    n = ctypes.c_size_t()
+    _check(lib.gst_compress_dxt(ctx.handle, width, height, b.ctypes.data, out.ctypes.data, cap, ctypes.byref(n)),
+           "gst_compress_dxt")
     return out[: n.value].tobytes()

@@ -83,6 +83,53 @@ gst_status gst_encode_streams(gst_ctx *ctx, const gst_stream_symbols *imgs, int 
 gst_status gst_compress_symbols(gst_ctx *ctx, uint32_t width, uint32_t height, uint32_t palette_bytes,
                                 const uint8_t *symbols, uint8_t *gst_out, size_t out_cap, size_t *out_len);
 
+/* --- endpoint stages: DXT1 blocks -> symbol sections ----------------------
+ *
+ *   reference                                       this header
+ *   ----------------------------------------------  -------------------------
+ *   RunDXTEndpointPipeline + RGB565toYCoCg667 +     gst_prepare_symbols
+ *     ImageSplit (codec/encoder.cpp:20-98;
+ *     FWavelet2D, codec/image_processing.h:267-333)
+ *   DXTImage::Reencode's index palette              gst_prepare_symbols (a
+ *     (codec/dxt_image.cpp:510-624)                 different, parallel rule)
+ *   GenTC::CompressDXTImage                         gst_compress_dxt
+ *     (codec/encoder.cpp:39-180)
+ *
+ * The Y and chroma sections are the reference's, byte for byte.  The index
+ * palette is not the reference's least-squares search (sequential over the
+ * blocks, in floating point): a block whose 32-bit index word equals the
+ * previous block's (raster order) reuses its entry, any other block appends
+ * its word.  Blocks keep their endpoints and words, so the stream decodes to
+ * the given blocks wherever their wavelet coefficients fit in 8 bits (they
+ * wrap as in the reference otherwise). */
+
+/* One image: w*h/16 DXT1 blocks in (8-byte aligned device memory, raster
+ * order, {u16 ep1, u16 ep2, u32 indices}), its sections out (16-byte aligned
+ * device memory). */
+typedef struct gst_symbol_buffers {
+  uint32_t width, height;
+  const void *d_blocks;
+  void *d_y;       /* 2B bytes                                    */
+  void *d_chroma;  /* 4B bytes                                    */
+  void *d_palette; /* gst_palette_capacity(width, height) bytes   */
+  void *d_indices; /* B bytes                                     */
+} gst_symbol_buffers;
+
+/* 4B bytes rounded up to 8192: room for a palette of one word per block. */
+size_t gst_palette_capacity(uint32_t width, uint32_t height);
+
+/* The endpoint stages for n images; d_palette_bytes[i] (device u32) receives
+ * image i's palette bytes (padded to a multiple of 8192), the palette_bytes of
+ * its gst_stream_symbols. */
+gst_status gst_prepare_symbols(gst_ctx *ctx, const gst_symbol_buffers *imgs, int n, uint32_t *d_palette_bytes,
+                               void *stream);
+
+/* Blocking host-to-host form for one image: DXT1 blocks -> GST stream
+ * (out_cap at least gst_encode_stream_bound(width, height,
+ * gst_palette_capacity(width, height))). */
+gst_status gst_compress_dxt(gst_ctx *ctx, uint32_t width, uint32_t height, const uint64_t *blocks, uint8_t *gst_out,
+                            size_t out_cap, size_t *out_len);
+
 /* ans::ocl::NormalizeFrequencies on the GPU (blocking, host arrays): n <= 256
  * byte counts -> n frequencies summing to 2048.  GST_E_ARG when every count is
  * zero (the reference asserts). */

@@ -69,6 +69,10 @@ def load() -> ctypes.CDLL:
         lib.gsto_encode_section_bound.argtypes = [S]
         lib.gsto_encode_section_bound.restype = S
         lib.gsto_encode_stream.argtypes = [U32, U32, U32, P, P, P, P, P, S, ctypes.POINTER(S)]
+        lib.gsto_endpoint_planes.argtypes = [U32, U32, P, P, P]
+        lib.gsto_endpoint_planes.restype = ctypes.c_uint64
+        lib.gsto_run_palette.argtypes = [U32, U32, P, P, S, P]
+        lib.gsto_run_palette.restype = U32
         lib.gsto_section_search.restype = U32
         _lib = lib
     return _lib
@@ -198,3 +202,26 @@ def encode_stream(width: int, height: int, palette_bytes: int, y, chroma, palett
     st = lib.gsto_encode_stream(width, height, palette_bytes, *(a.ctypes.data for a in secs), out.ctypes.data, cap,
                                 ctypes.byref(n))
     return int(st), out[: n.value].tobytes()
+
+
+def endpoint_planes(width: int, height: int, blocks: np.ndarray) -> tuple[np.ndarray, np.ndarray, int]:
+    """The encoder's endpoint stages restated -> (Y section, chroma section, clipped coefficients)."""
+    lib = load()
+    blk = np.ascontiguousarray(blocks, dtype=np.uint64)
+    B = width * height // 16
+    y = np.zeros(2 * B, np.uint8)
+    c = np.zeros(4 * B, np.uint8)
+    clips = lib.gsto_endpoint_planes(width, height, blk.ctypes.data, y.ctypes.data, c.ctypes.data)
+    return y, c, int(clips)
+
+
+def run_palette(width: int, height: int, blocks: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """The GPU pipeline's run palette restated -> (padded palette bytes, index deltas)."""
+    lib = load()
+    blk = np.ascontiguousarray(blocks, dtype=np.uint64)
+    B = width * height // 16
+    cap = (4 * B + 8191) // 8192 * 8192
+    pal = np.zeros(cap, np.uint8)
+    d = np.zeros(B, np.uint8)
+    n = lib.gsto_run_palette(width, height, blk.ctypes.data, pal.ctypes.data, cap, d.ctypes.data)
+    return pal[:n], d

@@ -838,3 +838,88 @@ int gsto_encode_stream(uint32_t w, uint32_t h, uint32_t palette_bytes, const uin
   *out_len = (size_t)(body - out);
   return GSTO_OK;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Endpoint stages of the encoder.                                           */
+
+/* codec/image_processing.cpp:10-27 */
+static void rgb565_to_ycocg667(uint16_t c, int *y, int *co, int *cg) {
+  const int r = c >> 11, g = (c >> 5) & 63, b = c & 31;
+  *co = r - b;
+  const int t = r + b + (b >> 4);
+  *cg = g - t;
+  *y = t + (*cg / 2);
+}
+
+/* codec/wavelet.cpp:56-88 (ForwardWavelet1D), int16 storage */
+static void forward_line(const int16_t *src, int16_t *dst, int len) {
+  const int mid = len - len / 2;
+  for (int i = 1; i < len; i += 2) {
+    const int prev = normalize_index(i - 1, len), next = normalize_index(i + 1, len);
+    dst[mid + i / 2] = (int16_t)(src[i] - (src[prev] + src[next]) / 2);
+  }
+  for (int i = 0; i < len; i += 2) {
+    const int prev = mid + normalize_index(i - 1, len) / 2, next = mid + normalize_index(i + 1, len) / 2;
+    dst[i / 2] = (int16_t)(src[i] + (dst[prev] + dst[next] + 2) / 4);
+  }
+}
+
+/* codec/wavelet.cpp:123-157 (ForwardWavelet2D) on the top-left dim x dim of a
+ * 32x32 tile: every column, then every row. */
+static void forward_level(int16_t *blk, int dim) {
+  int16_t line[32], out[32];
+  for (int x = 0; x < dim; ++x) {
+    for (int y = 0; y < dim; ++y) line[y] = blk[y * 32 + x];
+    forward_line(line, out, dim);
+    for (int y = 0; y < dim; ++y) blk[y * 32 + x] = out[y];
+  }
+  for (int y = 0; y < dim; ++y) {
+    forward_line(blk + y * 32, out, dim);
+    memcpy(blk + y * 32, out, sizeof(int16_t) * (size_t)dim);
+  }
+}
+
+uint64_t gsto_endpoint_planes(uint32_t w, uint32_t h, const uint64_t *blocks, uint8_t *y, uint8_t *chroma) {
+  const uint32_t bx = w / 4, by = h / 4, tx_n = bx / 32, ty_n = by / 32;
+  const size_t B = (size_t)bx * by;
+  uint8_t *dst[6] = {y, chroma, chroma + B, y + B, chroma + 2 * B, chroma + 3 * B}; /* Y1 Co1 Cg1 Y2 Co2 Cg2 */
+  uint64_t clips = 0;
+  int16_t blk[6][1024];
+  for (uint32_t ty = 0; ty < ty_n; ++ty) {
+    for (uint32_t tx = 0; tx < tx_n; ++tx) {
+      for (int i = 0; i < 1024; ++i) {
+        const uint64_t b = blocks[((size_t)ty * 32 + (size_t)(i / 32)) * bx + (size_t)tx * 32 + (size_t)(i % 32)];
+        int v[6];
+        rgb565_to_ycocg667((uint16_t)b, &v[0], &v[1], &v[2]);
+        rgb565_to_ycocg667((uint16_t)(b >> 16), &v[3], &v[4], &v[5]);
+        for (int p = 0; p < 6; ++p) blk[p][i] = (int16_t)v[p];
+      }
+      for (int p = 0; p < 6; ++p) {
+        for (int dim = 32; dim > 1; dim /= 2) forward_level(blk[p], dim);
+        uint8_t *o = dst[p] + ((size_t)ty * tx_n + tx) * 1024;
+        for (int i = 0; i < 1024; ++i) {
+          if (blk[p][i] < -128 || blk[p][i] > 127) ++clips;
+          o[i] = (uint8_t)(blk[p][i] + 128);
+        }
+      }
+    }
+  }
+  return clips;
+}
+
+uint32_t gsto_run_palette(uint32_t w, uint32_t h, const uint64_t *blocks, uint8_t *palette, size_t pal_cap,
+                          uint8_t *deltas) {
+  const size_t B = (size_t)(w / 4) * (h / 4);
+  const size_t need = (4 * B + GSTO_SYMS_PER_GROUP - 1) / GSTO_SYMS_PER_GROUP * GSTO_SYMS_PER_GROUP;
+  if (pal_cap < need) return 0;
+  size_t n = 0;
+  for (size_t b = 0; b < B; ++b) {
+    const uint32_t word = (uint32_t)(blocks[b] >> 32);
+    const int fresh = b == 0 || word != (uint32_t)(blocks[b - 1] >> 32);
+    if (fresh) wr32(palette + 4 * n++, word);
+    deltas[b] = (uint8_t)(128 + (b > 0 && fresh ? 1 : 0));
+  }
+  const size_t bytes = (4 * n + GSTO_SYMS_PER_GROUP - 1) / GSTO_SYMS_PER_GROUP * GSTO_SYMS_PER_GROUP;
+  memset(palette + 4 * n, 0, bytes - 4 * n);
+  return (uint32_t)bytes;
+}

@@ -144,6 +144,30 @@ size_t gsto_encode_section_bound(size_t n);
 int gsto_encode_stream(uint32_t w, uint32_t h, uint32_t palette_bytes, const uint8_t *y, const uint8_t *chroma,
                        const uint8_t *palette, const uint8_t *indices, uint8_t *out, size_t cap, size_t *out_len);
 
+/* The endpoint stages of GenTC::CompressDXTImage (codec/encoder.cpp:20-98):
+ * per block, RGB565 endpoints -> YCoCg667 (codec/image_processing.cpp:10-27,
+ * RGB565toYCoCg667), the six planes split (ImageSplit), each 32x32 tile
+ * transformed by five levels of the forward 5/3 wavelet, columns then rows
+ * per level (codec/image_processing.h:267-333 FWavelet2D with
+ * codec/wavelet.cpp:37-157, int16 storage, truncating division, mirrored
+ * edges), then MakeUnsigned / Linearize / RearrangeStream / ReducePrecision:
+ * byte = (coefficient + 128) mod 256, tile-major, row-major within a tile.
+ * Writes the Y section (Y1 then Y2 planes, 2B bytes) and the chroma section
+ * (Co1, Cg1, Co2, Cg2, 4B bytes) of B = w*h/16 DXT1 blocks (u64, raster
+ * order).  Returns the number of coefficients outside [-128, 127] (those wrap,
+ * as in the reference encoder). */
+uint64_t gsto_endpoint_planes(uint32_t w, uint32_t h, const uint64_t *blocks, uint8_t *y, uint8_t *chroma);
+
+/* The run index palette of the GPU pipeline (this project's rule in place of
+ * the reference's sequential least-squares search, codec/dxt_image.cpp:510-624):
+ * a block whose index word equals the previous block's reuses its entry,
+ * otherwise the word is appended.  Writes the palette words (LE, padded with
+ * zeros to a multiple of 8192 bytes) and B index deltas (+128: 128 or 129),
+ * and returns the padded palette bytes; pal_cap must be at least 4B rounded up
+ * to 8192. */
+uint32_t gsto_run_palette(uint32_t w, uint32_t h, const uint64_t *blocks, uint8_t *palette, size_t pal_cap,
+                          uint8_t *deltas);
+
 /* ans_decode.cl:97-143 section lookup (ans_decode_multiple), for tests: returns
  * the section x the work-group at `wg` is assigned to by the kernel's search. */
 uint32_t gsto_section_search(const uint32_t *output_offsets, uint32_t num_offsets, uint32_t wg);

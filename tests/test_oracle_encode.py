@@ -92,3 +92,31 @@ def test_normalize_matches_reference_on_random_counts():
         assert ref.gstref_generate_histogram(counts.ctypes.data, counts.size, M, want.ctypes.data) == 0
         st, out = oracle.normalize(counts, M)
         assert st == 0 and np.array_equal(out, want)
+
+
+@pytest.mark.parametrize("name", ["test1.gst", "synth512_s0.gst", "synth768x512_s3.gst"])
+def test_endpoint_planes_rebuild_reference_sections(name):
+    # codec/encoder.cpp:20-98 over the blocks a reference stream decodes to
+    # gives back that stream's Y and chroma sections.
+    s = golden_stream(name)
+    w, h, pal = (int.from_bytes(s[i:i + 4], "little") for i in (0, 4, 8))
+    st, dxt = oracle.decode(s, oracle.SCAN_EXACT)
+    assert st == 0
+    st, sym = oracle.decode_symbols(s)
+    y, c, clips = oracle.endpoint_planes(w, h, np.frombuffer(dxt.tobytes(), np.uint64))
+    B = w * h // 16
+    assert clips == 0 and np.array_equal(y, sym[:2 * B]) and np.array_equal(c, sym[2 * B:6 * B])
+
+
+def test_run_palette_stream_decodes_to_its_blocks():
+    from gst_gb300 import encoder
+    rgb = encoder.synth_image(1024, 512, 31, 0.1)
+    _, blocks, clips = encoder.encode_rgb(rgb)
+    assert clips == 0
+    y, c, clips = oracle.endpoint_planes(1024, 512, blocks)
+    pal, deltas = oracle.run_palette(1024, 512, blocks)
+    assert clips == 0 and set(np.unique(deltas)) <= {128, 129} and pal.size % 8192 == 0
+    st, stream = oracle.encode_stream(1024, 512, pal.size, y, c, pal, deltas)
+    assert st == 0
+    st, dxt = oracle.decode(stream, oracle.SCAN_EXACT)
+    assert st == 0 and np.array_equal(np.frombuffer(dxt.tobytes(), np.uint64), blocks)

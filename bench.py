@@ -283,6 +283,7 @@ def run_only(args, local):
     if args.only == "encode":
         ctx.set_option("encode_hist_match", args.encode_hist_match)
         out = encode_workloads(ctx, stream, flush, device, measured_peak_hbm()[0], args.steps, args.warmup)
+        out.update(dxt_workloads(ctx, stream, flush, device, measured_peak_hbm()[0], args.steps, args.warmup))
         ctx.close()
         return {"only": "encode", **out}
     if args.only == "rans":
@@ -515,6 +516,7 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
         }
         rb.close()
     out.update(encode_workloads(ctx, stream, flush, device, peak, steps, 3))
+    out.update(dxt_workloads(ctx, stream, flush, device, peak, steps, 3))
     sec = workloads.rans_section()
     t, ok, rtuning = time_rans_section(ctx, sec, device, stream, flush, steps, 3)
     alg = len(sec.section) + sec.symbols.size
@@ -564,6 +566,7 @@ def encode_workloads(ctx, stream, flush, device, peak, steps, warmup):
         syms = [device_symbols(ctx, im.stream, device) for im in imgs]
         hdrs = [decoder.parse_header(im.stream) for im in imgs]
         descs = [entropy.stream_symbols(h.width, h.height, h.palette_bytes, s) for h, s in zip(hdrs, syms)]
+        descs = (entropy.StreamSymbols * len(descs))(*descs)
         cap = sum(entropy.stream_bound(h.width, h.height, h.palette_bytes) for h in hdrs)
         d_out = torch.zeros(cap, dtype=torch.uint8, device=device)
         d_offs = torch.zeros(len(imgs) + 1, dtype=torch.int64, device=device)
@@ -605,6 +608,83 @@ def encode_workloads(ctx, stream, flush, device, peak, steps, warmup):
             out[name]["e2e"] = {"ms": round(statistics.median(e2e), 3),
                                 "value": round(n_sym / (statistics.median(e2e) / 1e3) / 1e9, 3), "unit": "Gsym/s",
                                 "h2d_bytes": n_sym, "d2h_bytes": len(s2), "byte_exact": s2 == imgs[0].stream}
+    return out
+
+
+def dxt_workloads(ctx, stream, flush, device, peak, steps, warmup):
+    """The whole encoder on the GPU from DXT1 blocks (include/gst_encode.h):
+    per step gst_prepare_symbols (YCoCg planes, forward wavelet, run palette),
+    the palette sizes read back (the host builds the entropy plan from them),
+    then gst_encode_streams; output checked against the oracle-free property
+    that it decodes to the given blocks.  The endpoint stages are also timed
+    alone.  Inputs: the 64-image batch's and the 8192x8192 texture's blocks."""
+    import torch
+    from gst_gb300 import decoder, entropy, workloads
+    out = {}
+    for name, imgs in (("dxt_to_gst_batched_64", workloads.batched(64)), ("dxt_to_gst_large_8192", [workloads.large()])):
+        bufs, prep, hdr = [], [], []
+        for im in imgs:
+            B = im.width * im.height // 16
+            t = {"b": torch.from_numpy(im.blocks.view(np.int64).copy()).to(device),
+                 "y": torch.empty(2 * B, dtype=torch.uint8, device=device),
+                 "c": torch.empty(4 * B, dtype=torch.uint8, device=device),
+                 "p": torch.empty(entropy.palette_capacity(im.width, im.height), dtype=torch.uint8, device=device),
+                 "i": torch.empty(B, dtype=torch.uint8, device=device)}
+            bufs.append(t)
+            prep.append((im.width, im.height, t["b"], t["y"], t["c"], t["p"], t["i"]))
+        pal = torch.zeros(len(imgs), dtype=torch.int32, device=device)
+        h_pal = torch.zeros(len(imgs), dtype=torch.int32).pin_memory()
+        cap = sum(entropy.stream_bound(im.width, im.height, entropy.palette_capacity(im.width, im.height)) for im in imgs)
+        d_out = torch.zeros(cap, dtype=torch.uint8, device=device)
+        d_offs = torch.zeros(len(imgs) + 1, dtype=torch.int64, device=device)
+
+        prep = entropy.symbol_buffers(prep)  # descriptors built once, as a caller with fixed buffers would
+        descs = (entropy.StreamSymbols * len(imgs))(*[
+            entropy.StreamSymbols(im.width, im.height, 0, 0, t["y"].data_ptr(), t["c"].data_ptr(), t["p"].data_ptr(),
+                                  t["i"].data_ptr()) for im, t in zip(imgs, bufs)])
+
+        def step():
+            entropy.prepare_symbols(ctx, prep, pal, stream)
+            with torch.cuda.stream(stream):
+                h_pal.copy_(pal, non_blocking=True)
+            stream.synchronize()
+            for k, v in enumerate(h_pal.tolist()):
+                descs[k].palette_bytes = v
+            entropy.encode_streams(ctx, descs, d_out, d_offs, stream)
+
+        t_all, _ = time_steps(step, steps, warmup, stream, flush, clear=d_out)
+        ok = decoder.sync_status(ctx, stream) == decoder.GST_OK
+        o = d_offs.cpu().numpy()
+        host = d_out[: int(o[-1])].cpu().numpy().tobytes()
+        for k, im in enumerate(imgs[:8] if len(imgs) > 8 else imgs):
+            got = decoder.decompress_dxt(ctx, host[o[k]:o[k + 1]])
+            ok = ok and bool(np.array_equal(got.view(np.uint64), im.blocks))
+        t_prep, _ = time_steps(lambda: entropy.prepare_symbols(ctx, prep, pal, stream), steps, warmup, stream, flush)
+        ctx.set_profiling(True)
+        _, k = time_steps(lambda: entropy.prepare_symbols(ctx, prep, pal, stream), 3, 1, stream, flush, ctx)
+        ctx.set_profiling(False)
+        ks = kernel_summary(k)
+        ms, ms_prep = statistics.mean(t_all), statistics.mean(t_prep)
+        px = sum(im.pixels for im in imgs)
+        blk_bytes = sum(im.blocks.nbytes for im in imgs)
+        out[name] = {
+            "value": round(px / (ms / 1e3) / 1e6, 1), "unit": "Mpix/s", "ms_per_call": round(ms, 4),
+            "endpoint_stages_ms": round(ms_prep, 4),
+            "endpoint_stages_gbs": round(blk_bytes * 2 / (ms_prep / 1e3) / 1e9, 1),
+            "endpoint_kernels": {kk: round(v["avg_ms"], 4) for kk, v in ks.items()},
+            "dxt1_bytes": blk_bytes, "gst_bytes": int(o[-1]), "decodes_to_blocks": bool(ok),
+        }
+        if name == "dxt_to_gst_large_8192":
+            im = imgs[0]
+            entropy.compress_dxt(ctx, im.width, im.height, im.blocks)
+            e2e = []
+            for _ in range(5):
+                t0 = time.perf_counter()
+                s2 = entropy.compress_dxt(ctx, im.width, im.height, im.blocks)
+                e2e.append((time.perf_counter() - t0) * 1e3)
+            out[name]["e2e"] = {"ms": round(statistics.median(e2e), 3),
+                                "value": round(px / (statistics.median(e2e) / 1e3) / 1e6, 1), "unit": "Mpix/s",
+                                "h2d_bytes": blk_bytes, "d2h_bytes": len(s2)}
     return out
 
 
@@ -716,9 +796,24 @@ def cpu_baseline_encode(images):
         res = list(ex.map(lambda a: oracle.encode_stream(a[0], a[1], a[2], *a[3]), inputs))
     dt = time.perf_counter() - t0
     assert all(st == 0 and s == im.stream for (st, s), im in zip(res, images))
+
+    def from_blocks(im):  # the whole encoder from DXT1 blocks, as the GPU pipeline runs it
+        y, c, _ = oracle.endpoint_planes(im.width, im.height, im.blocks)
+        p, d = oracle.run_palette(im.width, im.height, im.blocks)
+        return oracle.encode_stream(im.width, im.height, p.size, y, c, p, d)
+
+    px = sum(im.pixels for im in images)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        res2 = list(ex.map(from_blocks, images))
+    dt2 = time.perf_counter() - t0
+    assert all(st == 0 for st, _ in res2)
     return {"value": round(n_sym / dt / 1e9, 4), "unit": "Gsym/s", "cores": threads, "kind": "port",
             "sample": f"symbol sections of the first {len(images)} images of the batched workload "
-                      f"({n_sym / 1e6:.1f} M symbols), oracle encode, {threads} threads, {dt:.2f} s"}
+                      f"({n_sym / 1e6:.1f} M symbols), oracle encode, {threads} threads, {dt:.2f} s",
+            "dxt_to_gst": {"value": round(px / dt2 / 1e6, 1), "unit": "Mpix/s", "cores": threads, "kind": "port",
+                           "sample": f"the same {len(images)} images from their DXT1 blocks (endpoint planes, "
+                                     f"run palette, entropy stages), {dt2:.2f} s"}}
 
 
 def run_reference(args, rank, world):

@@ -306,8 +306,8 @@ struct PrepIn {
   uint8_t *y, *chroma, *palette, *indices;
 };
 
-// Builds and launches the endpoint stages of one call; zeroes the palettes.
-gst_status prepare_locked(EncodeState *st, const std::vector<PrepIn> &imgs, uint32_t *d_palette_bytes,
+// Builds and launches the endpoint stages of one call.
+gst_status prepare_locked(gst_ctx *ctx, EncodeState *st, const std::vector<PrepIn> &imgs, uint32_t *d_palette_bytes,
                           cudaStream_t stream) {
   const uint32_t n = static_cast<uint32_t>(imgs.size());
   uint64_t tiles = 0, chunks = 0;
@@ -347,12 +347,13 @@ gst_status prepare_locked(EncodeState *st, const std::vector<PrepIn> &imgs, uint
       pc[c] = {i, k * 8192u, std::min<uint32_t>(8192u, B - k * 8192u), first, first + count - 1};
   }
   cudaError_t e = cudaMemcpyAsync(st->prep_d, st->prep_h, bytes, cudaMemcpyHostToDevice, stream);
-  for (const auto &im : imgs)
-    if (e == cudaSuccess) e = cudaMemsetAsync(im.palette, 0, palette_capacity(im.width, im.height), stream);
+  cudaEvent_t *ev = ctx_timing_events(ctx, false);
   if (e == cudaSuccess)
     e = launch_prepare(reinterpret_cast<const EncPrepImage *>(st->prep_d), n, t,
                        reinterpret_cast<const EncPrepChunk *>(st->prep_d + off_chunks), c,
-                       reinterpret_cast<uint32_t *>(st->prep_d + off_counts), d_palette_bytes, stream);
+                       reinterpret_cast<uint32_t *>(st->prep_d + off_counts), d_palette_bytes, stream, ev,
+                       ctx_timed_names(ctx));
+  ctx_set_timed(ctx, ev ? 3 : 0, 3);
   if (e != cudaSuccess) return cuda_status(e);
   cudaEventRecord(st->prep_done, stream);
   st->prep_used = true;
@@ -481,7 +482,7 @@ gst_status gst_prepare_symbols(gst_ctx *ctx, const gst_symbol_buffers *imgs, int
   EncodeState *st = nullptr;
   const gst_status r = get_state(ctx, &st);
   if (r != GST_OK) return r;
-  return prepare_locked(st, in, d_palette_bytes, static_cast<cudaStream_t>(stream));
+  return prepare_locked(ctx, st, in, d_palette_bytes, static_cast<cudaStream_t>(stream));
 }
 
 gst_status gst_compress_dxt(gst_ctx *ctx, uint32_t width, uint32_t height, const uint64_t *blocks, uint8_t *gst_out,
@@ -510,7 +511,7 @@ gst_status gst_compress_dxt(gst_ctx *ctx, uint32_t width, uint32_t height, const
   if (e != cudaSuccess) return cuda_status(e);
   uint8_t *d = st->in_d;
   const std::vector<PrepIn> in = {{width, height, st->blocks_d, d, d + 2 * B, d + 7 * B, d + 6 * B}};
-  r = prepare_locked(st, in, st->pal_bytes_d, st->own);
+  r = prepare_locked(ctx, st, in, st->pal_bytes_d, st->own);
   if (r != GST_OK) return r;
   uint32_t pal_bytes = 0;
   e = cudaMemcpyAsync(&pal_bytes, st->pal_bytes_d, sizeof(pal_bytes), cudaMemcpyDeviceToHost, st->own);

@@ -25,10 +25,11 @@ cudaError_t launch_encode(const EncPlanView &v, int sm_count, cudaStream_t strea
 
 // gst_prepare.cu
 // Enqueues the endpoint stages (forward wavelet planes, run palette) of the
-// images of a plan; their palettes must be zeroed beforehand.
+// images of a plan.
 cudaError_t launch_prepare(const EncPrepImage *d_images, uint32_t n_images, uint32_t n_tiles,
                            const EncPrepChunk *d_chunks, uint32_t n_chunks, uint32_t *d_counts,
-                           uint32_t *d_palette_bytes, cudaStream_t stream);
+                           uint32_t *d_palette_bytes, cudaStream_t stream, cudaEvent_t *ev = nullptr,
+                           const char **names = nullptr);
 
 // gst_kernels.cu
 // Enqueues the kernels of one plan; names (may be null) receives the name of

@@ -18,7 +18,8 @@
 //     This replaces the reference's sequential least-squares search
 //     (codec/dxt_image.cpp:510-624) with a rule that parallelises: 8192-block
 //     chunks count their new words, then each chunk sums the counts of the
-//     chunks before it in its image, scans its own flags and writes.
+//     chunks before it in its image and writes its entries at ballot
+//     positions.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -82,9 +83,16 @@ __device__ __forceinline__ void forward_level(int *planes, int t) {
 __global__ void __launch_bounds__(kTileThreads) gst_fwd_tile_kernel(const EncPrepImage *__restrict__ images,
                                                                     uint32_t n_images) {
   __shared__ int planes[6 * 32 * kLineStride];
-  // the image of this tile (few images: a linear search)
-  uint32_t im = 0;
-  while (im + 1 < n_images && images[im + 1].first_tile <= blockIdx.x) ++im;
+  // the image of this tile: the last with first_tile <= blockIdx.x
+  uint32_t lo = 0, hi = n_images;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) / 2;
+    if (images[mid].first_tile <= blockIdx.x)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  const uint32_t im = lo;
   const EncPrepImage &img = images[im];
   const uint32_t tile = blockIdx.x - img.first_tile;
   const uint32_t bx = img.width / 4, tiles_x = bx / 32;
@@ -155,57 +163,91 @@ __global__ void __launch_bounds__(kChunkThreads) gst_fwd_count_kernel(const EncP
   if (threadIdx.x == 0) counts[blockIdx.x] = static_cast<uint32_t>(n);
 }
 
+// Each warp takes 1024 consecutive blocks of the chunk, 32 per step (lane =
+// block): the previous block's word comes from the lane below (one load for
+// lane 0), new-word positions from a ballot.  Pass 1 counts per warp; after a
+// scan of the warp counts, pass 2 writes the palette words and index deltas.
 __global__ void __launch_bounds__(kChunkThreads) gst_fwd_palette_kernel(const EncPrepImage *__restrict__ images,
                                                                         const EncPrepChunk *__restrict__ chunks,
                                                                         const uint32_t *__restrict__ counts,
                                                                         uint32_t *__restrict__ palette_bytes) {
-  __shared__ int red[kChunkThreads / 32];
-  __shared__ int scan[kChunkThreads];
+  constexpr int kWarps = kChunkThreads / 32;
+  constexpr int kPerWarp = kChunkBlocks / kWarps;
+  __shared__ int red[kWarps];
+  __shared__ int warp_base[kWarps];
+  __shared__ uint32_t total;
   const EncPrepChunk ch = chunks[blockIdx.x];
   const EncPrepImage &img = images[ch.image];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t lt = (1u << lane) - 1;
   // entries written by the chunks before this one in its image
   int before = 0;
   for (uint32_t c = ch.first_chunk + threadIdx.x; c < blockIdx.x; c += kChunkThreads) before += counts[c];
   before = cta_sum(before, red);
-  // each thread takes a run of consecutive blocks: its flags, then a CTA scan
-  constexpr int kPer = kChunkBlocks / kChunkThreads;
-  const uint32_t lo = threadIdx.x * kPer;
-  int mine = 0;
-  for (int k = 0; k < kPer; ++k)
-    if (lo + k < ch.len) mine += fresh(img.blocks, size_t(ch.start) + lo + k);
-  scan[threadIdx.x] = mine;
+  const uint32_t lo = warp * kPerWarp, hi = min(lo + kPerWarp, ch.len);
+  auto flags = [&](uint32_t at, uint32_t &word) -> uint32_t {  // ballot of new words in blocks at .. at + 31
+    const size_t b = size_t(ch.start) + at + lane;
+    const bool in = at + lane < hi;
+    word = in ? index_word(img.blocks, b) : 0u;
+    uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, word, 1);
+    if (lane == 0) prev = b > 0 ? index_word(img.blocks, b - 1) : ~word;
+    return __ballot_sync(0xFFFFFFFFu, in && (b == 0 || word != prev));
+  };
+  int n = 0;
+  for (uint32_t at = lo; at < hi; at += 32) {
+    uint32_t word;
+    n += __popc(flags(at, word));
+  }
+  if (lane == 0) warp_base[warp] = n;
   __syncthreads();
-  for (int o = 1; o < kChunkThreads; o <<= 1) {
-    const int u = threadIdx.x >= static_cast<unsigned>(o) ? scan[threadIdx.x - o] : 0;
-    __syncthreads();
-    scan[threadIdx.x] += u;
-    __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = before;
+    for (int w = 0; w < kWarps; ++w) {
+      const int c = warp_base[w];
+      warp_base[w] = run;
+      run += c;
+    }
+    total = 4u * static_cast<uint32_t>(run);
   }
-  int at = before + scan[threadIdx.x] - mine;  // palette entries before this thread's run
+  __syncthreads();
+  int base = warp_base[warp];
   uint32_t *pal = reinterpret_cast<uint32_t *>(img.palette);
-  for (int k = 0; k < kPer; ++k) {
-    if (lo + k >= ch.len) break;
-    const size_t b = size_t(ch.start) + lo + k;
-    const uint32_t f = fresh(img.blocks, b);
-    if (f) pal[at++] = index_word(img.blocks, b);
-    img.indices[b] = static_cast<uint8_t>(128 + (b > 0 ? f : 0));
+  for (uint32_t at = lo; at < hi; at += 32) {
+    uint32_t word;
+    const uint32_t m = flags(at, word);
+    const size_t b = size_t(ch.start) + at + lane;
+    if (m >> lane & 1) pal[base + __popc(m & lt)] = word;
+    if (at + lane < hi) img.indices[b] = static_cast<uint8_t>(128 + (b > 0 ? (m >> lane & 1) : 0));
+    base += __popc(m);
   }
-  if (blockIdx.x == ch.last_chunk && threadIdx.x == kChunkThreads - 1) {
-    const uint32_t bytes = 4u * static_cast<uint32_t>(at);
-    palette_bytes[ch.image] = (bytes + kSymsPerGroup - 1) / kSymsPerGroup * kSymsPerGroup;
+  if (blockIdx.x == ch.last_chunk) {
+    // the image's last chunk: its palette size, and zeros up to the padded end
+    const uint32_t end = (total + kSymsPerGroup - 1) / kSymsPerGroup * kSymsPerGroup;
+    for (uint32_t q = total + threadIdx.x; q < end; q += kChunkThreads) img.palette[q] = 0;
+    if (threadIdx.x == 0) palette_bytes[ch.image] = end;
   }
 }
 
 }  // namespace
 
-// Enqueues the endpoint stages of one plan; the palettes must be zeroed
-// beforehand (their padding stays zero).
+// Enqueues the endpoint stages of one plan.
+// With `ev` non-null, records ev[0] before the first kernel and ev[i + 1]
+// after kernel i, whose name goes to names[i] (instrumentation).
 cudaError_t launch_prepare(const EncPrepImage *d_images, uint32_t n_images, uint32_t n_tiles,
                            const EncPrepChunk *d_chunks, uint32_t n_chunks, uint32_t *d_counts,
-                           uint32_t *d_palette_bytes, cudaStream_t stream) {
+                           uint32_t *d_palette_bytes, cudaStream_t stream, cudaEvent_t *ev, const char **names) {
+  if (ev) cudaEventRecord(ev[0], stream);
   gst_fwd_tile_kernel<<<n_tiles, kTileThreads, 0, stream>>>(d_images, n_images);
+  if (ev) cudaEventRecord(ev[1], stream);
   gst_fwd_count_kernel<<<n_chunks, kChunkThreads, 0, stream>>>(d_images, d_chunks, d_counts);
+  if (ev) cudaEventRecord(ev[2], stream);
   gst_fwd_palette_kernel<<<n_chunks, kChunkThreads, 0, stream>>>(d_images, d_chunks, d_counts, d_palette_bytes);
+  if (ev) cudaEventRecord(ev[3], stream);
+  if (names) {
+    names[0] = "gst_fwd_tile_kernel";
+    names[1] = "gst_fwd_count_kernel";
+    names[2] = "gst_fwd_palette_kernel";
+  }
   return cudaGetLastError();
 }
 

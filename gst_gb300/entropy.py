@@ -59,12 +59,13 @@ def stream_symbols(width: int, height: int, palette_bytes: int, symbols) -> Stre
                          base + 6 * B + palette_bytes)
 
 
-def encode_streams(ctx: GPUContext, images: Sequence[StreamSymbols], out, offsets, stream=None) -> None:
+def encode_streams(ctx: GPUContext, images, out, offsets, stream=None) -> None:
     """Enqueues one GST stream per image into `out`; `offsets` (int64,
-    len(images) + 1) receives the stream starts and the total."""
+    len(images) + 1) receives the stream starts and the total.  `images`: a
+    sequence of StreamSymbols or a ctypes array of them (reused as is)."""
     lib = load_library()
-    arr = (StreamSymbols * len(images))(*images)
-    _check(lib.gst_encode_streams(ctx.handle, arr, len(images), _ptr(out), int(out.numel()), _ptr(offsets),
+    arr = images if isinstance(images, ctypes.Array) else (StreamSymbols * len(images))(*images)
+    _check(lib.gst_encode_streams(ctx.handle, arr, len(arr), _ptr(out), int(out.numel()), _ptr(offsets),
                                   _stream(stream)), "gst_encode_streams")
 
 
@@ -86,14 +87,20 @@ def palette_capacity(width: int, height: int) -> int:
     return int(load_library().gst_palette_capacity(width, height))
 
 
-def prepare_symbols(ctx: GPUContext, images: Sequence[tuple], d_palette_bytes, stream=None) -> None:
+def symbol_buffers(images: Sequence[tuple]) -> ctypes.Array:
+    """The gst_symbol_buffers array of (width, height, d_blocks, d_y, d_chroma,
+    d_palette, d_indices) tuples (device tensors or pointers), for reuse."""
+    return (SymbolBuffers * len(images))(*[SymbolBuffers(w, h, *(_ptr(b) for b in bufs)) for w, h, *bufs in images])
+
+
+def prepare_symbols(ctx: GPUContext, images, d_palette_bytes, stream=None) -> None:
     """Enqueues the endpoint stages; images: (width, height, d_blocks, d_y,
-    d_chroma, d_palette, d_indices) with device buffers (uint8 / uint64
-    tensors or pointers); d_palette_bytes: uint32/int32 device array, one per
-    image."""
+    d_chroma, d_palette, d_indices) tuples with device buffers (uint8 / uint64
+    tensors or pointers), or a symbol_buffers() array; d_palette_bytes:
+    uint32/int32 device array, one per image."""
     lib = load_library()
-    arr = (SymbolBuffers * len(images))(*[SymbolBuffers(w, h, *(_ptr(b) for b in bufs)) for w, h, *bufs in images])
-    _check(lib.gst_prepare_symbols(ctx.handle, arr, len(images), _ptr(d_palette_bytes), _stream(stream)),
+    arr = images if isinstance(images, ctypes.Array) else symbol_buffers(images)
+    _check(lib.gst_prepare_symbols(ctx.handle, arr, len(arr), _ptr(d_palette_bytes), _stream(stream)),
            "gst_prepare_symbols")
 
 

@@ -282,6 +282,12 @@ void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph,
   uint64_t body = page + size_t(n) * 4 * kFreqTableBytes;
   uint64_t scratch_off = 0, out_off = 0;
   uint32_t ri = 0, ti = 0;
+  struct SectionItems {
+    uint64_t cost;  // compressed bytes per group (x16)
+    uint32_t first, count;
+  };
+  std::vector<SectionItems> by_section;
+  by_section.reserve(4 * size_t(n));
   for (int i = 0; i < n; ++i) {
     const gst_header &h = hdrs[i];
     GstImageDesc &d = imgs[i];
@@ -302,9 +308,11 @@ void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph,
       d.sec_out[s] = o;
       in += lens[s];
       o += syms[s];
+      by_section.push_back({uint64_t(lens[s]) * 16 / std::max<uint32_t>(1u, d.sec_groups[s]), ri, 0});
       for (uint32_t g = 0; g < d.sec_groups[s]; g += kGroupsPerRansCta)
         rans[ri++] = {uint32_t(i), uint32_t(s), g, uint16_t(std::min(kGroupsPerRansCta, d.sec_groups[s] - g)),
                       uint16_t(kStreamsPerGroup)};
+      by_section.back().count = ri - by_section.back().first;
     }
     d.bx = h.width / 4;
     d.by = h.height / 4;
@@ -320,13 +328,14 @@ void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph,
   // start first, so that the launch does not end on a few long items.  (The
   // persistent kernel keeps image order, so that images finish one after
   // another and their tiles can start early.)
+  // The cost is a section's, so sorting the sections (stably) and emitting
+  // each one's items in turn gives the items' stable order by cost.
   uint32_t *order = reinterpret_cast<uint32_t *>(ph + L.off_order);
-  for (uint32_t k = 0; k < ri; ++k) order[k] = k;
-  auto cost = [&](uint32_t k) {
-    const GstImageDesc &d = imgs[rans[k].image];
-    return uint64_t(d.sec_len[rans[k].section]) * 16 / std::max<uint32_t>(1u, d.sec_groups[rans[k].section]);
-  };
-  std::stable_sort(order, order + ri, [&](uint32_t a, uint32_t b) { return cost(a) > cost(b); });
+  std::stable_sort(by_section.begin(), by_section.end(),
+                   [](const SectionItems &a, const SectionItems &b) { return a.cost > b.cost; });
+  uint32_t k = 0;
+  for (const SectionItems &sec : by_section)
+    for (uint32_t j = 0; j < sec.count; ++j) order[k++] = sec.first + j;
 }
 
 GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) {
@@ -370,6 +379,35 @@ gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8
     ctx->scratch_used = true;
   }
   return GST_OK;
+}
+
+// Chunk boundaries of a pipelined host-to-host decode: contiguous runs of
+// images whose block counts rise as 1, 2, 4, ... and fall again towards the
+// end (..., 4, 2, 1).  The copies out are the slowest stage (the decode runs
+// ~2.4x faster than the device-to-host link), so a small first chunk starts
+// them early, every later chunk is decoded while the copies out before it
+// run, and a small last chunk leaves little to copy after the last decode.
+std::vector<int> chunk_cuts(const gst_header *hdrs, int n, int chunks, uint64_t blocks) {
+  std::vector<double> bound(chunks);  // cumulative fraction of the blocks at the end of chunk k
+  double wsum = 0;
+  auto weight = [&](int k) { return 1u << std::min(k, chunks - 1 - k); };
+  for (int k = 0; k < chunks; ++k) wsum += double(weight(k));
+  for (int k = 0, acc_w = 0; k < chunks; ++k) {
+    acc_w += int(weight(k));
+    bound[k] = double(acc_w) / wsum;
+  }
+  std::vector<int> cut(1, 0);
+  uint64_t acc = 0;
+  for (int i = 0; i < n; ++i) {
+    acc += image_blocks(hdrs[i]);
+    const int k = int(cut.size()) - 1;  // the chunk image i belongs to
+    const int left_images = n - (i + 1), left_chunks = chunks - int(cut.size());
+    if (left_chunks > 0 && left_images >= left_chunks &&
+        (double(acc) >= bound[k] * double(blocks) || left_images == left_chunks))
+      cut.push_back(i + 1);
+  }
+  cut.push_back(n);
+  return cut;
 }
 
 gst_status read_device_status(gst_ctx *ctx, cudaStream_t stream) {
@@ -427,6 +465,21 @@ struct gst_batch {
   const void *graph_cmp = nullptr;
   void *graph_out = nullptr;
   GstTuning graph_tuning;
+  std::vector<gst_header> hdrs;
+  // Host-buffer launches (gst_batch_host_launch): device mirrors of the
+  // caller's pinned input and output, per-chunk plans uploaded once, and the
+  // captured pipeline per (input, output, chunks, tuning).
+  uint8_t *hm_cmp = nullptr, *hm_out = nullptr;
+  uint8_t *hm_plans = nullptr;
+  int hm_chunks = 0;
+  std::vector<int> hm_cut;
+  std::vector<PlanLayout> hm_lay;
+  std::vector<size_t> hm_plan_off;
+  cudaStream_t hm_stream[3] = {};
+  cudaGraphExec_t hm_graph = nullptr;
+  const void *hm_graph_cmp = nullptr;
+  void *hm_graph_out = nullptr;
+  GstTuning hm_graph_tuning;
 };
 
 namespace {
@@ -702,10 +755,7 @@ gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const
     if (e != cudaSuccess) return cuda_status(e);
   }
   // Where each image's tables, sections and blocks are (the reference's
-  // layout, codec/decoder.cpp:430-476), and the chunk boundaries: contiguous
-  // runs of images whose block counts grow as 1, 1, 2, 4, ... so that the
-  // first copy out starts early and every later chunk is decoded while the
-  // copies out before it run.
+  // layout, codec/decoder.cpp:430-476), and the chunk boundaries.
   const size_t page = offsets_page_bytes(n);
   std::vector<uint64_t> body(n + 1), out(n + 1);
   body[0] = page + size_t(n) * 4 * kFreqTableBytes;
@@ -716,24 +766,7 @@ gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const
     out[i + 1] = out[i] + 8 * image_blocks(hdrs[i]);
     blocks += image_blocks(hdrs[i]);
   }
-  std::vector<double> bound(chunks);  // cumulative fraction of the blocks at the end of chunk k
-  double wsum = 0;
-  for (int k = 0; k < chunks; ++k) wsum += k < 2 ? 1.0 : double(1u << (k - 1));
-  for (int k = 0, acc_w = 0; k < chunks; ++k) {
-    acc_w += k < 2 ? 1 : int(1u << (k - 1));
-    bound[k] = double(acc_w) / wsum;
-  }
-  std::vector<int> cut(1, 0);
-  uint64_t acc = 0;
-  for (int i = 0; i < n; ++i) {
-    acc += image_blocks(hdrs[i]);
-    const int k = int(cut.size()) - 1;  // the chunk image i belongs to
-    const int left_images = n - (i + 1), left_chunks = chunks - int(cut.size());
-    if (left_chunks > 0 && left_images >= left_chunks &&
-        (double(acc) >= bound[k] * double(blocks) || left_images == left_chunks))
-      cut.push_back(i + 1);
-  }
-  cut.push_back(n);
+  const std::vector<int> cut = chunk_cuts(hdrs, n, chunks, blocks);
   const int nc = int(cut.size()) - 1;
   gst_status st = grow_device(&ctx->hs_cmp_d, &ctx->hs_cmp_cap, body[n]);
   if (st == GST_OK) st = grow_device(&ctx->hs_out_d, &ctx->hs_out_cap, out[n]);
@@ -904,6 +937,7 @@ gst_status gst_batch_create(gst_ctx *ctx, const gst_header *hdrs, int n, gst_bat
   cudaSetDevice(ctx->device);
   gst_batch *b = new gst_batch();
   b->ctx = ctx;
+  b->hdrs.assign(hdrs, hdrs + n);
   b->layout = plan_layout(hdrs, n);
   b->compressed_bytes = gst_batch_layout_bytes(hdrs, n);
   for (int i = 0; i < n; ++i) b->out_bytes += size_t(image_blocks(hdrs[i])) * 8;
@@ -925,6 +959,12 @@ void gst_batch_destroy(gst_batch *b) {
   cudaSetDevice(b->ctx->device);
   cudaDeviceSynchronize();
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->hm_graph) cudaGraphExecDestroy(b->hm_graph);
+  for (cudaStream_t s : b->hm_stream)
+    if (s) cudaStreamDestroy(s);
+  cudaFree(b->hm_cmp);
+  cudaFree(b->hm_out);
+  cudaFree(b->hm_plans);
   cudaFree(b->plan_d);
   cudaFree(b->scratch);
   delete b;
@@ -986,6 +1026,149 @@ gst_status gst_batch_graph_launch(gst_batch *b, const void *d_cmp, void *d_out, 
     b->graph_tuning = batch_tuning(b);
   }
   return cuda_status(cudaGraphLaunch(b->graph, static_cast<cudaStream_t>(stream)));
+}
+
+gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, int chunks, void *stream) {
+  if (!b || !h_cmp || !h_out || chunks < 0) return GST_E_ARG;
+  gst_ctx *ctx = b->ctx;
+  const int n = int(b->hdrs.size());
+  if (chunks == 0) chunks = std::min(n, 3);
+  chunks = std::min(chunks, n);
+  cudaSetDevice(ctx->device);
+  cudaStream_t caller = static_cast<cudaStream_t>(stream);
+  if (capturing(caller)) return GST_E_ARG;
+  const GstTuning tuning = batch_tuning(b);
+  const gst_header *hdrs = b->hdrs.data();
+  const size_t page = offsets_page_bytes(n);
+  std::vector<uint64_t> body(n + 1), out(n + 1);
+  body[0] = page + size_t(n) * 4 * kFreqTableBytes;
+  out[0] = 0;
+  uint64_t blocks = 0;
+  for (int i = 0; i < n; ++i) {
+    body[i + 1] = body[i] + section_bytes(hdrs[i]);
+    out[i + 1] = out[i] + 8 * image_blocks(hdrs[i]);
+    blocks += image_blocks(hdrs[i]);
+  }
+  cudaError_t e = cudaSuccess;
+  if (!b->hm_cmp) {
+    e = cudaMalloc(reinterpret_cast<void **>(&b->hm_cmp), body[n]);
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(&b->hm_out), out[n]);
+    for (auto &s : b->hm_stream)
+      if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  if (b->hm_chunks != chunks) {
+    // Per-chunk plans with absolute addresses in the mirrors, uploaded once.
+    const std::vector<int> cut = chunk_cuts(hdrs, n, chunks, blocks);
+    const int nc = int(cut.size()) - 1;
+    std::vector<PlanLayout> lay(nc);
+    std::vector<size_t> off(nc + 1, 0);
+    for (int c = 0; c < nc; ++c) {
+      lay[c] = plan_layout(hdrs + cut[c], cut[c + 1] - cut[c]);
+      off[c + 1] = align_up(off[c] + lay[c].bytes, 256);
+    }
+    if (b->hm_graph) cudaGraphExecDestroy(b->hm_graph);
+    b->hm_graph = nullptr;
+    cudaDeviceSynchronize();  // earlier launches may still read the old plans
+    cudaFree(b->hm_plans);
+    b->hm_plans = nullptr;
+    b->hm_chunks = 0;
+    e = cudaMalloc(reinterpret_cast<void **>(&b->hm_plans), std::max<size_t>(off[nc], 256));
+    if (e != cudaSuccess) return cuda_status(e);
+    std::vector<uint8_t> ph(off[nc]);
+    for (int c = 0; c < nc; ++c) {
+      const int i0 = cut[c], m = cut[c + 1] - i0;
+      std::vector<uint64_t> fa(m), ba(m), oa(m);
+      for (int k = 0; k < m; ++k) {
+        fa[k] = reinterpret_cast<uint64_t>(b->hm_cmp + page + size_t(i0 + k) * 4 * kFreqTableBytes);
+        ba[k] = reinterpret_cast<uint64_t>(b->hm_cmp + body[i0 + k]);
+        oa[k] = reinterpret_cast<uint64_t>(b->hm_out + out[i0 + k]);
+      }
+      write_plan(lay[c], hdrs + i0, m, ph.data() + off[c], fa.data(), ba.data(), oa.data());
+    }
+    e = cudaMemcpy(b->hm_plans, ph.data(), off[nc], cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_status(e);
+    b->hm_cut = cut;
+    b->hm_lay = std::move(lay);
+    b->hm_plan_off = std::move(off);
+    b->hm_chunks = chunks;
+  }
+  if (!b->hm_graph || b->hm_graph_cmp != h_cmp || b->hm_graph_out != h_out || b->hm_graph_tuning != tuning) {
+    // Capture the copies in, decodes and copies out of every chunk on three
+    // streams, enqueued in three passes as gst_load_host_dxts does.
+    {
+      std::lock_guard<std::mutex> lock(ctx->mu);
+      launch_decode(nullptr, nullptr, nullptr, GstPlanView{}, nullptr, &ctx->last_launches, nullptr,
+                    GstTuning{});  // configure attributes
+    }
+    const int nc = int(b->hm_cut.size()) - 1;
+    const uint8_t *hc = static_cast<const uint8_t *>(h_cmp);
+    uint8_t *ho = static_cast<uint8_t *>(h_out);
+    cudaStream_t cs = nullptr, si = b->hm_stream[0], sc = b->hm_stream[1], so = b->hm_stream[2];
+    std::vector<cudaEvent_t> evs(2 * nc + 4, nullptr);
+    e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    for (auto &ev : evs)
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    cudaGraph_t g = nullptr;
+    bool capturing_now = false;
+    if (e == cudaSuccess) {
+      e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+      capturing_now = e == cudaSuccess;
+    }
+    cudaEvent_t fork = evs[2 * nc], end_i = evs[2 * nc + 1], end_c = evs[2 * nc + 2], end_o = evs[2 * nc + 3];
+    if (e == cudaSuccess) e = cudaEventRecord(fork, cs);
+    for (cudaStream_t s : {si, sc, so})
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, fork, 0);
+    for (int c = 0; c < nc && e == cudaSuccess; ++c) {
+      const int i0 = b->hm_cut[c], i1 = b->hm_cut[c + 1];
+      const size_t t0 = page + size_t(i0) * 4 * kFreqTableBytes, t1 = page + size_t(i1) * 4 * kFreqTableBytes;
+      e = cudaMemcpyAsync(b->hm_cmp + t0, hc + t0, t1 - t0, cudaMemcpyHostToDevice, si);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->hm_cmp + body[i0], hc + body[i0], body[i1] - body[i0], cudaMemcpyHostToDevice, si);
+      if (e == cudaSuccess) e = cudaEventRecord(evs[c], si);
+    }
+    for (int c = 0; c < nc && e == cudaSuccess; ++c) {
+      e = cudaStreamWaitEvent(sc, evs[c], 0);
+      GstPlanView view = plan_view(b->hm_lay[c], b->hm_plans + b->hm_plan_off[c], ctx->status_d);
+      view.image_err = nullptr;
+      view.wait_limit_ns = ctx->wait_limit_ns;
+      int launches = 0;
+      if (e == cudaSuccess) e = launch_decode(nullptr, b->scratch, nullptr, view, sc, &launches, nullptr, tuning);
+      if (e == cudaSuccess) e = cudaEventRecord(evs[nc + c], sc);
+    }
+    for (int c = 0; c < nc && e == cudaSuccess; ++c) {
+      const int i0 = b->hm_cut[c], i1 = b->hm_cut[c + 1];
+      e = cudaStreamWaitEvent(so, evs[nc + c], 0);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ho + out[i0], b->hm_out + out[i0], out[i1] - out[i0], cudaMemcpyDeviceToHost, so);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(end_i, si);
+    if (e == cudaSuccess) e = cudaEventRecord(end_c, sc);
+    if (e == cudaSuccess) e = cudaEventRecord(end_o, so);
+    for (cudaEvent_t ev : {end_i, end_c, end_o})
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev, 0);
+    if (capturing_now) {
+      const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+      if (e == cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) {
+      if (b->hm_graph) cudaGraphExecDestroy(b->hm_graph);
+      b->hm_graph = nullptr;
+      e = cudaGraphInstantiate(&b->hm_graph, g, 0);
+    }
+    if (g) cudaGraphDestroy(g);
+    for (auto ev : evs)
+      if (ev) cudaEventDestroy(ev);
+    if (cs) cudaStreamDestroy(cs);
+    if (e != cudaSuccess) {
+      b->hm_graph = nullptr;
+      return cuda_status(e);
+    }
+    b->hm_graph_cmp = h_cmp;
+    b->hm_graph_out = h_out;
+    b->hm_graph_tuning = tuning;
+  }
+  return cuda_status(cudaGraphLaunch(b->hm_graph, caller));
 }
 
 gst_status gst_set_option(gst_ctx *ctx, const char *name, int value) {

@@ -44,7 +44,7 @@ EXPORTED_SYMBOLS = (
     "gst_load_host_dxts",
     "gst_batch_layout_bytes", "gst_pack_batch", "gst_decode_rans_groups",
     "gst_batch_create", "gst_batch_destroy", "gst_batch_device_bytes", "gst_batch_launch",
-    "gst_batch_graph_launch", "gst_batch_autotune", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
+    "gst_batch_graph_launch", "gst_batch_host_launch", "gst_batch_autotune", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
     "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times", "gst_set_option",
     "gst_status_string",
     "gst_server_create", "gst_server_destroy", "gst_server_now_ns", "gst_server_submit", "gst_server_poll",
@@ -172,6 +172,7 @@ def load_library() -> ctypes.CDLL:
         "gst_batch_autotune": (I, [P, P, P, P, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]),
         "gst_batch_set_tuning": (I, [P, I, I, I]),
         "gst_batch_graph_launch": (I, [P, P, P, P]),
+        "gst_batch_host_launch": (I, [P, P, P, I, P]),
         "gst_load_compressed_dxt_static": (I, [HP, P, P, P, ctypes.POINTER(U32)]),
         "gst_sync_status": (I, [P, P]),
         "gst_last_launch_count": (I, [P]),
@@ -309,6 +310,12 @@ class ResidentBatch:
         fn = load_library().gst_batch_graph_launch if graph else load_library().gst_batch_launch
         _check(fn(self._h, _ptr(cmp_data), _ptr(output), _stream(stream)), "gst_batch_launch")
 
+    def host_launch(self, h_cmp, h_out, chunks: int = 0, stream=None) -> None:
+        """gst_batch_host_launch: pinned host layout in, pinned DXT1 out, the
+        pipelined copies and decodes replayed from a captured graph."""
+        _check(load_library().gst_batch_host_launch(self._h, _ptr(h_cmp), _ptr(h_out), int(chunks), _stream(stream)),
+               "gst_batch_host_launch")
+
     def autotune(self, cmp_data, output, stream=None, iterations: int = 3) -> tuple[int, int, int]:
         """gst_batch_autotune: times each launch configuration on this batch
         and keeps the fastest; returns (blocks_per_sm, stage_words, persistent)."""
@@ -366,11 +373,16 @@ def load_compressed_dxts(ctx: GPUContext, hdrs: Sequence[GenTCHeader], cmp_data,
                                                    _stream(stream)), "gst_load_compressed_dxts")
 
 
-def load_host_dxts(ctx: GPUContext, hdrs: Sequence[GenTCHeader], h_cmp, h_out, chunks: int = 0,
-                   stream=None) -> None:
+def header_array(hdrs: Sequence[GenTCHeader]) -> ctypes.Array:
+    """The gst_header array of a batch, for calls that reuse it."""
+    return (GenTCHeader * len(hdrs))(*hdrs)
+
+
+def load_host_dxts(ctx: GPUContext, hdrs, h_cmp, h_out, chunks: int = 0, stream=None) -> None:
     """gst_load_host_dxts: pinned host layout in, pinned host DXT1 out, with the
-    copies in, decodes and copies out of `chunks` runs of images overlapped."""
-    arr = (GenTCHeader * len(hdrs))(*hdrs)
+    copies in, decodes and copies out of `chunks` runs of images overlapped.
+    `hdrs`: GenTCHeader sequence or a header_array()."""
+    arr = hdrs if isinstance(hdrs, ctypes.Array) else header_array(hdrs)
     _check(load_library().gst_load_host_dxts(ctx.handle, arr, len(hdrs), _ptr(h_cmp), _ptr(h_out), int(chunks),
                                              _stream(stream)), "gst_load_host_dxts")
 

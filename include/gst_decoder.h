@@ -118,10 +118,12 @@ gst_status gst_load_rgbs(gst_ctx *ctx, const gst_header *hdrs, int n, const void
  * demo/photos_sf.cpp:688-830, no counterpart API in the reference): h_cmp is
  * the reference's layout (as for gst_load_compressed_dxts) and h_out the
  * DXT1 output, both in pinned host memory (cudaMallocHost / cudaHostAlloc).
- * The n images are split into `chunks` (0 = up to 8) contiguous runs of about
- * equal block counts; each run's tables and sections are copied in, decoded
- * and copied out on three internal streams, so that copies in, decodes and
- * copies out of different runs overlap.  Enqueued after the work already on
+ * The n images are split into `chunks` (0 = up to 8) contiguous runs whose
+ * block counts rise as 1, 2, 4, ... and fall again towards the end; each
+ * run's tables and sections are copied in, decoded and copied out on three
+ * internal streams, so that copies in, decodes and copies out of different
+ * runs overlap (small first and last runs: the copies out, the slowest stage,
+ * start early and little is left after the last decode).  Enqueued after the work already on
  * `stream`, and `stream` waits for the last copy out: h_out is complete once
  * `stream` reaches that point.  Calls on one context run one after another. */
 gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const void *h_cmp, void *h_out,
@@ -143,6 +145,15 @@ void gst_batch_destroy(gst_batch *batch);
 size_t gst_batch_device_bytes(const gst_batch *batch);
 gst_status gst_batch_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
 gst_status gst_batch_graph_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
+
+/* The batch from pinned host memory to pinned host memory: gst_load_host_dxts's
+ * pipeline (copies in, decodes and copies out of `chunks` runs overlapped,
+ * 0 = 3) with the batch's own device mirrors and per-run plans, built once per
+ * chunk count, and the whole pipeline captured as one CUDA graph per (h_cmp,
+ * h_out, chunks, tuning) and replayed: a call costs one graph launch of host
+ * work, while every copy and decode runs each time.  The batch's device
+ * launches and its host launches must not run concurrently. */
+gst_status gst_batch_host_launch(gst_batch *batch, const void *h_cmp, void *h_out, int chunks, void *stream);
 
 /* Per-batch tuning of the launch (no counterpart in the reference).
  * gst_batch_autotune decodes the batch under each of a fixed set of

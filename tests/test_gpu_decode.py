@@ -372,6 +372,29 @@ def test_load_host_dxts_pipelined(gpu_ctx, chunks):
         assert np.array_equal(h_out.numpy().view(np.uint64), want)
 
 
+@pytest.mark.parametrize("chunks,persistent", [(1, 0), (3, 0), (5, 1)])
+def test_batch_host_launch_graph(gpu_ctx, chunks, persistent):
+    # gst_batch_host_launch: the pipelined host-to-host decode replayed from a
+    # captured graph; repeated calls (outputs cleared in between), a new
+    # output buffer and a change of chunk count each give the right blocks.
+    imgs = [workloads.encode_image(w, h, 870 + i) for i, (w, h) in
+            enumerate([(512, 512), (2048, 1024), (1024, 512), (512, 2048), (1024, 1024), (512, 1024)])]
+    hdrs, packed = decoder.pack_batch([im.stream for im in imgs])
+    want = np.concatenate([im.blocks for im in imgs])
+    rb = decoder.ResidentBatch(gpu_ctx, hdrs)
+    rb.set_tuning(8, 1016, persistent)
+    h_cmp = torch.from_numpy(packed).pin_memory()
+    outs = [torch.zeros(sum(h.dxt_bytes for h in hdrs), dtype=torch.uint8).pin_memory() for _ in range(2)]
+    s = torch.cuda.Stream()
+    for it, (k, c) in enumerate([(0, chunks), (0, chunks), (1, chunks), (0, 2)]):
+        outs[k].zero_()
+        rb.host_launch(h_cmp, outs[k], c, s)
+        s.synchronize()
+        assert decoder.sync_status(gpu_ctx, s) == decoder.GST_OK
+        assert np.array_equal(outs[k].numpy().view(np.uint64), want), it
+    rb.close()
+
+
 def test_persistent_wait_times_out_and_context_survives():
     # Fault injection on the host: the persistent launch leaves out its rANS
     # items, so every tile's bounded wait runs out (1 ms here) and the call

@@ -42,6 +42,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "gst_encode_plan.h"
 #include "gst_plan.h"
 
@@ -712,7 +714,7 @@ __global__ void __launch_bounds__(kFinishThreads) gst_enc_finish_kernel(EncPlanV
   }
 }
 
-int g_rans_blocks_per_sm = 0;
+std::atomic<int> g_rans_blocks_per_sm{0};  // occupancy of the encode kernel, computed once per process
 
 }  // namespace
 
@@ -739,15 +741,17 @@ cudaError_t launch_encode(const EncPlanView &v, int sm_count, cudaStream_t strea
   gst_enc_normalize_kernel<<<v.n_sections, kNormThreads + 32, 0, stream>>>(v);
   mark("gst_enc_normalize_kernel");
   if (!normalize_only) {
-    if (g_rans_blocks_per_sm == 0) {
+    int per_sm = g_rans_blocks_per_sm.load(std::memory_order_relaxed);
+    if (per_sm == 0) {
       int b = 0;
       const cudaError_t e =
           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, gst_enc_rans_kernel<kEncWarps>, kEncWarps * 32, 0);
       if (e != cudaSuccess) return e;
-      g_rans_blocks_per_sm = b > 0 ? b : 1;
+      per_sm = b > 0 ? b : 1;
+      g_rans_blocks_per_sm.store(per_sm, std::memory_order_relaxed);
     }
     const uint32_t need = (v.n_groups + kEncWarps - 1) / kEncWarps;
-    const uint32_t fill = static_cast<uint32_t>(g_rans_blocks_per_sm * sm_count);
+    const uint32_t fill = static_cast<uint32_t>(per_sm * sm_count);
     gst_enc_rans_kernel<kEncWarps><<<need < fill ? need : fill, kEncWarps * 32, 0, stream>>>(v);
     mark("gst_enc_rans_kernel");
     gst_enc_finish_kernel<<<v.n_sections, kFinishThreads, 0, stream>>>(v);

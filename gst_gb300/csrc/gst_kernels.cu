@@ -29,6 +29,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "gst_plan.h"
 
@@ -861,8 +862,8 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
                           cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning,
                           const char **names) {
   *launches = 0;
-  static bool configured = false;  // per process; the attribute applies to every device context
-  if (!configured) {
+  static std::atomic<bool> configured{false};  // per process; the attribute applies to every device context
+  if (!configured.load(std::memory_order_acquire)) {
     const int bytes = static_cast<int>(rans_smem_bytes(kMaxStageWords));
     cudaError_t e = cudaFuncSetAttribute(gst_rans_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
@@ -873,7 +874,7 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
       e = cudaFuncSetAttribute(gst_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                static_cast<int>(persistent_smem_bytes(kMaxStageWords)));
     if (e != cudaSuccess) return e;
-    configured = true;
+    configured.store(true, std::memory_order_release);  // setting the attributes twice is harmless
   }
   if (tuning.stage_words < kMinStageWords || tuning.stage_words > kMaxStageWords || (tuning.stage_words & 7))
     return cudaErrorInvalidValue;

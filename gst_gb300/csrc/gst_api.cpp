@@ -132,6 +132,7 @@ struct gst_ctx {
   bool hs_used = false;
   gst::host::EncodeState *enc = nullptr;  // encoder calls (gst_encode_api.cpp)
   bool enc_hist_match = false;            // encoder byte counts: merge equal lanes before the atomic
+  bool inject_encode_stall = false;       // fault injection for tests: group 1 never publishes its size
 };
 
 namespace gst {
@@ -443,6 +444,7 @@ void ctx_set_timed(gst_ctx *ctx, int kernels, int launches) {
 }
 const char **ctx_timed_names(gst_ctx *ctx) { return ctx->timed_names; }
 bool ctx_enc_hist_match(gst_ctx *ctx) { return ctx->enc_hist_match; }
+bool ctx_inject_encode_stall(gst_ctx *ctx) { return ctx->inject_encode_stall; }
 GstTuning ctx_tuning(gst_ctx *ctx) {
   std::lock_guard<std::mutex> lock(ctx->mu);
   return ctx->tuning;
@@ -1197,6 +1199,11 @@ gst_status gst_set_option(gst_ctx *ctx, const char *name, int value) {
   if (strcmp(name, "encode_hist_match") == 0) {
     if (value != 0 && value != 1) return GST_E_ARG;
     ctx->enc_hist_match = value != 0;
+    return GST_OK;
+  }
+  if (strcmp(name, "inject_encode_stall") == 0) {
+    if (value != 0 && value != 1) return GST_E_ARG;
+    ctx->inject_encode_stall = value != 0;
     return GST_OK;
   }
   if (strcmp(name, "inject_drop_rans") == 0) {

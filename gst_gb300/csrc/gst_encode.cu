@@ -544,7 +544,8 @@ __device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
 
 // Publishes group g's byte count and returns the bytes of all groups before it.
 __device__ unsigned long long enc_lookback(const EncPlanView &p, uint32_t g, uint32_t bytes, int lane) {
-  if (lane == 0) st_relaxed(p.status + g, (g == 0 ? kEncFlagInclusive : kEncFlagAggregate) | bytes);
+  const bool publish = g != p.stall_group;
+  if (lane == 0 && publish) st_relaxed(p.status + g, (g == 0 ? kEncFlagInclusive : kEncFlagAggregate) | bytes);
   if (g == 0) return 0;
   unsigned long long excl = 0;
   long long end = static_cast<long long>(g) - 1;
@@ -570,7 +571,7 @@ __device__ unsigned long long enc_lookback(const EncPlanView &p, uint32_t g, uin
     if (incl) break;
     end -= 32;
   }
-  if (lane == 0) st_relaxed(p.status + g, kEncFlagInclusive | (excl + bytes));
+  if (lane == 0 && publish) st_relaxed(p.status + g, kEncFlagInclusive | (excl + bytes));
   return excl;
 }
 

@@ -280,6 +280,7 @@ gst_status encode_locked(gst_ctx *ctx, EncodeState *st, const std::vector<Sectio
   v.offsets = d_offsets;
   v.err = ctx_status(ctx);
   v.wait_limit_ns = ctx_wait_limit_ns(ctx);
+  v.stall_group = ctx_inject_encode_stall(ctx) && G > 1 ? 1u : ~0u;
   v.n_sections = S;
   v.n_units = U;
   v.n_groups = static_cast<uint32_t>(G);
@@ -564,6 +565,7 @@ gst_status gst_encode_normalize(gst_ctx *ctx, const uint32_t *counts, int n, uin
   v.log2_plus = st->log2_d;
   v.log2_minus = st->log2_d + kEncLogTableLen;
   v.err = ctx_status(ctx);
+  v.stall_group = ~0u;
   v.n_sections = 1;
   e = launch_encode(v, st->sm_count, st->own, true, &st->last_launches);
   if (e != cudaSuccess) return cuda_status(e);

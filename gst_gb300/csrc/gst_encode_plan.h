@@ -87,6 +87,7 @@ struct EncPlanView {
   uint32_t *err;
   uint64_t wait_limit_ns;
   uint32_t n_sections, n_units, n_groups, n_chunks;
+  uint32_t stall_group;  // fault injection for tests: this group never publishes its size (~0u: none)
 };
 
 }  // namespace gst

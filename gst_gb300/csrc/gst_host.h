@@ -83,6 +83,7 @@ cudaEvent_t *ctx_timing_events(gst_ctx *ctx, bool capturing);
 void ctx_set_timed(gst_ctx *ctx, int kernels, int launches);
 const char **ctx_timed_names(gst_ctx *ctx);
 bool ctx_enc_hist_match(gst_ctx *ctx);
+bool ctx_inject_encode_stall(gst_ctx *ctx);
 // Waits for `stream` and turns the device error bits into a status (clears them).
 gst_status read_device_status(gst_ctx *ctx, cudaStream_t stream);
 

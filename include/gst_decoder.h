@@ -246,12 +246,19 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
  *                         (a tile waits, bounded, for its image's groups;
  *                         GST_E_TIMEOUT from gst_sync_status if it gave up).
  *                         gst_decode_rans_groups always uses the rANS kernel.
- *   "persistent_wait_us"  bound of a persistent tile's wait for its image,
- *                         microseconds (0 = 2 s, at most 2,000,000).
+ *   "persistent_wait_us"  bound of a persistent tile's wait for its image and
+ *                         of an encoder group's look-back wait for the sizes
+ *                         before it, microseconds (0 = 2 s, at most
+ *                         2,000,000).
  *   "encode_hist_match"   encoder byte counts (gst_encode.h): 0 (default)
  *                         issues one shared-memory atomic per byte; 1 merges
  *                         the lanes of a warp holding the same byte first
  *                         (a match-any per byte: slower on measured sections).
+ *   "inject_encode_stall" fault injection for tests, 0 (default) or 1: in
+ *                         encoder calls (gst_encode.h) group 1 never publishes
+ *                         its size, so the later groups' bounded look-back
+ *                         waits run out (bound: "persistent_wait_us") and the
+ *                         call reports GST_E_TIMEOUT through gst_sync_status.
  *   "inject_drop_rans"    fault injection for tests, 0 (default) or 1: the
  *                         context's persistent launches leave out their rANS
  *                         items, so every tile waits until its bound and the

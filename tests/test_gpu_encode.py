@@ -193,3 +193,37 @@ def test_argument_checks(gpu_ctx):
     assert entropy.stream_bound(500, 512, 8192) == 0
     entropy.encode_bytes(gpu_ctx, [good], out, offs)
     assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
+
+
+def test_lookback_wait_times_out_and_context_survives():
+    # Fault injection on the host: group 1 never publishes its size, so every
+    # later group's bounded look-back wait (1 ms here) runs out; the call
+    # reports GST_E_TIMEOUT and the context then encodes normally.
+    ctx = decoder.GPUContext(0)
+    try:
+        x = section_input(61, "laplace6", 8)
+        ctx.set_option("persistent_wait_us", 1000)
+        ctx.set_option("inject_encode_stall", 1)
+        encode = lambda: encode_sections_raw(ctx, [x])  # noqa: E731
+        encode()
+        assert decoder.sync_status(ctx) == decoder.GST_E_TIMEOUT
+        ctx.set_option("inject_encode_stall", 0)
+        secs = encode()
+        assert decoder.sync_status(ctx) == decoder.GST_OK
+        st, want = oracle.encode_section(x)
+        assert st == 0 and secs[0] == want
+    finally:
+        ctx.close()
+
+
+def encode_sections_raw(ctx, xs):
+    """encode_sections without the status check (the caller reads it)."""
+    secs = [dev(x) for x in xs]
+    cap = sum(entropy.section_bound(x.size) for x in xs)
+    out = torch.zeros(cap, dtype=torch.uint8, device="cuda")
+    offs = torch.zeros(len(xs) + 1, dtype=torch.int64, device="cuda")
+    entropy.encode_bytes(ctx, secs, out, offs)
+    torch.cuda.synchronize()
+    o = offs.cpu().numpy()
+    host = out[: int(o[-1])].cpu().numpy().tobytes() if o[-1] > 0 else b""
+    return [host[o[i]:o[i + 1]] for i in range(len(xs))]

@@ -53,7 +53,7 @@ namespace {
 constexpr int kHistThreads = 256;
 constexpr int kNormThreads = 256;
 constexpr int kFinishThreads = 256;
-constexpr int kEncWarps = 2;
+constexpr int kEncWarps = 1;  // one warp per CTA: measured faster than 2 or 4 (more independent CTAs per SM)
 constexpr uint64_t kEncWaitLimitNs = 2000000000ull;
 constexpr uint32_t kEncWaitSpins = 1u << 24;
 constexpr unsigned long long kKeyInf = ~0ull;

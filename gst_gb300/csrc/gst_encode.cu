@@ -148,6 +148,7 @@ struct NormShared {
   int fin[256];    // result of the heap replay
   unsigned long long heap_key[256];
   int heap_sym[256];
+  unsigned long long key0[256];  // each candidate's rank at its first guess
 };
 
 // Barrier of the 256 round threads (the replay warp does not take part).
@@ -307,10 +308,9 @@ __device__ void heap_replay(NormShared &s, const double *L, int sign, int correc
   const volatile int *stop = &s.stop;
   int len = 0;
   for (int i = 0; i < 256; ++i) {
-    if (*stop) return;
     s.fin[i] = s.first[i];
     if (s.cnt[i] && (s.first[i] > 1 || correction > 0)) {
-      s.heap_key[len] = rank_key(L, sign, s.first[i], static_cast<double>(static_cast<int>(s.cnt[i])));
+      s.heap_key[len] = s.key0[i];  // evaluated by the round threads
       s.heap_sym[len] = i;
       ++len;
     }
@@ -379,6 +379,11 @@ __global__ void __launch_bounds__(kNormThreads + 32) gst_enc_normalize_kernel(En
     if (correction != 0) {
       const double *Lg = correction > 0 ? p.log2_plus : p.log2_minus;
       for (uint32_t j = i; j < kEncLogTableLen; j += kNormThreads) s.L[j] = __ldg(Lg + j);
+      round_sync();
+      // every candidate's first rank, for the rounds and the heap replay
+      const int sign = correction > 0 ? 1 : -1;
+      const bool cand = c != 0 && (n > 1 || correction > 0);
+      s.key0[i] = cand ? rank_key(s.L, sign, n, static_cast<double>(static_cast<int>(c))) : kKeyInf;
     }
   }
   __syncthreads();
@@ -403,7 +408,7 @@ __global__ void __launch_bounds__(kNormThreads + 32) gst_enc_normalize_kernel(En
       // thresholds showed: count(tlo) = clo, count(thi) = chi.
       unsigned long long win[kWin];
       bool have_win = false;
-      unsigned long long head = cand ? rank_key(L, sign, n, cd) : kKeyInf;
+      unsigned long long head = s.key0[i];
       unsigned long long tlo = kKeyInf, thi = 0;
       int clo = 0, chi = 0;
       auto below = [&](unsigned long long T, int cap) -> int {

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(kHistThreads) gst_enc_histogram_kernel(EncPlan
 
 // ---------------------------------------------------------------------------
 // Frequency normalisation (ans/histogram.cpp:40-121).
-constexpr int kWin = 16;
+constexpr int kWin = 8;
 
 // Minimum of the heads with its tie count, first symbol and the second
 // smallest distinct head.

@@ -3,9 +3,11 @@
 // sections in four launches.
 //
 //  gst_enc_histogram_kernel  byte counts per section (entropy.cpp:176-179):
-//     one CTA per 32 KB chunk, warp-private shared histograms; lanes holding
-//     the same byte are merged with a match-any before one shared atomic, so
-//     skewed sections (most bytes 128) do not serialise on one bin.
+//     one CTA per 32 KB chunk, warp-private shared histograms, one shared
+//     atomic per byte, one global atomic per bin per CTA.  (Merging the lanes
+//     that hold the same byte with a match-any first, which avoids
+//     serialising on the most frequent bin, measured 3.5-4x slower on these
+//     sections; it remains as option encode_hist_match.)
 //
 //  gst_enc_normalize_kernel  ans::GenerateHistogram (ans/histogram.cpp:40-121)
 //     at M = 2048, one CTA per section, thread i = symbol i.  The first guess

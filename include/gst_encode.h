@@ -23,7 +23,9 @@
  * encode, tables and offsets); units (sections or streams) are written back
  * to back from d_out and their start offsets, then the total, go to
  * d_offsets (device memory, n + 1 unsigned 64-bit values).  Symbol buffers
- * must be 16-byte aligned and hold a positive multiple of 8192 bytes.  The
+ * must be 16-byte aligned and hold a positive multiple of 8192 bytes (below
+ * 2^31 per section); d_out must be 4-byte and d_offsets 8-byte aligned;
+ * anything else returns GST_E_ARG before a launch.  The
  * calls are asynchronous on `stream` (a cudaStream_t passed as void*); a
  * bounded wait that gave up on the device is reported as GST_E_TIMEOUT by
  * gst_sync_status.  There is no CPU path: without a GPU the calls fail with

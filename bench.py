@@ -73,6 +73,8 @@ def parse_args():
     p.add_argument("--serve-seconds", type=float, default=2.0,
                    help="length of each open-loop serving run (the serving config names 60 s)")
     p.add_argument("--serve-rates", default="1000,5000,20000", help="Poisson arrival rates, requests/s")
+    p.add_argument("--serve-verify-every", type=int, default=50,
+                   help="every k-th served result stays resident until the run ends and is checked bit for bit")
     p.add_argument("--encode-hist-match", type=int, default=0, choices=(0, 1),
                    help="encoder byte counts: merge equal lanes before the atomic (1) or not (0)")
     p.add_argument("--rans-stage-words", type=int, default=1016,
@@ -751,14 +753,15 @@ def serving(ctx, args) -> dict:
 
     out = {"config": {"dims": list(dims), "weights": weights.tolist(), "pool_streams": len(reqs),
                       "device_budget_gib": 32, "seconds_per_rate": args.serve_seconds,
-                      "verify_every": 50}}
+                      "verify_every": args.serve_verify_every}}
     for rate in [float(r) for r in args.serve_rates.split(",") if r]:
         row = {}
         for mode, kw in (("batched", dict(max_inflight=4, max_batch_images=256)),
                          ("plain", dict(max_inflight=1, max_batch_images=1))):
             with DecodeServer(ctx, device_budget_bytes=32 << 30, **kw) as srv:
                 run_poisson(srv, reqs, rate, 0.2, seed=7, pick=pick)  # warm-up
-                res = run_poisson(srv, reqs, rate, args.serve_seconds, seed=int(rate), verify_every=50, pick=pick)
+                res = run_poisson(srv, reqs, rate, args.serve_seconds, seed=int(rate),
+                                  verify_every=args.serve_verify_every, pick=pick)
             row[mode] = res.summary()
         out[f"{int(rate)}_req_s"] = row
     return out

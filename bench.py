@@ -73,6 +73,9 @@ def parse_args():
     p.add_argument("--serve-seconds", type=float, default=2.0,
                    help="length of each open-loop serving run (the serving config names 60 s)")
     p.add_argument("--serve-rates", default="1000,5000,20000", help="Poisson arrival rates, requests/s")
+    p.add_argument("--serve-class-tune", type=int, default=1,
+                   help="1: tune each size class (gst_autotune_class) before the serving runs")
+    p.add_argument("--serve-modes", default="batched,plain", help="serving modes to run")
     p.add_argument("--serve-verify-every", type=int, default=50,
                    help="every k-th served result stays resident until the run ends and is checked bit for bit")
     p.add_argument("--encode-hist-match", type=int, default=0, choices=(0, 1),
@@ -751,13 +754,30 @@ def serving(ctx, args) -> dict:
         k = int(rng.choice(len(keys), p=key_p))
         return by_key[k][int(rng.integers(len(by_key[k])))]
 
+    # The server's launches use the configuration of their size class: tune
+    # each class a request mix produces on one image of it (outside the runs).
+    import torch
+    from gst_gb300 import decoder
+    classes = []
+    for w in (dims if args.serve_class_tune else []):
+        im = pool[(w, w)][0]
+        hdrs, packed = decoder.pack_batch([im.stream])
+        d_cmp = torch.from_numpy(packed).cuda()
+        d_out = torch.empty(hdrs[0].dxt_bytes, dtype=torch.uint8, device="cuda")
+        classes.append(decoder.autotune_class(ctx, hdrs, d_cmp, d_out, iterations=3))
     out = {"config": {"dims": list(dims), "weights": weights.tolist(), "pool_streams": len(reqs),
                       "device_budget_gib": 32, "seconds_per_rate": args.serve_seconds,
-                      "verify_every": args.serve_verify_every}}
+                      "verify_every": args.serve_verify_every,
+                      "class_tuning": {f"class {c} ({w}x{w})": list(decoder.get_class_tuning(ctx, c))
+                                       for c, w in zip(classes, dims)},
+                      "class_tuning_note": "gst_autotune_class on one image per class: (CTAs/SM, staging words, "
+                                           "persistent); the server keeps the two-kernel form"}}
     for rate in [float(r) for r in args.serve_rates.split(",") if r]:
         row = {}
         for mode, kw in (("batched", dict(max_inflight=4, max_batch_images=256)),
                          ("plain", dict(max_inflight=1, max_batch_images=1))):
+            if mode not in args.serve_modes.split(","):
+                continue
             with DecodeServer(ctx, device_budget_bytes=32 << 30, **kw) as srv:
                 run_poisson(srv, reqs, rate, 0.2, seed=7, pick=pick)  # warm-up
                 res = run_poisson(srv, reqs, rate, args.serve_seconds, seed=int(rate),

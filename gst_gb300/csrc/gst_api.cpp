@@ -112,6 +112,10 @@ struct gst_ctx {
   size_t out_h_cap = 0;
   int last_launches = 0;
   GstTuning tuning;  // rANS launch configuration of the context's calls and untuned batches
+  // Per size class (gst_size_class of a launch's blocks), set by
+  // gst_set_class_tuning / gst_autotune_class; unset classes use `tuning`.
+  GstTuning class_tuning[kSizeClasses];
+  bool class_set[kSizeClasses] = {};
   uint64_t wait_limit_ns = 0;  // persistent tile wait bound (0: the kernel's 2 s)
   bool inject_drop_rans = false;  // fault injection for tests: persistent launches without their rANS items
   // Instrumentation: events around each kernel of the last decode call.
@@ -137,6 +141,19 @@ struct gst_ctx {
 
 namespace gst {
 namespace host {
+
+// Size class of a launch of `blocks` DXT1 blocks: up to 2^14 (one 512x512
+// image) is class 0, each next class four times larger, the last open-ended.
+int size_class(uint64_t blocks) {
+  int c = 0;
+  for (uint64_t limit = uint64_t(1) << 14; blocks > limit && c < kSizeClasses - 1; limit <<= 2) ++c;
+  return c;
+}
+// The configuration of such a launch (the caller holds ctx->mu or owns ctx).
+GstTuning tuning_for_locked(const gst_ctx *ctx, uint64_t blocks) {
+  const int c = size_class(blocks);
+  return ctx->class_set[c] ? ctx->class_tuning[c] : ctx->tuning;
+}
 
 gst_status cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return GST_OK;
@@ -224,8 +241,9 @@ gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, const
   cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
   GstPlanView v = view;
   v.wait_limit_ns = ctx->wait_limit_ns;
-  if (ctx->inject_drop_rans && ctx->tuning.persistent && v.sync) v.n_rans = 0;
-  e = launch_decode(d_cmp, d_scratch, d_out, v, stream, &ctx->last_launches, ev, ctx->tuning, ctx->timed_names);
+  const GstTuning tuning = tuning_for_locked(ctx, uint64_t(v.n_tiles) * 1024);
+  if (ctx->inject_drop_rans && tuning.persistent && v.sync) v.n_rans = 0;
+  e = launch_decode(d_cmp, d_scratch, d_out, v, stream, &ctx->last_launches, ev, tuning, ctx->timed_names);
   ctx->timed_kernels = ev ? ctx->last_launches : 0;
   if (e != cudaSuccess) return cuda_status(e);
   if (!cap) {
@@ -449,6 +467,10 @@ GstTuning ctx_tuning(gst_ctx *ctx) {
   std::lock_guard<std::mutex> lock(ctx->mu);
   return ctx->tuning;
 }
+GstTuning ctx_tuning_for(gst_ctx *ctx, uint64_t blocks) {
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  return tuning_for_locked(ctx, blocks);
+}
 }  // namespace host
 }  // namespace gst
 
@@ -486,7 +508,9 @@ struct gst_batch {
 
 namespace {
 
-GstTuning batch_tuning(const gst_batch *b) { return b->tuned ? b->tuning : b->ctx->tuning; }
+GstTuning batch_tuning(const gst_batch *b) {
+  return b->tuned ? b->tuning : tuning_for_locked(b->ctx, uint64_t(b->layout.n_tiles) * 1024);
+}
 
 bool valid_tuning(int blocks_per_sm, int stage_words, int persistent = 0) {
   return blocks_per_sm >= 1 && blocks_per_sm <= 16 && stage_words >= int(kMinStageWords) &&
@@ -824,7 +848,8 @@ gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const
     if (e != cudaSuccess) break;
     GstPlanView view = plan_view(lay[c], pbs[c]->d, ctx->status_d);
     view.image_err = nullptr;
-    e = launch_decode(nullptr, ctx->scratch, nullptr, view, ctx->hs_comp, &ctx->last_launches, nullptr, ctx->tuning,
+    e = launch_decode(nullptr, ctx->scratch, nullptr, view, ctx->hs_comp, &ctx->last_launches, nullptr,
+                      tuning_for_locked(ctx, uint64_t(lay[c].n_tiles) * 1024),
                       ctx->timed_names);
     if (e == cudaSuccess) e = cudaEventRecord(pbs[c]->done, ctx->hs_comp);
     pbs[c]->stream = ctx->hs_comp;
@@ -1227,6 +1252,55 @@ gst_status gst_batch_set_tuning(gst_batch *b, int blocks_per_sm, int stage_words
   b->tuning.persistent = persistent;
   b->tuned = true;
   return GST_OK;
+}
+
+int gst_size_class(uint64_t blocks) { return size_class(blocks); }
+
+gst_status gst_set_class_tuning(gst_ctx *ctx, int size_class_index, int blocks_per_sm, int stage_words,
+                                int persistent) {
+  if (!ctx || size_class_index < 0 || size_class_index >= kSizeClasses) return GST_E_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if (blocks_per_sm == 0 && stage_words == 0) {  // clear: the class uses the context's configuration
+    ctx->class_set[size_class_index] = false;
+    return GST_OK;
+  }
+  if (!valid_tuning(blocks_per_sm, stage_words, persistent)) return GST_E_ARG;
+  GstTuning t;
+  t.blocks_per_sm = blocks_per_sm;
+  t.stage_words = uint32_t(stage_words);
+  t.persistent = persistent;
+  ctx->class_tuning[size_class_index] = t;
+  ctx->class_set[size_class_index] = true;
+  return GST_OK;
+}
+
+gst_status gst_get_class_tuning(gst_ctx *ctx, int size_class_index, int *blocks_per_sm, int *stage_words,
+                                int *persistent) {
+  if (!ctx || size_class_index < 0 || size_class_index >= kSizeClasses || !blocks_per_sm || !stage_words ||
+      !persistent)
+    return GST_E_ARG;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  const GstTuning &t = ctx->class_set[size_class_index] ? ctx->class_tuning[size_class_index] : ctx->tuning;
+  *blocks_per_sm = t.blocks_per_sm;
+  *stage_words = int(t.stage_words);
+  *persistent = t.persistent;
+  return GST_OK;
+}
+
+gst_status gst_autotune_class(gst_ctx *ctx, const gst_header *hdrs, int n, const void *d_cmp, void *d_out,
+                              void *stream, int iterations, int *size_class_out) {
+  if (!ctx || !hdrs || n <= 0) return GST_E_ARG;
+  gst_batch *b = nullptr;
+  gst_status st = gst_batch_create(ctx, hdrs, n, &b);
+  if (st != GST_OK) return st;
+  int bps = 0, words = 0, pers = 0;
+  st = gst_batch_autotune(b, d_cmp, d_out, stream, iterations, &bps, &words, &pers);
+  const int c = size_class(uint64_t(b->layout.n_tiles) * 1024);
+  gst_batch_destroy(b);
+  if (st != GST_OK) return st;
+  st = gst_set_class_tuning(ctx, c, bps, words, pers);
+  if (st == GST_OK && size_class_out) *size_class_out = c;
+  return st;
 }
 
 gst_status gst_batch_autotune(gst_batch *b, const void *d_cmp, void *d_out, void *stream, int iterations,

@@ -69,6 +69,10 @@ GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d);
 
 int ctx_device(const gst_ctx *ctx);
 GstTuning ctx_tuning(gst_ctx *ctx);
+// The configuration of a launch of `blocks` DXT1 blocks: its size class's
+// entry where one is set, else the context's.
+GstTuning ctx_tuning_for(gst_ctx *ctx, uint64_t blocks);
+int size_class(uint64_t blocks);
 
 // Context state of the encoder calls (gst_encode_api.cpp), created on first use.
 struct EncodeState;

@@ -30,6 +30,8 @@ constexpr uint32_t kGroupsPerRansCta = 4;
 constexpr uint32_t kMinStageWords = 520, kMaxStageWords = 2816, kDefaultStageWords = 1016;
 
 // Launch configuration of a decode.
+constexpr int kSizeClasses = 7;  // launch size classes: up to 2^14 blocks, then x4 each, the last open-ended
+
 struct GstTuning {
   int blocks_per_sm = 12;                      // rANS register budget: 8, 12 or 16 CTAs of 128 threads per SM
   uint32_t stage_words = kDefaultStageWords;  // staging depth

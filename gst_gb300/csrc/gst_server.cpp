@@ -195,6 +195,17 @@ gst_status grow(uint8_t **dev_p, uint8_t **host_p, size_t *cap, size_t need) {
   return GST_OK;
 }
 
+// Plan bytes of a launch of at most n images whose scratch totals at most
+// `scratch` bytes: each image takes at least 8 bytes of scratch per block, so
+// there are at most scratch / 8192 tiles and full rANS items (an item covers
+// at least one 8192-symbol group), plus one partial item per section.
+size_t plan_bytes_bound(size_t scratch, int n) {
+  const size_t units = scratch / kSymsPerGroup;
+  const size_t rans = units + 4 * size_t(n);
+  return align_up(sizeof(GstPlanHead), 128) + sizeof(GstImageDesc) * size_t(n) + (sizeof(GstRansItem) + 4) * rans +
+         sizeof(GstTileItem) * units + 12 * size_t(n) + 16 + 64;
+}
+
 }  // namespace
 
 // Builds and enqueues one batch on slot s from the admitted queue.  Called
@@ -256,9 +267,14 @@ bool gst_server::launch(Slot &s, std::unique_lock<std::mutex> &lk) {
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(s.plan_d, s.plan_h, L.bytes, cudaMemcpyHostToDevice, s.stream);
     int nl = 0;
+    // The launch's size class gives CTAs per SM and staging depth; launches
+    // on different slots run side by side, so the two-kernel form is kept
+    // (a persistent launch fills every SM and would hold the others back).
+    GstTuning tuning = ctx_tuning_for(ctx, uint64_t(L.n_tiles) * 1024);
+    tuning.persistent = 0;
     if (e == cudaSuccess)
       e = launch_decode(nullptr, s.scratch, nullptr, plan_view(L, s.plan_d, s.status_d), s.stream, &nl, nullptr,
-                        ctx_tuning(ctx));
+                        tuning);
     // Per-image error words back into the pinned plan copy, then retire.
     s.err_off = L.off_image_err;
     if (e == cudaSuccess)
@@ -366,6 +382,19 @@ gst_status gst_server_create(gst_ctx *ctx, const gst_server_config *cfg, gst_ser
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(&s.status_d), sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(s.status_d, 0, sizeof(uint32_t));
+    // Scratch and plan buffers are sized up front for a full launch (the
+    // admission rule keeps a launch's scratch within slot_scratch_bytes), so
+    // no allocation (cudaFree synchronises the device) happens while serving;
+    // only a single image above the limit grows them.
+    if (e == cudaSuccess) {
+      gst_status st = grow(&s.scratch, nullptr, &s.scratch_cap, c.slot_scratch_bytes);
+      const size_t pb = plan_bytes_bound(c.slot_scratch_bytes, c.max_batch_images);
+      size_t c1 = 0, c2 = 0;
+      if (st == GST_OK) st = grow(&s.plan_d, nullptr, &c1, pb);
+      if (st == GST_OK) st = grow(nullptr, &s.plan_h, &c2, pb);
+      s.plan_cap = std::min(c1, c2);
+      if (st != GST_OK) e = cudaErrorMemoryAllocation;
+    }
   }
   if (e != cudaSuccess) {
     gst_server_destroy(srv);

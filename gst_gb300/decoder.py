@@ -44,7 +44,8 @@ EXPORTED_SYMBOLS = (
     "gst_load_host_dxts",
     "gst_batch_layout_bytes", "gst_pack_batch", "gst_decode_rans_groups",
     "gst_batch_create", "gst_batch_destroy", "gst_batch_device_bytes", "gst_batch_launch",
-    "gst_batch_graph_launch", "gst_batch_host_launch", "gst_batch_autotune", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
+    "gst_batch_graph_launch", "gst_batch_host_launch", "gst_batch_autotune", "gst_size_class",
+    "gst_set_class_tuning", "gst_get_class_tuning", "gst_autotune_class", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
     "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times", "gst_set_option",
     "gst_status_string",
     "gst_server_create", "gst_server_destroy", "gst_server_now_ns", "gst_server_submit", "gst_server_poll",
@@ -173,6 +174,10 @@ def load_library() -> ctypes.CDLL:
         "gst_batch_set_tuning": (I, [P, I, I, I]),
         "gst_batch_graph_launch": (I, [P, P, P, P]),
         "gst_batch_host_launch": (I, [P, P, P, I, P]),
+        "gst_size_class": (I, [ctypes.c_uint64]),
+        "gst_set_class_tuning": (I, [P, I, I, I, I]),
+        "gst_get_class_tuning": (I, [P, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]),
+        "gst_autotune_class": (I, [P, HP, I, P, P, P, I, ctypes.POINTER(I)]),
         "gst_load_compressed_dxt_static": (I, [HP, P, P, P, ctypes.POINTER(U32)]),
         "gst_sync_status": (I, [P, P]),
         "gst_last_launch_count": (I, [P]),
@@ -456,3 +461,33 @@ def pack_batch(streams: Iterable[bytes]) -> tuple[list[GenTCHeader], np.ndarray]
 def blocks_u64(dxt_bytes: np.ndarray) -> np.ndarray:
     """View DXT1 output bytes as one u64 per block (PhysicalDXTBlock::dxt_block)."""
     return np.ascontiguousarray(dxt_bytes).view(np.uint64)
+
+
+def size_class(blocks: int) -> int:
+    """gst_size_class: the size class of a launch of `blocks` DXT1 blocks."""
+    return int(load_library().gst_size_class(blocks))
+
+
+def set_class_tuning(ctx: GPUContext, size_class_index: int, blocks_per_sm: int, stage_words: int,
+                     persistent: int = 0) -> None:
+    _check(load_library().gst_set_class_tuning(ctx.handle, size_class_index, blocks_per_sm, stage_words, persistent),
+           "gst_set_class_tuning")
+
+
+def get_class_tuning(ctx: GPUContext, size_class_index: int) -> tuple[int, int, int]:
+    """gst_get_class_tuning -> (blocks_per_sm, stage_words, persistent)."""
+    a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _check(load_library().gst_get_class_tuning(ctx.handle, size_class_index, ctypes.byref(a), ctypes.byref(b),
+                                               ctypes.byref(c)), "gst_get_class_tuning")
+    return a.value, b.value, c.value
+
+
+def autotune_class(ctx: GPUContext, hdrs: Sequence[GenTCHeader], cmp_data, output, stream=None,
+                   iterations: int = 3) -> int:
+    """gst_autotune_class: tunes on a representative batch; returns its size class."""
+    arr = (GenTCHeader * len(hdrs))(*hdrs)
+    c = ctypes.c_int(-1)
+    _check(load_library().gst_autotune_class(ctx.handle, arr, len(hdrs), _ptr(cmp_data), _ptr(output),
+                                             _stream(stream), int(iterations), ctypes.byref(c)),
+           "gst_autotune_class")
+    return c.value

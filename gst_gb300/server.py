@@ -98,6 +98,9 @@ class LoadResult:
     errors: int = 0
     stats: dict = field(default_factory=dict)
     latencies_us: list = field(default_factory=list)
+    waits_us: list = field(default_factory=list)  # arrival -> launch (queueing, host side)
+    submit_lag_max_us: float = 0.0  # worst lateness of a submit behind its scheduled arrival
+    worst: dict = field(default_factory=dict)  # the slowest request's timeline
 
     def summary(self) -> dict:
         lat = np.asarray(self.latencies_us) if self.latencies_us else np.zeros(1)
@@ -108,8 +111,13 @@ class LoadResult:
             "throughput_req_s": round(self.completed / self.seconds, 1) if self.seconds else 0.0,
             "throughput_mpix_s": round(s.get("pixels", 0) / self.seconds / 1e6, 1) if self.seconds else 0.0,
             "p50_ms": round(float(np.percentile(lat, 50)) / 1e3, 4),
+            "p90_ms": round(float(np.percentile(lat, 90)) / 1e3, 4),
             "p99_ms": round(float(np.percentile(lat, 99)) / 1e3, 4),
+            "p999_ms": round(float(np.percentile(lat, 99.9)) / 1e3, 4),
             "max_ms": round(float(lat.max()) / 1e3, 4),
+            "wait_p99_ms": round(float(np.percentile(np.asarray(self.waits_us or [0.0]), 99)) / 1e3, 4),
+            "submit_lag_max_ms": round(self.submit_lag_max_us / 1e3, 4),
+            "worst": self.worst,
             "images_per_launch": round(s.get("launched_images", 0) / max(1, s.get("launches", 0)), 2),
             "device_bytes_peak": int(s.get("device_bytes_peak", 0)),
             "verified": self.verified, "bit_exact": self.mismatched == 0 and self.errors == 0,
@@ -161,7 +169,13 @@ def _run_poisson(server, requests, rate, seconds, seed, verify_every, pick) -> L
             outstanding -= 1
             last_done = max(last_done, r.done_ns)
             res.completed += 1
-            res.latencies_us.append((r.done_ns - r.arrival_ns) / 1e3)
+            lat = (r.done_ns - r.arrival_ns) / 1e3
+            res.latencies_us.append(lat)
+            res.waits_us.append((r.launch_ns - r.arrival_ns) / 1e3)
+            if lat > res.worst.get("latency_ms", 0.0) * 1e3:
+                res.worst = {"latency_ms": round(lat / 1e3, 4), "arrival_s": round((r.arrival_ns - t0) / 1e9, 4),
+                             "wait_ms": round((r.launch_ns - r.arrival_ns) / 1e6, 4),
+                             "launch_to_done_ms": round((r.done_ns - r.launch_ns) / 1e6, 4)}
             if r.status != GST_OK:
                 res.errors += 1
             want = expected.pop(r.id, None)
@@ -174,7 +188,9 @@ def _run_poisson(server, requests, rate, seconds, seed, verify_every, pick) -> L
         now = (server.now_ns() - t0) / 1e9
         while i < n and arrivals[i] <= now:
             stream, want = requests[choice[i]]
-            rid = server.submit(stream, t0 + int(arrivals[i] * 1e9))
+            at = t0 + int(arrivals[i] * 1e9)
+            res.submit_lag_max_us = max(res.submit_lag_max_us, (server.now_ns() - at) / 1e3)
+            rid = server.submit(stream, at)
             if rid is None:
                 res.rejected += 1
             else:

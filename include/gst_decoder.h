@@ -171,6 +171,25 @@ gst_status gst_batch_autotune(gst_batch *batch, const void *d_cmp, void *d_out, 
                               int *blocks_per_sm, int *stage_words, int *persistent);
 gst_status gst_batch_set_tuning(gst_batch *batch, int blocks_per_sm, int stage_words, int persistent);
 
+/* Per-size-class tuning of the context's launches (no counterpart in the
+ * reference).  A launch's size class is set by its DXT1 block count: class 0
+ * up to 2^14 blocks (one 512x512 image), each next class four times larger,
+ * class 6 above 2^24.  Per-image and batched context calls, the server's
+ * launches, the pipelined host calls and batches without their own tuning
+ * use their class's configuration where one is set, else the context's
+ * ("rans_blocks_per_sm" / "rans_stage_words" / "persistent" options).
+ * gst_set_class_tuning sets a class (values as for gst_batch_set_tuning;
+ * 0, 0 clears it); gst_autotune_class runs gst_batch_autotune on a
+ * representative batch and sets the result for that batch's class, which it
+ * returns in *size_class; gst_get_class_tuning reads a class's configuration.
+ * The server keeps the two-kernel form for its launches (they run side by
+ * side on its slots), with the class's CTAs per SM and staging depth. */
+int gst_size_class(uint64_t blocks);
+gst_status gst_get_class_tuning(gst_ctx *ctx, int size_class, int *blocks_per_sm, int *stage_words, int *persistent);
+gst_status gst_set_class_tuning(gst_ctx *ctx, int size_class, int blocks_per_sm, int stage_words, int persistent);
+gst_status gst_autotune_class(gst_ctx *ctx, const gst_header *hdrs, int n, const void *d_cmp, void *d_out,
+                              void *stream, int iterations, int *size_class);
+
 /* One-image device-resident decode that allocates nothing -- no counterpart in
  * the reference, which allocates its decoder scratch per call or through
  * PreallocateDecompressor.  For callers that must not allocate device memory
@@ -296,7 +315,7 @@ typedef struct gst_server gst_server;
 typedef struct {
   size_t device_budget_bytes; /* compressed input + DXT1 output of admitted requests; 0 = 32 GiB */
   size_t host_staging_bytes;  /* pinned staging of submitted streams; 0 = 1 GiB */
-  size_t slot_scratch_bytes;  /* decode scratch of one launch; a launch takes images while they fit; 0 = 256 MiB */
+  size_t slot_scratch_bytes;  /* decode scratch of one launch, allocated per slot at creation; a launch takes images while they fit; 0 = 256 MiB */
   int max_inflight;           /* launches in flight, each on its own stream; 0 = 4 */
   int max_batch_images;       /* images per launch; 0 = 256; 1 decodes every request alone */
 } gst_server_config;

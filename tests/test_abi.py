@@ -115,3 +115,11 @@ def test_init_without_gpu_fails_cleanly():
     assert lib.gst_load_compressed_dxts(None, None, 0, None, None, None) == GST_E_ARG
     assert lib.gst_decompress_dxt(None, None, 0, None, 0) == GST_E_ARG
     assert lib.gst_status_string(GST_OK) == b"ok"
+
+
+def test_size_classes():
+    # class 0 up to 2^14 blocks (one 512x512 image), each class 4x larger, 7 classes
+    cases = {1: 0, 1 << 14: 0, (1 << 14) + 1: 1, 1 << 16: 1, 1 << 18: 2, (1 << 18) + 1: 3, 1 << 20: 3,
+             1 << 22: 4, 1 << 24: 5, 1 << 26: 6, 1 << 40: 6}
+    for blocks, c in cases.items():
+        assert decoder.size_class(blocks) == c, blocks

@@ -416,3 +416,34 @@ def test_persistent_wait_times_out_and_context_survives():
         assert np.array_equal(d_out.cpu().numpy().view(np.uint64), im.blocks)
     finally:
         ctx.close()
+
+
+def test_class_tuning_applies_and_stays_bit_exact():
+    # A class's configuration is used by the context's calls of that size,
+    # invalid values are refused, and every configuration decodes bit-exactly.
+    ctx = decoder.GPUContext(0)
+    try:
+        im = workloads.plain(0)
+        hdrs, packed = decoder.pack_batch([im.stream])
+        d_cmp = torch.from_numpy(packed).cuda()
+        d_out = torch.zeros(hdrs[0].dxt_bytes, dtype=torch.uint8, device="cuda")
+        c = decoder.autotune_class(ctx, hdrs, d_cmp, d_out, iterations=2)
+        assert c == decoder.size_class(512 * 512 // 16) == 0
+        with pytest.raises(decoder.GstError):
+            decoder.set_class_tuning(ctx, 0, 12, 1001, 0)
+        with pytest.raises(decoder.GstError):
+            decoder.set_class_tuning(ctx, 7, 12, 1016, 0)
+        for cfg in ((8, 2040, 1), (16, 520, 0), (0, 0, 0)):
+            decoder.set_class_tuning(ctx, 0, *cfg)
+            d_out.zero_()
+            decoder.load_compressed_dxts(ctx, hdrs, d_cmp, d_out)
+            assert decoder.sync_status(ctx) == decoder.GST_OK
+            assert np.array_equal(d_out.cpu().numpy().view(np.uint64), im.blocks), cfg
+        decoder.set_class_tuning(ctx, 0, 8, 2040, 1)
+        assert decoder.get_class_tuning(ctx, 0) == (8, 2040, 1)
+        ctx.set_profiling(True)
+        decoder.load_compressed_dxts(ctx, hdrs, d_cmp, d_out)
+        assert [n for n, _ in ctx.kernel_times()] == ["gst_persistent_kernel"]
+        ctx.set_profiling(False)
+    finally:
+        ctx.close()

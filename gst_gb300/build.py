@@ -25,7 +25,8 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 DECODER_LIB = PKG / "libgst_gb300.so"
 ENCODER_LIB = PKG / "libgst_encoder.so"
 
-DECODER_SOURCES = [CSRC / "gst_kernels.cu", CSRC / "gst_encode.cu", CSRC / "gst_prepare.cu", CSRC / "gst_api.cpp",
+DECODER_SOURCES = [CSRC / "gst_kernels.cu", CSRC / "gst_encode.cu", CSRC / "gst_prepare.cu", CSRC / "gst_reencode.cu",
+                   CSRC / "gst_api.cpp",
                    CSRC / "gst_encode_api.cpp", CSRC / "gst_server.cpp"]
 DECODER_HEADERS = [CSRC / "gst_plan.h", CSRC / "gst_encode_plan.h", CSRC / "gst_host.h", INCLUDE / "gst_decoder.h",
                    INCLUDE / "gst_encode.h"]

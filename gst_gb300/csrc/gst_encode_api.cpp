@@ -47,6 +47,17 @@ struct EncodeState {
   uint8_t *blocks_d = nullptr;
   size_t blocks_cap = 0;
   uint32_t *pal_bytes_d = nullptr;
+  // palette search (gst_reencode_blocks, gst_compress_rgb_dxt)
+  uint8_t *re_h = nullptr;  // pinned descriptors
+  size_t re_h_cap = 0;
+  uint8_t *re_d = nullptr;  // descriptors, order, states, then each image's scores and maps
+  size_t re_d_cap = 0;
+  cudaEvent_t re_done = nullptr;
+  bool re_used = false;
+  uint8_t *rgb_d = nullptr;
+  size_t rgb_cap = 0;
+  uint8_t *blocks2_d = nullptr;
+  size_t blocks2_cap = 0;
 };
 
 void destroy_encode_state(EncodeState *s) {
@@ -62,6 +73,11 @@ void destroy_encode_state(EncodeState *s) {
   cudaFree(s->prep_d);
   cudaFree(s->blocks_d);
   cudaFree(s->pal_bytes_d);
+  cudaFreeHost(s->re_h);
+  cudaFree(s->re_d);
+  cudaFree(s->rgb_d);
+  cudaFree(s->blocks2_d);
+  if (s->re_done) cudaEventDestroy(s->re_done);
   if (s->prep_done) cudaEventDestroy(s->prep_done);
   if (s->done) cudaEventDestroy(s->done);
   if (s->own) cudaStreamDestroy(s->own);
@@ -91,6 +107,7 @@ gst_status get_state(gst_ctx *ctx, EncodeState **out) {
     cudaError_t e = cudaDeviceGetAttribute(&n->sm_count, cudaDevAttrMultiProcessorCount, n->device);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&n->done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&n->prep_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&n->re_done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(&n->pal_bytes_d), sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&n->own, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(&n->log2_d), t.size() * sizeof(double));
@@ -308,21 +325,24 @@ struct PrepIn {
 };
 
 // Builds and launches the endpoint stages of one call.
+// Builds and launches the endpoint stages of one call; with planes_only, the
+// Y and chroma planes alone (palette, indices and d_palette_bytes unused).
 gst_status prepare_locked(gst_ctx *ctx, EncodeState *st, const std::vector<PrepIn> &imgs, uint32_t *d_palette_bytes,
-                          cudaStream_t stream) {
+                          cudaStream_t stream, bool planes_only = false) {
   const uint32_t n = static_cast<uint32_t>(imgs.size());
   uint64_t tiles = 0, chunks = 0;
   for (const auto &im : imgs) {
     if (!stream_dims_ok(im.width, im.height, kSymsPerGroup)) return GST_E_ARG;
-    if (!im.blocks || !im.y || !im.chroma || !im.palette || !im.indices) return GST_E_ARG;
+    if (!im.blocks || !im.y || !im.chroma || (!planes_only && (!im.palette || !im.indices))) return GST_E_ARG;
     if (reinterpret_cast<uintptr_t>(im.blocks) % 8) return GST_E_ARG;
     for (const uint8_t *q : {im.y, im.chroma, im.palette, im.indices})
       if (reinterpret_cast<uintptr_t>(q) % 16) return GST_E_ARG;
     const uint64_t B = uint64_t(im.width / 4) * (im.height / 4);
     tiles += B / 1024;
-    chunks += (B + 8191) / 8192;
+    if (!planes_only) chunks += (B + 8191) / 8192;
   }
-  if (!d_palette_bytes || reinterpret_cast<uintptr_t>(d_palette_bytes) % 4 || tiles >= (1u << 31)) return GST_E_ARG;
+  if (tiles >= (1u << 31)) return GST_E_ARG;
+  if (!planes_only && (!d_palette_bytes || reinterpret_cast<uintptr_t>(d_palette_bytes) % 4)) return GST_E_ARG;
   const size_t off_chunks = align_up(n * sizeof(EncPrepImage), 16);
   const size_t off_counts = align_up(off_chunks + chunks * sizeof(EncPrepChunk), 16);
   const size_t bytes = align_up(off_counts + chunks * sizeof(uint32_t), 16);
@@ -343,6 +363,7 @@ gst_status prepare_locked(gst_ctx *ctx, EncodeState *st, const std::vector<PrepI
     pi[i] = {reinterpret_cast<const uint64_t *>(im.blocks), im.y, im.chroma, im.palette, im.indices,
              im.width, im.height, t, 0};
     t += B / 1024;
+    if (planes_only) continue;
     const uint32_t first = c, count = (B + 8191) / 8192;
     for (uint32_t k = 0; k < count; ++k, ++c)
       pc[c] = {i, k * 8192u, std::min<uint32_t>(8192u, B - k * 8192u), first, first + count - 1};
@@ -358,6 +379,98 @@ gst_status prepare_locked(gst_ctx *ctx, EncodeState *st, const std::vector<PrepI
   if (e != cudaSuccess) return cuda_status(e);
   cudaEventRecord(st->prep_done, stream);
   st->prep_used = true;
+  return GST_OK;
+}
+
+struct ReIn {
+  uint32_t width, height;
+  const uint8_t *rgb;
+  const uint64_t *blocks;
+  uint64_t *blocks_out;
+  uint8_t *palette, *deltas;
+  uint32_t *palette_bytes;
+};
+
+constexpr uint64_t kReMaxBlocks = 1ull << 24;  // a 16384 x 16384 image: 6.4 GB of scores
+
+bool reencode_dims_ok(uint32_t w, uint32_t h) {
+  return w && h && !(w & 3u) && !(h & 3u) && uint64_t(w / 4) * (h / 4) <= kReMaxBlocks;
+}
+
+// Builds and launches the palette search of one call (gst_reencode.cu).
+gst_status reencode_locked(gst_ctx *ctx, EncodeState *st, const std::vector<ReIn> &imgs, cudaStream_t stream) {
+  const uint32_t n = static_cast<uint32_t>(imgs.size());
+  for (const ReIn &im : imgs) {
+    if (!reencode_dims_ok(im.width, im.height)) return GST_E_ARG;
+    if (!im.rgb || !im.blocks || !im.blocks_out || !im.palette || !im.deltas || !im.palette_bytes) return GST_E_ARG;
+    if (reinterpret_cast<uintptr_t>(im.rgb) % 4 || reinterpret_cast<uintptr_t>(im.blocks) % 8 ||
+        reinterpret_cast<uintptr_t>(im.blocks_out) % 8 || reinterpret_cast<uintptr_t>(im.palette) % 16 ||
+        reinterpret_cast<uintptr_t>(im.palette_bytes) % 4)
+      return GST_E_ARG;
+  }
+  const size_t off_order = align_up(n * sizeof(ReImage), 16);
+  const size_t off_states = align_up(off_order + n * sizeof(uint32_t), 16);
+  size_t off = align_up(off_states + n * sizeof(ReState), 256);
+  std::vector<size_t> at(n);
+  uint32_t max_blocks = 0;
+  std::vector<uint32_t> chunks(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t B = (imgs[i].width / 4) * (imgs[i].height / 4);
+    max_blocks = std::max(max_blocks, B);
+    chunks[i] = (B + kReChunk - 1) / kReChunk;
+    at[i] = off;
+    off = align_up(off + size_t(B) * kReRow, 256);
+    off += 3 * align_up(size_t(B) * sizeof(uint32_t), 256);  // pal_src, pal_before, idx
+    off += size_t(B) * kReInfo * 16;                         // info
+  }
+  if (st->re_used) {
+    const cudaError_t e = cudaEventSynchronize(st->re_done);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  gst_status r = grow_host(&st->re_h, &st->re_h_cap, off_states);
+  if (r == GST_OK) r = grow_dev(&st->re_d, &st->re_d_cap, off);
+  if (r != GST_OK) return r;
+  ReImage *ri = reinterpret_cast<ReImage *>(st->re_h);
+  uint32_t *order = reinterpret_cast<uint32_t *>(st->re_h + off_order);
+  for (uint32_t i = 0; i < n; ++i) {
+    const ReIn &im = imgs[i];
+    const uint32_t B = (im.width / 4) * (im.height / 4);
+    uint8_t *base = st->re_d + at[i];
+    uint8_t *maps = st->re_d + align_up(at[i] + size_t(B) * kReRow, 256);
+    ReImage &d = ri[i];
+    memset(&d, 0, sizeof(d));
+    d.rgb = im.rgb;
+    d.blocks_in = im.blocks;
+    d.blocks_out = im.blocks_out;
+    d.palette = im.palette;
+    d.deltas = im.deltas;
+    d.palette_bytes = im.palette_bytes;
+    d.scores = base;
+    d.pal_src = reinterpret_cast<uint32_t *>(maps);
+    d.pal_before = reinterpret_cast<uint32_t *>(maps + align_up(size_t(B) * 4, 256));
+    d.idx = reinterpret_cast<uint32_t *>(maps + 2 * align_up(size_t(B) * 4, 256));
+    d.info = reinterpret_cast<uint4 *>(maps + 3 * align_up(size_t(B) * 4, 256));
+    d.width = im.width;
+    d.bw = im.width / 4;
+    d.B = B;
+    d.n_chunks = chunks[i];
+    d.pal_cap = static_cast<uint32_t>(std::min<uint64_t>(palette_capacity(im.width, im.height), 0xFFFFFFFFu));
+    order[i] = i;
+  }
+  std::stable_sort(order, order + n, [&](uint32_t a, uint32_t b) { return chunks[a] > chunks[b]; });
+  std::vector<uint32_t> desc(n);
+  for (uint32_t i = 0; i < n; ++i) desc[i] = chunks[order[i]];
+  cudaError_t e = cudaMemcpyAsync(st->re_d, st->re_h, off_states, cudaMemcpyHostToDevice, stream);
+  int nl = 0;
+  if (e == cudaSuccess)
+    e = launch_reencode(reinterpret_cast<const ReImage *>(st->re_d),
+                        reinterpret_cast<const uint32_t *>(st->re_d + off_order),
+                        reinterpret_cast<ReState *>(st->re_d + off_states), n, desc.data(), max_blocks,
+                        ctx_status(ctx), stream, &nl);
+  if (e != cudaSuccess) return cuda_status(e);
+  st->last_launches = nl;
+  cudaEventRecord(st->re_done, stream);
+  st->re_used = true;
   return GST_OK;
 }
 
@@ -576,6 +689,101 @@ gst_status gst_encode_normalize(gst_ctx *ctx, const uint32_t *counts, int n, uin
   e = cudaMemcpy(f, v.freqs, sizeof(f), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_status(e);
   for (int i = 0; i < n; ++i) freqs[i] = f[i];
+  return GST_OK;
+}
+
+gst_status gst_reencode_blocks(gst_ctx *ctx, const gst_reencode_image *imgs, int n, void *stream) {
+  if (!ctx || !imgs || n <= 0) return GST_E_ARG;
+  std::vector<ReIn> in(n);
+  for (int i = 0; i < n; ++i)
+    in[i] = {imgs[i].width,
+             imgs[i].height,
+             static_cast<const uint8_t *>(imgs[i].d_rgb),
+             static_cast<const uint64_t *>(imgs[i].d_blocks),
+             static_cast<uint64_t *>(imgs[i].d_blocks_out),
+             static_cast<uint8_t *>(imgs[i].d_palette),
+             static_cast<uint8_t *>(imgs[i].d_indices),
+             imgs[i].d_palette_bytes};
+  std::lock_guard<std::mutex> lock(ctx_mutex(ctx));
+  cudaSetDevice(ctx_device(ctx));
+  EncodeState *st = nullptr;
+  const gst_status r = get_state(ctx, &st);
+  if (r != GST_OK) return r;
+  return reencode_locked(ctx, st, in, static_cast<cudaStream_t>(stream));
+}
+
+gst_status gst_prepare_planes(gst_ctx *ctx, const gst_symbol_buffers *imgs, int n, void *stream) {
+  if (!ctx || !imgs || n <= 0) return GST_E_ARG;
+  std::vector<PrepIn> in(n);
+  for (int i = 0; i < n; ++i)
+    in[i] = {imgs[i].width, imgs[i].height, static_cast<const uint8_t *>(imgs[i].d_blocks),
+             static_cast<uint8_t *>(imgs[i].d_y), static_cast<uint8_t *>(imgs[i].d_chroma), nullptr, nullptr};
+  std::lock_guard<std::mutex> lock(ctx_mutex(ctx));
+  cudaSetDevice(ctx_device(ctx));
+  EncodeState *st = nullptr;
+  const gst_status r = get_state(ctx, &st);
+  if (r != GST_OK) return r;
+  return prepare_locked(ctx, st, in, nullptr, static_cast<cudaStream_t>(stream), true);
+}
+
+gst_status gst_compress_rgb_dxt(gst_ctx *ctx, uint32_t width, uint32_t height, const uint8_t *rgb,
+                                const uint64_t *blocks, uint8_t *gst_out, size_t out_cap, size_t *out_len) {
+  if (!ctx || !rgb || !blocks || !gst_out || !out_len) return GST_E_ARG;
+  if (!stream_dims_ok(width, height, kSymsPerGroup) || !reencode_dims_ok(width, height)) return GST_E_ARG;
+  const uint64_t B = uint64_t(width / 4) * (height / 4);
+  const uint64_t pal_cap = palette_capacity(width, height);
+  std::lock_guard<std::mutex> lock(ctx_mutex(ctx));
+  cudaSetDevice(ctx_device(ctx));
+  EncodeState *st = nullptr;
+  gst_status r = get_state(ctx, &st);
+  if (r != GST_OK) return r;
+  for (cudaEvent_t ev : {st->done, st->prep_done, st->re_done}) {
+    const cudaError_t e = cudaEventSynchronize(ev);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  // device symbol buffer: Y 2B | chroma 4B | indices B | palette (capacity)
+  const size_t sym_bytes = static_cast<size_t>(7 * B + pal_cap);
+  const size_t rgb_bytes = static_cast<size_t>(width) * height * 3;
+  const size_t bound =
+      gst_encode_stream_bound(width, height, static_cast<uint32_t>(std::min<uint64_t>(pal_cap, 0xFFFFE000u)));
+  r = grow_dev(&st->blocks_d, &st->blocks_cap, static_cast<size_t>(8 * B));
+  if (r == GST_OK) r = grow_dev(&st->blocks2_d, &st->blocks2_cap, static_cast<size_t>(8 * B));
+  if (r == GST_OK) r = grow_dev(&st->rgb_d, &st->rgb_cap, rgb_bytes);
+  if (r == GST_OK) r = grow_dev(&st->in_d, &st->in_cap, sym_bytes);
+  if (r == GST_OK) r = grow_dev(&st->out_d, &st->out_cap, bound);
+  if (r != GST_OK) return r;
+  cudaError_t e = cudaMemcpyAsync(st->blocks_d, blocks, static_cast<size_t>(8 * B), cudaMemcpyHostToDevice, st->own);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(st->rgb_d, rgb, rgb_bytes, cudaMemcpyHostToDevice, st->own);
+  if (e != cudaSuccess) return cuda_status(e);
+  uint8_t *d = st->in_d;
+  const std::vector<ReIn> re = {{width, height, st->rgb_d, reinterpret_cast<const uint64_t *>(st->blocks_d),
+                                 reinterpret_cast<uint64_t *>(st->blocks2_d), d + 7 * B, d + 6 * B, st->pal_bytes_d}};
+  r = reencode_locked(ctx, st, re, st->own);
+  if (r != GST_OK) return r;
+  const std::vector<PrepIn> in = {{width, height, st->blocks2_d, d, d + 2 * B, nullptr, nullptr}};
+  r = prepare_locked(ctx, st, in, nullptr, st->own, true);
+  if (r != GST_OK) return r;
+  uint32_t pal_bytes = 0;
+  e = cudaMemcpyAsync(&pal_bytes, st->pal_bytes_d, sizeof(pal_bytes), cudaMemcpyDeviceToHost, st->own);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st->own);
+  if (e != cudaSuccess) return cuda_status(e);
+  r = read_device_status(ctx, st->own);
+  if (r != GST_OK) return r;
+  if (pal_bytes == 0 || pal_bytes > pal_cap) return GST_E_CUDA;
+  std::vector<SectionIn> secs = {{d, 2 * B}, {d + 2 * B, 4 * B}, {d + 7 * B, pal_bytes}, {d + 6 * B, B}};
+  std::vector<UnitIn> units = {{true, width, height, pal_bytes, 0, 4}};
+  r = encode_locked(ctx, st, secs, units, st->out_d, st->out_cap, st->offsets_d, st->own);
+  if (r != GST_OK) return r;
+  r = read_device_status(ctx, st->own);
+  if (r != GST_OK) return r;
+  unsigned long long off[2] = {0, 0};
+  e = cudaMemcpy(off, st->offsets_d, sizeof(off), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e);
+  const size_t len = static_cast<size_t>(off[1] - off[0]);
+  if (len > out_cap) return GST_E_ARG;
+  e = cudaMemcpy(gst_out, st->out_d + off[0], len, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e);
+  *out_len = len;
   return GST_OK;
 }
 

@@ -58,6 +58,41 @@ struct EncPrepImage {
   uint32_t pad;
 };
 
+// Index palette search (DXTImage::Reencode, codec/dxt_image.cpp:510-624).
+// Blocks are decided kReChunk at a time: every block of a chunk is first
+// scored against the window at the chunk's start (the last 127 palette
+// words) and against the chunk's earlier blocks, then one warp walks the
+// chunk in order and decides which blocks append their word.
+constexpr uint32_t kReWindow = 127;    // palette words a block may reuse (dxt_image.cpp:509, 562)
+constexpr uint32_t kReThreshold = 35;  // largest error increase + 1 of a reuse (dxt_image.cpp:508, 597)
+constexpr uint32_t kReChunk = 256;
+constexpr uint32_t kReRow = 128 + kReChunk;  // score row: window slots 0..126, a pad byte, chunk slots
+constexpr uint32_t kReInfo = 6;              // uint4 per block of ReImage::info
+
+struct ReImage {
+  const uint8_t *rgb;        // width * height * 3 bytes, 4-byte aligned
+  const uint64_t *blocks_in;  // the given blocks, raster order
+  uint64_t *blocks_out;       // the blocks after the search
+  uint8_t *palette;           // palette words (capacity pal_cap bytes), 16-byte aligned
+  uint8_t *deltas;            // B index deltas + 128
+  uint32_t *palette_bytes;    // the padded palette size (device u32)
+  uint8_t *scores;            // B rows of kReRow bytes: min(max(error increase, 0), 35), 35 = not usable
+  uint32_t *pal_src;          // palette index -> the block that appended it
+  uint32_t *pal_before;       // block -> palette size before it
+  uint32_t *idx;              // block -> its palette index
+  uint4 *info;                // per block kReInfo uint4: its 16 pixels (0x00BBGGRR), then {word,
+                              // asq, bsq, ab} and {1 / (asq bsq - ab ab), error as given, 0, 0}
+  uint32_t width, bw, B, n_chunks;
+  uint32_t pal_cap;
+  uint32_t pad[3];
+};
+
+struct ReState {  // per image, device
+  uint32_t P;       // palette words so far
+  uint32_t arrive;  // scoring CTAs of the current step that are done
+  uint32_t pad[2];
+};
+
 struct EncPrepChunk {  // 8192 blocks (or the image's rest) in raster order
   uint32_t image, start, len;
   uint32_t first_chunk, last_chunk;  // the image's chunks

@@ -770,6 +770,21 @@ extern "C" int gst_encode_rgb(uint32_t w, uint32_t h, const uint8_t *rgb, uint8_
   return encode_blocks(w, h, rgb, blocks, out, out_len, blocks_out, clips, nthreads);
 }
 
+extern "C" int gst_compress_blocks(uint32_t w, uint32_t h, const uint8_t *rgb, uint8_t *blocks_out, int nthreads) {
+  if (!rgb || !blocks_out || !w || !h || (w & 3) || (h & 3)) return 1;
+  const uint32_t bx = w / 4, by = h / 4;
+  uint64_t *blocks = reinterpret_cast<uint64_t *>(blocks_out);
+  parallel_for(by, nthreads, [&](uint32_t lo, uint32_t hi) {
+    uint8_t px[48];
+    for (uint32_t j = lo; j < hi; ++j)
+      for (uint32_t i = 0; i < bx; ++i) {
+        block_pixels(rgb, w, i, j, px);
+        blocks[size_t(j) * bx + i] = compress_block(px);
+      }
+  });
+  return 0;
+}
+
 extern "C" int gst_encode_dxt(uint32_t w, uint32_t h, const uint8_t *rgb, const uint8_t *dxt, uint8_t **out,
                               size_t *out_len, uint8_t *blocks_out, uint64_t *clips) {
   if (!dxt || !out || !out_len || !dims_ok(w, h)) return 1;

@@ -40,6 +40,11 @@ int gst_synth_image(uint32_t w, uint32_t h, uint64_t seed, double checker_frac, 
 int gst_encode_rgb(uint32_t w, uint32_t h, const uint8_t *rgb, uint8_t **out, size_t *out_len,
                    uint8_t *blocks, uint64_t *wavelet_clips, int nthreads);
 
+/* The block compressor alone: RGB8 image -> w*h/16 DXT1 blocks (8-byte
+ * aligned, raster order), before any palette search; w and h multiples of 4.
+ * Returns 0 on success. */
+int gst_compress_blocks(uint32_t w, uint32_t h, const uint8_t *rgb, uint8_t *blocks, int nthreads);
+
 /* DXT1 blocks (w*h/2 bytes, raster order) -> GST stream, with the index
  * palette built from the given blocks' interpolation words. */
 int gst_encode_dxt(uint32_t w, uint32_t h, const uint8_t *rgb, const uint8_t *dxt, uint8_t **out,

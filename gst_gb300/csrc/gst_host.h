@@ -26,6 +26,9 @@ cudaError_t launch_encode(const EncPlanView &v, int sm_count, cudaStream_t strea
 // gst_prepare.cu
 // Enqueues the endpoint stages (forward wavelet planes, run palette) of the
 // images of a plan.
+cudaError_t launch_reencode(const ReImage *d_imgs, const uint32_t *d_order, ReState *d_states, uint32_t n_images,
+                            const uint32_t *chunks_desc, uint32_t max_blocks, uint32_t *d_status, cudaStream_t stream,
+                            int *launches);
 cudaError_t launch_prepare(const EncPrepImage *d_images, uint32_t n_images, uint32_t n_tiles,
                            const EncPrepChunk *d_chunks, uint32_t n_chunks, uint32_t *d_counts,
                            uint32_t *d_palette_bytes, cudaStream_t stream, cudaEvent_t *ev = nullptr,

@@ -51,6 +51,7 @@ constexpr uint32_t kErrGroup = 2u;       // a group end offset is out of order o
 constexpr uint32_t kErrStream = 4u;      // a renormalisation read left its group
 constexpr uint32_t kErrPalette = 8u;     // a palette index is outside the palette
 constexpr uint32_t kErrTimeout = 16u;    // a bounded wait of the persistent kernel gave up
+constexpr uint32_t kErrReencode = 32u;   // the palette search's decision and selection passes disagree
 
 struct alignas(16) GstImageDesc {
   uint64_t freq_off;    // bytes from the compressed base to this image's 4 tables

@@ -239,6 +239,14 @@ cudaError_t launch_prepare(const EncPrepImage *d_images, uint32_t n_images, uint
   if (ev) cudaEventRecord(ev[0], stream);
   gst_fwd_tile_kernel<<<n_tiles, kTileThreads, 0, stream>>>(d_images, n_images);
   if (ev) cudaEventRecord(ev[1], stream);
+  if (n_chunks == 0) {  // the planes only: palette and deltas come from elsewhere
+    if (ev) {
+      cudaEventRecord(ev[2], stream);
+      cudaEventRecord(ev[3], stream);
+    }
+    if (names) names[0] = "gst_fwd_tile_kernel", names[1] = names[2] = "";
+    return cudaGetLastError();
+  }
   gst_fwd_count_kernel<<<n_chunks, kChunkThreads, 0, stream>>>(d_images, d_chunks, d_counts);
   if (ev) cudaEventRecord(ev[2], stream);
   gst_fwd_palette_kernel<<<n_chunks, kChunkThreads, 0, stream>>>(d_images, d_chunks, d_counts, d_palette_bytes);

@@ -53,7 +53,7 @@ EXPORTED_SYMBOLS = (
     # include/gst_encode.h
     "gst_encode_section_bound", "gst_encode_stream_bound", "gst_encode_bytes", "gst_encode_streams",
     "gst_compress_symbols", "gst_encode_normalize", "gst_palette_capacity", "gst_prepare_symbols",
-    "gst_compress_dxt",
+    "gst_compress_dxt", "gst_prepare_planes", "gst_reencode_blocks", "gst_compress_rgb_dxt",
 )
 
 
@@ -103,6 +103,14 @@ class SymbolBuffers(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("d_blocks", ctypes.c_void_p),
                 ("d_y", ctypes.c_void_p), ("d_chroma", ctypes.c_void_p), ("d_palette", ctypes.c_void_p),
                 ("d_indices", ctypes.c_void_p)]
+
+
+class ReencodeImage(ctypes.Structure):
+    """gst_reencode_image: one image's RGB8 source and DXT1 blocks in; the
+    searched blocks, palette, index deltas and palette size out (device pointers)."""
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("d_rgb", ctypes.c_void_p),
+                ("d_blocks", ctypes.c_void_p), ("d_blocks_out", ctypes.c_void_p), ("d_palette", ctypes.c_void_p),
+                ("d_indices", ctypes.c_void_p), ("d_palette_bytes", ctypes.c_void_p)]
 
 
 class GenTCHeader(ctypes.Structure):
@@ -202,6 +210,9 @@ def load_library() -> ctypes.CDLL:
         "gst_palette_capacity": (S, [U32, U32]),
         "gst_prepare_symbols": (I, [P, ctypes.POINTER(SymbolBuffers), I, P, P]),
         "gst_compress_dxt": (I, [P, U32, U32, P, P, S, ctypes.POINTER(S)]),
+        "gst_prepare_planes": (I, [P, ctypes.POINTER(SymbolBuffers), I, P]),
+        "gst_reencode_blocks": (I, [P, ctypes.POINTER(ReencodeImage), I, P]),
+        "gst_compress_rgb_dxt": (I, [P, U32, U32, P, P, P, S, ctypes.POINTER(S)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

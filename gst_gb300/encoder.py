@@ -33,6 +33,7 @@ def load_library() -> ctypes.CDLL:
                                    ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]
     lib.gst_encode_dxt.argtypes = [ctypes.c_uint32, ctypes.c_uint32, P, P, ctypes.POINTER(P), ctypes.POINTER(S), P,
                                    ctypes.POINTER(ctypes.c_uint64)]
+    lib.gst_compress_blocks.argtypes = [ctypes.c_uint32, ctypes.c_uint32, P, P, ctypes.c_int]
     lib.gst_encode_section.argtypes = [P, S, ctypes.POINTER(P), ctypes.POINTER(S), ctypes.c_int]
     lib.gst_normalize_frequencies.argtypes = [P, S, ctypes.c_int, P]
     lib.gst_encoder_free.argtypes = [P]
@@ -73,6 +74,18 @@ def encode_rgb(rgb: np.ndarray, nthreads: int = 0) -> tuple[bytes, np.ndarray, i
     if rc != 0:
         raise ValueError(f"gst_encode_rgb({w}x{h}) failed: {rc}")
     return _take(out, n.value), blocks, int(clips.value)
+
+
+def compress_blocks(rgb: np.ndarray, nthreads: int = 0) -> np.ndarray:
+    """RGB8 image (h, w, 3) -> its DXT1 blocks (uint64, raster order) from the
+    block compressor alone, before any palette search."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
+    h, w, _ = rgb.shape
+    blocks = np.empty(w * h // 16, dtype=np.uint64)
+    rc = load_library().gst_compress_blocks(w, h, rgb.ctypes.data, blocks.ctypes.data, _threads(nthreads))
+    if rc != 0:
+        raise ValueError(f"gst_compress_blocks({w}x{h}) failed: {rc}")
+    return blocks
 
 
 def encode_dxt(w: int, h: int, dxt_blocks: np.ndarray, rgb: np.ndarray | None = None) -> tuple[bytes, np.ndarray, int]:

@@ -17,7 +17,7 @@ from typing import Sequence
 
 import numpy as np
 
-from .decoder import GPUContext, StreamSymbols, SymbolBuffers, _check, _ptr, _stream, load_library
+from .decoder import GPUContext, ReencodeImage, StreamSymbols, SymbolBuffers, _check, _ptr, _stream, load_library
 
 SYMS_PER_GROUP = 8192
 
@@ -115,4 +115,44 @@ def compress_dxt(ctx: GPUContext, width: int, height: int, blocks: np.ndarray) -
     n = ctypes.c_size_t()
     _check(lib.gst_compress_dxt(ctx.handle, width, height, b.ctypes.data, out.ctypes.data, cap, ctypes.byref(n)),
            "gst_compress_dxt")
+    return out[: n.value].tobytes()
+
+
+def prepare_planes(ctx: GPUContext, images, stream=None) -> None:
+    """Enqueues the Y and chroma sections only (gst_prepare_planes); images as
+    for prepare_symbols (d_palette and d_indices are not used)."""
+    lib = load_library()
+    arr = images if isinstance(images, ctypes.Array) else symbol_buffers(images)
+    _check(lib.gst_prepare_planes(ctx.handle, arr, len(arr), _stream(stream)), "gst_prepare_planes")
+
+
+def reencode_images(images: Sequence[tuple]) -> ctypes.Array:
+    """The gst_reencode_image array of (width, height, d_rgb, d_blocks,
+    d_blocks_out, d_palette, d_indices, d_palette_bytes) tuples, for reuse."""
+    return (ReencodeImage * len(images))(*[ReencodeImage(w, h, *(_ptr(b) for b in bufs)) for w, h, *bufs in images])
+
+
+def reencode_blocks(ctx: GPUContext, images, stream=None) -> None:
+    """Enqueues the reference's index palette search (gst_reencode_blocks) for
+    every image: tuples as for reencode_images, or such an array."""
+    lib = load_library()
+    arr = images if isinstance(images, ctypes.Array) else reencode_images(images)
+    _check(lib.gst_reencode_blocks(ctx.handle, arr, len(arr), _stream(stream)), "gst_reencode_blocks")
+
+
+def compress_rgb_dxt(ctx: GPUContext, width: int, height: int, rgb: np.ndarray, blocks: np.ndarray) -> bytes:
+    """Host-to-host: RGB8 source (h, w, 3) and its DXT1 blocks -> the GST
+    stream of the reference's CompressDXTImage(DXTImage(w, h, rgb, dxt))."""
+    lib = load_library()
+    px = np.ascontiguousarray(rgb, dtype=np.uint8)
+    b = np.ascontiguousarray(blocks, dtype=np.uint64)
+    if px.size != width * height * 3 or b.size != width * height // 16:
+        raise ValueError("rgb and blocks must match width x height")
+    cap = stream_bound(width, height, palette_capacity(width, height))
+    if cap == 0:
+        raise ValueError("dimensions the decoder would reject")
+    out = np.zeros(cap, dtype=np.uint8)
+    n = ctypes.c_size_t()
+    _check(lib.gst_compress_rgb_dxt(ctx.handle, width, height, px.ctypes.data, b.ctypes.data, out.ctypes.data, cap,
+                                    ctypes.byref(n)), "gst_compress_rgb_dxt")
     return out[: n.value].tobytes()

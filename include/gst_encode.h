@@ -132,6 +132,57 @@ gst_status gst_prepare_symbols(gst_ctx *ctx, const gst_symbol_buffers *imgs, int
 gst_status gst_compress_dxt(gst_ctx *ctx, uint32_t width, uint32_t height, const uint64_t *blocks, uint8_t *gst_out,
                             size_t out_cap, size_t *out_len);
 
+/* The Y and chroma sections alone (gst_prepare_symbols without the palette
+ * stage; d_palette and d_indices are not used), for blocks whose palette and
+ * index deltas come from gst_reencode_blocks. */
+gst_status gst_prepare_planes(gst_ctx *ctx, const gst_symbol_buffers *imgs, int n, void *stream);
+
+/* --- the reference's index palette search ----------------------------------
+ *
+ *   reference                                       this header
+ *   ----------------------------------------------  -------------------------
+ *   DXTImage::Reencode (codec/dxt_image.cpp:         gst_reencode_blocks
+ *     510-624), run by the DXTImage(width, height,
+ *     rgb, dxt) constructor (:455-468)
+ *   GenTC::CompressDXTImage of that image           gst_compress_rgb_dxt
+ *     (codec/encoder.cpp:39-180)
+ *
+ * Byte for byte the reference's results: each block, in raster order, tries
+ * the last min(127, palette size) palette words, most recent first, refitting
+ * its 16 source pixels to the word (least-squares endpoints snapped to
+ * 5:6:5); the first refit that does not raise the block's error, else the one
+ * of least raise, is taken if the raise is below 35, and the block then
+ * carries the refit endpoints and that word; any other block keeps its own
+ * endpoints and appends its word.  Float arithmetic is the reference's as
+ * compiled for x86-64 (no fused multiply-add; a float -> int conversion of
+ * NaN or of a value outside int32 gives INT32_MIN).
+ *
+ * The search is sequential through the palette, so one call decides 256
+ * blocks of every image per kernel launch: an image of B blocks takes
+ * ceil(B / 256) launches, and images of a call run side by side.  It keeps
+ * 492 bytes of scratch per block on the device (the context's, grown as
+ * needed). */
+
+/* One image: w, h multiples of 4, at most 2^24 blocks. */
+typedef struct gst_reencode_image {
+  uint32_t width, height;
+  const void *d_rgb;        /* w*h*3 bytes RGB8, row-major, 4-byte aligned        */
+  const void *d_blocks;     /* w*h/16 DXT1 blocks (raster order), 8-byte aligned  */
+  void *d_blocks_out;       /* w*h/16 blocks after the search, 8-byte aligned     */
+  void *d_palette;          /* palette words, 4B rounded up to 8192 bytes, 16-byte aligned */
+  void *d_indices;          /* B index deltas + 128                                */
+  uint32_t *d_palette_bytes; /* device u32: the palette's bytes padded to 8192     */
+} gst_reencode_image;
+
+gst_status gst_reencode_blocks(gst_ctx *ctx, const gst_reencode_image *imgs, int n, void *stream);
+
+/* Blocking host-to-host form: RGB8 source (w*h*3 bytes) and its DXT1 blocks
+ * -> the GST stream of the reference's CompressDXTImage(DXTImage(w, h, rgb,
+ * dxt)); out_cap at least gst_encode_stream_bound(width, height,
+ * gst_palette_capacity(width, height)). */
+gst_status gst_compress_rgb_dxt(gst_ctx *ctx, uint32_t width, uint32_t height, const uint8_t *rgb,
+                                const uint64_t *blocks, uint8_t *gst_out, size_t out_cap, size_t *out_len);
+
 /* ans::ocl::NormalizeFrequencies on the GPU (blocking, host arrays): n <= 256
  * byte counts -> n frequencies summing to 2048.  GST_E_ARG when every count is
  * zero (the reference asserts). */

@@ -73,6 +73,9 @@ def load() -> ctypes.CDLL:
         lib.gsto_endpoint_planes.restype = ctypes.c_uint64
         lib.gsto_run_palette.argtypes = [U32, U32, P, P, S, P]
         lib.gsto_run_palette.restype = U32
+        lib.gsto_reencode.argtypes = [U32, U32, P, P, P, P, S, P]
+        lib.gsto_reencode.restype = U32
+        lib.gsto_reencode_candidate.argtypes = [P, U32, P, P, P]
         lib.gsto_section_search.restype = U32
         _lib = lib
     return _lib
@@ -94,6 +97,9 @@ def load_ref():
         lib.gstref_inverse_wavelet2d.restype = None
         lib.gstref_rans_encode_single.argtypes = [P, S, P, S, P, S, ctypes.POINTER(S), ctypes.POINTER(ctypes.c_uint32)]
         lib.gstref_encode_interleaved.argtypes = [P, S, P, S, S, P, S, ctypes.POINTER(S)]
+        lib.gstref_reencode.argtypes = [I, I, P, P, P, P, S, ctypes.POINTER(S), P, P, S, ctypes.POINTER(S)]
+        lib.gstref_stb_blocks.argtypes = [I, I, P, P]
+        lib.gstref_stb_blocks.restype = None
         _ref = lib
     return _ref
 
@@ -213,6 +219,32 @@ def endpoint_planes(width: int, height: int, blocks: np.ndarray) -> tuple[np.nda
     c = np.zeros(4 * B, np.uint8)
     clips = lib.gsto_endpoint_planes(width, height, blk.ctypes.data, y.ctypes.data, c.ctypes.data)
     return y, c, int(clips)
+
+
+def reencode(width: int, height: int, rgb: np.ndarray, blocks: np.ndarray) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """DXTImage::Reencode restated -> (blocks after the search, padded palette bytes, index deltas)."""
+    lib = load()
+    px = np.ascontiguousarray(rgb, dtype=np.uint8).reshape(-1)
+    blk = np.ascontiguousarray(blocks, dtype=np.uint64)
+    B = width * height // 16
+    assert px.size == width * height * 3 and blk.size == B
+    cap = (4 * B + 8191) // 8192 * 8192
+    pal = np.zeros(cap, np.uint8)
+    d = np.zeros(B, np.uint8)
+    out = np.zeros(B, np.uint64)
+    n = lib.gsto_reencode(width, height, px.ctypes.data, blk.ctypes.data, out.ctypes.data, pal.ctypes.data, cap,
+                          d.ctypes.data)
+    return out, pal[:n], d
+
+
+def reencode_candidate(px48: np.ndarray, word: int) -> tuple[int, bool, int, int]:
+    """One refit of the Reencode search -> (error, ok, ep1, ep2)."""
+    lib = load()
+    px = np.ascontiguousarray(px48, dtype=np.uint8).reshape(48)
+    ok = ctypes.c_int()
+    e1, e2 = ctypes.c_uint16(), ctypes.c_uint16()
+    err = lib.gsto_reencode_candidate(px.ctypes.data, word, ctypes.byref(ok), ctypes.byref(e1), ctypes.byref(e2))
+    return int(err), bool(ok.value), e1.value, e2.value
 
 
 def run_palette(width: int, height: int, blocks: np.ndarray) -> tuple[np.ndarray, np.ndarray]:

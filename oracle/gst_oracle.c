@@ -923,3 +923,168 @@ uint32_t gsto_run_palette(uint32_t w, uint32_t h, const uint64_t *blocks, uint8_
   memset(palette + 4 * n, 0, bytes - 4 * n);
   return (uint32_t)bytes;
 }
+
+/* ---- DXTImage::Reencode: the sequential index-palette search ---------------
+ * codec/dxt_image.cpp:510-624 with its helpers (Decode565 :53-72, Pack565
+ * :74-80, ToFiveBits / ToSixBits :82-130, PhysicalToLogical :144-170,
+ * CompressedBlock::Error :266-285, AssignIndices + RecalculateEndpoints
+ * :295-359).  Float arithmetic is the reference's as compiled for x86-64 (SSE,
+ * no fused multiply-add: this file is built with -ffp-contract=off), including
+ * the float -> int32 conversion of cvttss2si. */
+
+/* cvttss2si: truncation toward zero; NaN and values outside the int32 range
+ * give INT32_MIN (dxt_image.cpp:345-346 on x86-64). */
+static int32_t f2i_x86(float q) {
+  if (!(q >= -2147483648.0f && q < 2147483648.0f)) return INT32_MIN;
+  return (int32_t)q;
+}
+
+static uint8_t absdiff8(uint8_t a, uint8_t b) { return a > b ? (uint8_t)(a - b) : (uint8_t)(b - a); }
+
+/* ToFiveBits (bits = 5) / ToSixBits (bits = 6): the nearest value of the form
+ * v | v >> bits among the channel's base, the next and the previous step. */
+static uint8_t snap_channel(uint8_t x, int bits) {
+  const uint8_t mask = bits == 5 ? 0xF8 : 0xFC, step = bits == 5 ? 4 : 2;
+  uint8_t base = (uint8_t)(x & mask);
+  uint8_t high = (uint8_t)(base + step);
+  uint8_t low = base == 0 ? base : (uint8_t)(base - step);
+  base = (uint8_t)(base | (base >> bits));
+  high = (uint8_t)(high | (high >> bits));
+  low = (uint8_t)(low | (low >> bits));
+  const uint8_t db = absdiff8(x, base), dh = absdiff8(x, high), dl = absdiff8(x, low);
+  if (db <= dh) return db < dl ? base : low;
+  return high;
+}
+
+static uint16_t pack565(const uint8_t c[3]) {
+  return (uint16_t)(((c[0] & 0xF8) << 8) | ((c[1] & 0xFC) << 3) | ((c[2] & 0xF8) >> 3));
+}
+
+static void unpack565(uint16_t v, uint8_t c[3]) {
+  const uint32_t r = v >> 11, g = (v >> 5) & 0x3F, b = v & 0x1F;
+  c[0] = (uint8_t)((r << 3) | (r >> 2));
+  c[1] = (uint8_t)((g << 2) | (g >> 4));
+  c[2] = (uint8_t)((b << 3) | (b >> 2));
+}
+
+/* Sum of squared channel differences over the 16 pixels, / 48. */
+static int block_error(const uint8_t px[48], uint8_t pal[4][3], uint32_t word) {
+  size_t err = 0;
+  for (int i = 0; i < 16; ++i) {
+    const uint8_t *p = pal[(word >> (2 * i)) & 3];
+    for (int c = 0; c < 3; ++c) {
+      const size_t d = absdiff8(px[3 * i + c], p[c]);
+      err += d * d;
+    }
+  }
+  return (int)(err / 48);
+}
+
+/* Error of the block as given (PhysicalToLogical's palette: three-colour
+ * mode, with black, when ep1 <= ep2). */
+static int given_error(const uint8_t px[48], uint64_t blk) {
+  const uint16_t e1 = (uint16_t)blk, e2 = (uint16_t)(blk >> 16);
+  uint8_t pal[4][3];
+  unpack565(e1, pal[0]);
+  unpack565(e2, pal[1]);
+  for (int c = 0; c < 3; ++c) {
+    if (e1 <= e2) {
+      pal[2][c] = (uint8_t)((pal[0][c] + pal[1][c]) / 2);
+      pal[3][c] = 0;
+    } else {
+      pal[2][c] = (uint8_t)((2 * pal[0][c] + pal[1][c]) / 3);
+      pal[3][c] = (uint8_t)((pal[0][c] + 2 * pal[1][c]) / 3);
+    }
+  }
+  return block_error(px, pal, (uint32_t)(blk >> 32));
+}
+
+/* The block's pixels refitted to index word `word`: least-squares endpoints,
+ * snapped to 5:6:5, four-colour palette.  *ok = 0 when the refit endpoints do
+ * not keep the word as is (Pack565(ep1) <= Pack565(ep2) would swap them). */
+int gsto_reencode_candidate(const uint8_t px[48], uint32_t word, int *ok, uint16_t *ep1, uint16_t *ep2) {
+  static const float order_of[4] = {0.0f, 3.0f, 1.0f, 2.0f};
+  float asq = 0.0f, bsq = 0.0f, ab = 0.0f;
+  float ax[3] = {0.0f, 0.0f, 0.0f}, bx[3] = {0.0f, 0.0f, 0.0f};
+  for (int i = 0; i < 16; ++i) {
+    const float o = order_of[(word >> (2 * i)) & 3];
+    const float a = (3.0f - o) / 3.0f, b = o / 3.0f;
+    asq += a * a;
+    bsq += b * b;
+    ab += a * b;
+    for (int c = 0; c < 3; ++c) {
+      ax[c] += (float)px[3 * i + c] * a;
+      bx[c] += (float)px[3 * i + c] * b;
+    }
+  }
+  const float f = 1.0f / (asq * bsq - ab * ab);
+  uint8_t pal[4][3];
+  for (int c = 0; c < 3; ++c) {
+    const float p1 = f * (ax[c] * bsq - bx[c] * ab);
+    const float p2 = f * (bx[c] * asq - ax[c] * ab);
+    int32_t q1 = f2i_x86(p1 + 0.5f), q2 = f2i_x86(p2 + 0.5f);
+    q1 = q1 < 0 ? 0 : q1 > 255 ? 255 : q1;
+    q2 = q2 < 0 ? 0 : q2 > 255 ? 255 : q2;
+    const int bits = c == 1 ? 6 : 5;
+    pal[0][c] = snap_channel((uint8_t)q1, bits);
+    pal[1][c] = snap_channel((uint8_t)q2, bits);
+  }
+  for (int c = 0; c < 3; ++c) {
+    pal[2][c] = (uint8_t)((2 * pal[0][c] + pal[1][c]) / 3);
+    pal[3][c] = (uint8_t)((pal[0][c] + 2 * pal[1][c]) / 3);
+  }
+  *ep1 = pack565(pal[0]);
+  *ep2 = pack565(pal[1]);
+  *ok = *ep1 > *ep2;
+  return block_error(px, pal, word);
+}
+
+uint32_t gsto_reencode(uint32_t w, uint32_t h, const uint8_t *rgb, const uint64_t *blocks_in, uint64_t *blocks_out,
+                       uint8_t *palette, size_t pal_cap, uint8_t *deltas) {
+  const uint32_t bw = w / 4, bh = h / 4;
+  const size_t B = (size_t)bw * bh;
+  const size_t need = (4 * B + GSTO_SYMS_PER_GROUP - 1) / GSTO_SYMS_PER_GROUP * GSTO_SYMS_PER_GROUP;
+  if (pal_cap < need || B == 0) return 0;
+  size_t n = 0;  /* palette words so far */
+  long last = 0; /* palette index of the previous block */
+  for (size_t b = 0; b < B; ++b) {
+    const uint32_t bx = (uint32_t)(b % bw), by = (uint32_t)(b / bw);
+    uint8_t px[48];
+    for (int r = 0; r < 4; ++r) memcpy(px + 12 * r, rgb + ((size_t)(4 * by + r) * w + 4 * bx) * 3, 12);
+    const uint64_t blk = blocks_in[b];
+    const int given = given_error(px, blk);
+    int best = INT32_MAX;
+    size_t best_r = 0;
+    uint16_t best_e1 = 0, best_e2 = 0;
+    const size_t window = n < 127 ? n : 127;
+    for (size_t r = 0; r < window; ++r) { /* most recent word first */
+      const uint32_t word = rd32(palette + 4 * (n - 1 - r));
+      int ok;
+      uint16_t e1, e2;
+      const int diff = gsto_reencode_candidate(px, word, &ok, &e1, &e2) - given;
+      if (!ok) continue;
+      if (diff < best) {
+        best = diff;
+        best_r = r;
+        best_e1 = e1;
+        best_e2 = e2;
+        if (diff <= 0) break;
+      }
+    }
+    long idx;
+    if (best < 35) {
+      const uint32_t word = rd32(palette + 4 * (n - 1 - best_r));
+      blocks_out[b] = (uint64_t)best_e1 | ((uint64_t)best_e2 << 16) | ((uint64_t)word << 32);
+      idx = (long)(n - 1 - best_r);
+    } else {
+      blocks_out[b] = blk;
+      wr32(palette + 4 * n, (uint32_t)(blk >> 32));
+      idx = (long)n++;
+    }
+    deltas[b] = (uint8_t)(idx - last + 128);
+    last = idx;
+  }
+  const size_t bytes = (4 * n + GSTO_SYMS_PER_GROUP - 1) / GSTO_SYMS_PER_GROUP * GSTO_SYMS_PER_GROUP;
+  memset(palette + 4 * n, 0, bytes - 4 * n);
+  return (uint32_t)bytes;
+}

@@ -168,6 +168,26 @@ uint64_t gsto_endpoint_planes(uint32_t w, uint32_t h, const uint64_t *blocks, ui
 uint32_t gsto_run_palette(uint32_t w, uint32_t h, const uint64_t *blocks, uint8_t *palette, size_t pal_cap,
                           uint8_t *deltas);
 
+/* DXTImage::Reencode (codec/dxt_image.cpp:510-624): the reference's index
+ * palette search over the blocks in raster order.  Each block (its 16 RGB8
+ * pixels from `rgb`, w*h*3 bytes) tries the last min(127, palette size)
+ * palette words, most recent first: the pixels are refitted to the word
+ * (least-squares endpoints snapped to 5:6:5), a refit whose endpoints would
+ * swap is skipped, and the first refit whose error does not exceed the given
+ * block's ends the search; otherwise the smallest error increase wins.  An
+ * increase below 35 reuses that word (blocks_out gets the refit block),
+ * anything else appends the block's own word (blocks_out = blocks_in).
+ * Writes the palette (padded with zeros to a multiple of 8192 bytes) and the
+ * B index deltas (+128); returns the padded palette bytes, 0 if pal_cap is
+ * below 4B rounded up to 8192. */
+uint32_t gsto_reencode(uint32_t w, uint32_t h, const uint8_t *rgb, const uint64_t *blocks_in, uint64_t *blocks_out,
+                       uint8_t *palette, size_t pal_cap, uint8_t *deltas);
+
+/* One refit of the Reencode search: 16 RGB8 pixels (row-major in the block)
+ * refitted to index word `word` -> the error (dxt_image.cpp:266-285), *ok and
+ * the refit endpoints. */
+int gsto_reencode_candidate(const uint8_t px[48], uint32_t word, int *ok, uint16_t *ep1, uint16_t *ep2);
+
 /* ans_decode.cl:97-143 section lookup (ans_decode_multiple), for tests: returns
  * the section x the work-group at `wg` is assigned to by the kernel's search. */
 uint32_t gsto_section_search(const uint32_t *output_offsets, uint32_t num_offsets, uint32_t wg);

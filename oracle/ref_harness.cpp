@@ -12,6 +12,9 @@
 //   gstref_generate_histogram  ans::GenerateHistogram  ans/histogram.cpp:40-121
 //   gstref_inverse_wavelet2d   GenTC::InverseWavelet2D codec/wavelet.cpp:133-155
 //   gstref_encode_interleaved  ans::EncodeInterleaved     ans/encode.cpp:224-259
+//   gstref_stb_blocks     CompressRGB's stb_dxt blocks     codec/dxt_image.cpp:362-384
+//   gstref_reencode       DXTImage(w, h, rgb, dxt) = DXTImage::Reencode
+//                         codec/dxt_image.cpp:455-468, 510-624 (+ CompressDXT)
 //   gstref_rans_encode_single  rANS encoder at the OpenCL decoder's settings
 //                              (ans/ans_ocl_encode.cpp:10-18, ans/encode.cpp:56-69)
 #include <cstdint>
@@ -26,6 +29,7 @@
 #include "encoder.h"
 #include "entropy.h"
 #include "wavelet.h"
+#include "stb_dxt.h"
 
 namespace {
 int copy_out(const std::vector<uint8_t> &v, uint8_t *out, size_t cap, size_t *out_len) {
@@ -123,6 +127,47 @@ int gstref_encode_interleaved(const uint32_t *F, size_t nF, const uint8_t *symbo
   std::vector<uint8_t> s(symbols, symbols + n);
   std::vector<uint8_t> r = ans::EncodeInterleaved(s, ans::ocl::GetOpenCLOptions(f), num_streams);
   return copy_out(r, out, cap, out_len);
+}
+
+// The reference encoder's DXT1 blocks before its palette search: each 4x4
+// block as RGBA (alpha 255) through stb_compress_dxt_block in high-quality
+// mode, as CompressRGB does (codec/dxt_image.cpp:362-384, 520-529).
+void gstref_stb_blocks(int w, int h, const uint8_t *rgb, uint8_t *blocks) {
+  for (int by = 0; by < h / 4; ++by)
+    for (int bx = 0; bx < w / 4; ++bx) {
+      unsigned char block[64];
+      for (int j = 0; j < 4; ++j)
+        for (int i = 0; i < 4; ++i) {
+          const uint8_t *p = rgb + ((size_t)(4 * by + j) * w + 4 * bx + i) * 3;
+          unsigned char *q = block + (j * 4 + i) * 4;
+          q[0] = p[0];
+          q[1] = p[1];
+          q[2] = p[2];
+          q[3] = 0xFF;
+        }
+      stb_compress_dxt_block(blocks + 8 * ((size_t)by * (w / 4) + bx), block, 0, STB_DXT_HIGHQUAL);
+    }
+}
+
+// GenTC::DXTImage(width, height, rgb, dxt) runs DXTImage::Reencode over the
+// given blocks (codec/dxt_image.cpp:455-468, 510-624): the blocks after the
+// search, the palette words and the index deltas; and, when stream is not
+// null, CompressDXT of that image (codec/encoder.cpp:39-195).
+int gstref_reencode(int w, int h, const uint8_t *rgb, const uint8_t *dxt, uint8_t *blocks_out, uint8_t *palette,
+                    size_t pal_cap, size_t *pal_len, uint8_t *deltas, uint8_t *stream, size_t cap,
+                    size_t *stream_len) {
+  const size_t nblk = static_cast<size_t>(w / 4) * (h / 4);
+  std::vector<uint8_t> px(rgb, rgb + static_cast<size_t>(w) * h * 3);
+  std::vector<uint8_t> blocks(dxt, dxt + 8 * nblk);
+  GenTC::DXTImage img(w, h, px, blocks);
+  const auto &pb = img.PhysicalBlocks();
+  memcpy(blocks_out, pb.data(), pb.size() * sizeof(pb[0]));
+  const std::vector<uint8_t> &d = img.IndexDiffs();
+  if (d.size() != nblk) return -3;
+  memcpy(deltas, d.data(), nblk);
+  if (copy_out(img.PaletteData(), palette, pal_cap, pal_len) != 0) return -1;
+  if (!stream) return 0;
+  return copy_out(GenTC::CompressDXT(img), stream, cap, stream_len);
 }
 
 }  // extern "C"

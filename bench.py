@@ -289,6 +289,7 @@ def run_only(args, local):
         ctx.set_option("encode_hist_match", args.encode_hist_match)
         out = encode_workloads(ctx, stream, flush, device, measured_peak_hbm()[0], args.steps, args.warmup)
         out.update(dxt_workloads(ctx, stream, flush, device, measured_peak_hbm()[0], args.steps, args.warmup))
+        out.update(rgb_workloads(ctx, stream, flush, device, args.steps, args.warmup))
         ctx.close()
         return {"only": "encode", **out}
     if args.only == "rans":
@@ -525,6 +526,7 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
         rb.close()
     out.update(encode_workloads(ctx, stream, flush, device, peak, steps, 3))
     out.update(dxt_workloads(ctx, stream, flush, device, peak, steps, 3))
+    out.update(rgb_workloads(ctx, stream, flush, device, steps, 3))
     sec = workloads.rans_section()
     t, ok, rtuning = time_rans_section(ctx, sec, device, stream, flush, steps, 3)
     alg = len(sec.section) + sec.symbols.size
@@ -694,6 +696,99 @@ def dxt_workloads(ctx, stream, flush, device, peak, steps, warmup):
                                 "value": round(px / (statistics.median(e2e) / 1e3) / 1e6, 1), "unit": "Mpix/s",
                                 "h2d_bytes": blk_bytes, "d2h_bytes": len(s2)}
     return out
+
+
+def rgb_workloads(ctx, stream, flush, device, steps, warmup):
+    """The reference encoder's path from an RGB8 source and its DXT1 blocks
+    (CompressDXTImage(DXTImage(w, h, rgb, dxt))), on the GPU: per step
+    gst_reencode_blocks (the reference's index palette search), gst_prepare_planes
+    on the searched blocks, the palette sizes read back, gst_encode_streams.
+    Inputs: the 64-image batch's synthetic RGB images (same seeds and sizes)
+    and their blocks from the project's block compressor.  Checked: the two
+    smallest images' streams equal the C oracle's whole pipeline (restating
+    the reference's), and every stream decodes to the searched blocks."""
+    import torch
+    from gst_gb300 import decoder, encoder, entropy, workloads
+    import oracle
+    dims = workloads.batched_dims(64)
+    imgs = []
+    for k, (w, h) in enumerate(dims):
+        rgb = encoder.synth_image(w, h, 1000 + k, 0.0)
+        imgs.append((w, h, rgb, encoder.compress_blocks(rgb)))
+    bufs, re_descs, prep = [], [], []
+    pal = torch.zeros(len(imgs), dtype=torch.int32, device=device)
+    for k, (w, h, rgb, blocks) in enumerate(imgs):
+        B = w * h // 16
+        t = {"rgb": torch.from_numpy(rgb.reshape(-1)).to(device),
+             "b": torch.from_numpy(blocks.view(np.int64).copy()).to(device),
+             "o": torch.empty(B, dtype=torch.int64, device=device),
+             "y": torch.empty(2 * B, dtype=torch.uint8, device=device),
+             "c": torch.empty(4 * B, dtype=torch.uint8, device=device),
+             "p": torch.empty(entropy.palette_capacity(w, h), dtype=torch.uint8, device=device),
+             "i": torch.empty(B, dtype=torch.uint8, device=device)}
+        bufs.append(t)
+        re_descs.append((w, h, t["rgb"], t["b"], t["o"], t["p"], t["i"], pal[k:k + 1]))
+        prep.append((w, h, t["o"], t["y"], t["c"], t["p"], t["i"]))
+    re_descs = entropy.reencode_images(re_descs)
+    prep = entropy.symbol_buffers(prep)
+    h_pal = torch.zeros(len(imgs), dtype=torch.int32).pin_memory()
+    cap = sum(entropy.stream_bound(w, h, entropy.palette_capacity(w, h)) for w, h, *_ in imgs)
+    d_out = torch.zeros(cap, dtype=torch.uint8, device=device)
+    d_offs = torch.zeros(len(imgs) + 1, dtype=torch.int64, device=device)
+    descs = (entropy.StreamSymbols * len(imgs))(*[
+        entropy.StreamSymbols(w, h, 0, 0, t["y"].data_ptr(), t["c"].data_ptr(), t["p"].data_ptr(), t["i"].data_ptr())
+        for (w, h, *_), t in zip(imgs, bufs)])
+
+    def step():
+        entropy.reencode_blocks(ctx, re_descs, stream)
+        entropy.prepare_planes(ctx, prep, stream)
+        with torch.cuda.stream(stream):
+            h_pal.copy_(pal, non_blocking=True)
+        stream.synchronize()
+        for k, v in enumerate(h_pal.tolist()):
+            descs[k].palette_bytes = v
+        entropy.encode_streams(ctx, descs, d_out, d_offs, stream)
+
+    t_all, _ = time_steps(step, steps, warmup, stream, flush, clear=d_out)
+    ok = decoder.sync_status(ctx, stream) == decoder.GST_OK
+    o = d_offs.cpu().numpy()
+    host = d_out[: int(o[-1])].cpu().numpy().tobytes()
+    for k, t in enumerate(bufs):
+        got = decoder.decompress_dxt(ctx, host[o[k]:o[k + 1]])
+        ok = ok and bool(np.array_equal(got.view(np.uint64), t["o"].cpu().numpy().view(np.uint64)))
+    for k in sorted(range(len(imgs)), key=lambda i: imgs[i][0] * imgs[i][1])[:2]:
+        w, h, rgb, blocks = imgs[k]
+        ob, op, od = oracle.reencode(w, h, rgb, blocks)
+        y, c, _ = oracle.endpoint_planes(w, h, ob)
+        st, want = oracle.encode_stream(w, h, op.size, y, c, op, od)
+        ok = ok and st == 0 and host[o[k]:o[k + 1]] == want
+    t_re, _ = time_steps(lambda: entropy.reencode_blocks(ctx, re_descs, stream), steps, warmup, stream, flush)
+    ms, ms_re = statistics.mean(t_all), statistics.mean(t_re)
+    px = sum(w * h for w, h, *_ in imgs)
+    nblk = px // 16
+    return {"rgb_dxt_to_gst_batched_64": {
+        "value": round(px / (ms / 1e3) / 1e6, 1), "unit": "Mpix/s", "ms_per_call": round(ms, 4),
+        "palette_search_ms": round(ms_re, 4), "palette_search_mblocks_s": round(nblk / (ms_re / 1e3) / 1e6, 1),
+        "palette_words": int(h_pal.sum().item()) // 4, "blocks": nblk, "gst_bytes": int(o[-1]),
+        "matches_oracle_and_decodes_to_searched_blocks": bool(ok),
+        "cpu_baseline": cpu_baseline_reencode(imgs)}}
+
+
+def cpu_baseline_reencode(imgs):
+    """The C oracle's Reencode restatement on all host cores, one image per
+    thread (largest first): the search is sequential within an image."""
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+    threads = os.cpu_count() or 1
+    order = sorted(imgs, key=lambda a: -a[0] * a[1])
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(lambda a: oracle.reencode(*a), order))
+    dt = time.perf_counter() - t0
+    nblk = sum(w * h // 16 for w, h, *_ in imgs)
+    return {"value": round(nblk / dt / 1e6, 3), "unit": "Mblocks/s", "cores": threads, "kind": "port",
+            "sample": f"palette search of all {len(imgs)} images ({nblk / 1e6:.2f} M blocks), {threads} threads, "
+                      f"{dt:.2f} s"}
 
 
 RANS_CANDIDATES = ((16, 520), (12, 520), (12, 1016), (8, 1528), (8, 2040))

@@ -18,7 +18,7 @@
 //       one refit per lane); the last scoring CTA of an image then walks the
 //       chunk: one warp decides, block after block, whether the block's
 //       window holds a usable word (bit masks: a chain of register operations
-//       per block, warp votes once more than 96 blocks of the chunk appended),
+//       per block, warp votes once more than 127 blocks of the chunk appended),
 //       and the CTA appends the words of the blocks that found none;
 //   gst_re_select_kernel  each block's word: the first of least score in
 //       recency order (what the reference's loop with its early exit picks),
@@ -248,7 +248,7 @@ __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t
   // bit 31: a usable appended block in the 32-block words before j's
   __shared__ uint32_t meta[kReChunk];
   __shared__ uint32_t app[kReMaskWords];  // appended blocks of the chunk, bit j
-  __shared__ uint16_t app_pos[kReChunk];  // their positions in order (once more than 96)
+  __shared__ uint16_t app_pos[kReChunk];  // their positions in order (once more than 127)
   const uint32_t t = threadIdx.x;
   const uint32_t Wn = min(P, kReWindow);
   if (t < K) {
@@ -281,12 +281,15 @@ __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t
   if (t < 32) {
     const uint32_t lane = t;
     const uint32_t nw = (K + 31) / 32;
-    uint32_t c = 0;  // appended so far in this chunk
-    uint32_t w = 0;
-    // Fast path, 32 blocks at a time while c + 31 <= 127 (no appended chunk
-    // block leaves the window): the hits in the finished words are found in
-    // parallel; the 32 decisions are then a chain of register operations.
-    for (; w < nw && c <= kReWindow - 31; ++w) {
+    uint32_t c = 0;   // appended so far in this chunk
+    uint32_t w = 0;   // word of the next block to decide
+    uint32_t j0 = 0;  // next block to decide
+    // Fast path, 32 blocks at a time while no appended chunk block has left
+    // the window (c <= 127 before each decision): the hits in the finished
+    // words are found in parallel; the 32 decisions are then a chain of
+    // register operations.  A word in which the 128th append happens keeps
+    // its decisions up to that block; the slow path takes the rest.
+    for (; w < nw && c <= kReWindow; ++w) {
       {
         const uint32_t j = 32 * w + lane;
         uint32_t low = 0;
@@ -303,27 +306,43 @@ __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t
         m[i] = meta[32 * w + i];
       }
       uint32_t A = 0;
+      const uint32_t c_start = c;
 #pragma unroll
       for (uint32_t i = 0; i < 32; ++i) {
         const bool hit = (m[i] >> 31) != 0u || (g[i] & A) != 0u || (m[i] & 0xFFu) + c < kReWindow;
         A |= static_cast<uint32_t>(!hit) << i;
         c += !hit;
       }
+      j0 = min(32 * w + 32, K);
+      if (c > kReWindow) {
+        // the (128 - c_start)-th append of this word is the last decision kept
+        uint32_t mm = A;
+        for (uint32_t k = 1; k < kReWindow + 1 - c_start; ++k) mm &= mm - 1u;
+        const uint32_t pos = static_cast<uint32_t>(__ffs(mm)) - 1u;
+        A &= pos == 31 ? 0xFFFFFFFFu : (2u << pos) - 1u;
+        c = kReWindow + 1;
+        j0 = 32 * w + pos + 1;
+      }
       if (lane == 0) app[w] = A;
       __syncwarp();
+      if (c > kReWindow) {
+        ++w;
+        break;
+      }
     }
-    if (w < nw) {
-      // Slow path: appended chunk blocks may leave the window.  Lane l keeps
-      // the appended bits of word l; app_pos lists the appended positions.
+    if (j0 < K) {
+      // Slow path: appended chunk blocks may leave the window (c > 127).
+      // Lane l keeps the appended bits of word l; app_pos lists the appended
+      // positions.
       if (lane == 0) {
         uint32_t n = 0;
-        for (uint32_t v = 0; v < w; ++v)
+        for (uint32_t v = 0; v < kReMaskWords; ++v)
           for (uint32_t mm = app[v]; mm; mm &= mm - 1) app_pos[n++] = static_cast<uint16_t>(32 * v + __ffs(mm) - 1);
       }
       __syncwarp();
       uint32_t A = lane < kReMaskWords ? app[lane] : 0u;
       uint32_t first_kept = c > kReWindow ? app_pos[c - kReWindow] : 0u;
-      for (uint32_t j = 32 * w; j < K; ++j) {
+      for (uint32_t j = j0; j < K; ++j) {
         const uint32_t g = lane < kReMaskWords ? usable[j][lane] : 0u;
         const uint32_t keep = first_kept <= 32 * lane ? 0xFFFFFFFFu
                               : first_kept >= 32 * lane + 32 ? 0u

@@ -422,6 +422,7 @@ gst_status reencode_locked(gst_ctx *ctx, EncodeState *st, const std::vector<ReIn
     off = align_up(off + size_t(B) * kReRow, 256);
     off += 3 * align_up(size_t(B) * sizeof(uint32_t), 256);  // pal_src, pal_before, idx
     off += size_t(B) * kReInfo * 16;                         // info
+    off += align_up(size_t(B) * kReGroupsPerBlock * 4, 256);  // masks
   }
   if (st->re_used) {
     const cudaError_t e = cudaEventSynchronize(st->re_done);
@@ -450,6 +451,7 @@ gst_status reencode_locked(gst_ctx *ctx, EncodeState *st, const std::vector<ReIn
     d.pal_before = reinterpret_cast<uint32_t *>(maps + align_up(size_t(B) * 4, 256));
     d.idx = reinterpret_cast<uint32_t *>(maps + 2 * align_up(size_t(B) * 4, 256));
     d.info = reinterpret_cast<uint4 *>(maps + 3 * align_up(size_t(B) * 4, 256));
+    d.masks = reinterpret_cast<uint32_t *>(maps + 3 * align_up(size_t(B) * 4, 256) + size_t(B) * kReInfo * 16);
     d.width = im.width;
     d.bw = im.width / 4;
     d.B = B;

@@ -68,6 +68,7 @@ constexpr uint32_t kReThreshold = 35;  // largest error increase + 1 of a reuse 
 constexpr uint32_t kReChunk = 256;
 constexpr uint32_t kReRow = 128 + kReChunk;  // score row: window slots 0..126, a pad byte, chunk slots
 constexpr uint32_t kReInfo = 6;              // uint4 per block of ReImage::info
+constexpr uint32_t kReGroupsPerBlock = 4 + kReChunk / 32;  // 32-slot groups of a score row
 
 struct ReImage {
   const uint8_t *rgb;        // width * height * 3 bytes, 4-byte aligned
@@ -80,6 +81,8 @@ struct ReImage {
   uint32_t *pal_src;          // palette index -> the block that appended it
   uint32_t *pal_before;       // block -> palette size before it
   uint32_t *idx;              // block -> its palette index
+  uint32_t *masks;            // per block kReGroupsPerBlock words: bit s of word g = slot 32g + s scores
+                              // below 35 (window slots in words 0-3, chunk slots in words 4-11)
   uint4 *info;                // per block kReInfo uint4: its 16 pixels (0x00BBGGRR), then {word,
                               // asq, bsq, ab} and {1 / (asq bsq - ab ab), error as given, 0, 0}
   uint32_t width, bw, B, n_chunks;

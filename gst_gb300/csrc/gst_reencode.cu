@@ -46,7 +46,7 @@ namespace {
 
 constexpr uint32_t kReWarps = 8;                   // warps per scoring CTA
 constexpr uint32_t kReThreads = 32 * kReWarps;     // = kReChunk: the walker has a thread per block
-constexpr uint32_t kReGroups = 4 + kReChunk / 32;  // 32-slot groups per block: 4 window, 8 chunk
+constexpr uint32_t kReGroups = kReGroupsPerBlock;  // 32-slot groups per block: 4 window, 8 chunk
 constexpr uint32_t kReMaskWords = kReChunk / 32;
 static_assert(kReThreads == kReChunk, "the walker's first pass has one thread per block of the chunk");
 
@@ -211,14 +211,6 @@ __device__ __forceinline__ uint32_t score_of(uint32_t err, uint32_t given, bool 
   return !ok ? kReThreshold : d <= 0 ? 0u : d >= static_cast<int32_t>(kReThreshold) ? kReThreshold : uint32_t(d);
 }
 
-// Bit k of the result: byte k of v is below 35.
-__device__ __forceinline__ uint32_t usable4(uint32_t v) {
-  return __dp4a(__vcmpltu4(v, 0x23232323u) & 0x08040201u, 0x01010101u, 0u);
-}
-__device__ __forceinline__ uint32_t usable16(uint4 v) {
-  return usable4(v.x) | (usable4(v.y) << 4) | (usable4(v.z) << 8) | (usable4(v.w) << 12);
-}
-
 // Per block, once per call: its pixels, the sums of its own word (what any
 // later block refitting to that word needs) and its error as given.
 __global__ void __launch_bounds__(256) gst_re_info_kernel(const ReImage *__restrict__ imgs) {
@@ -243,7 +235,7 @@ __global__ void __launch_bounds__(256) gst_re_info_kernel(const ReImage *__restr
 // chunk's start (c = blocks of the chunk appended before j) or an appended
 // chunk block among the last 127 appended.
 __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t K, uint32_t P) {
-  __shared__ uint32_t usable[kReChunk][kReMaskWords];  // chunk slots i < j whose score is below 35
+  __shared__ uint32_t usable[kReMaskWords][kReChunk];  // word w, block j: chunk slots 32w.. < j below 35
   // meta[j]: bits 0-7 the first window slot below 35 (255 if none or >= Wn);
   // bit 31: a usable appended block in the 32-block words before j's
   __shared__ uint32_t meta[kReChunk];
@@ -252,29 +244,18 @@ __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t
   const uint32_t t = threadIdx.x;
   const uint32_t Wn = min(P, kReWindow);
   if (t < K) {
-    const uint4 *row = reinterpret_cast<const uint4 *>(im.scores + static_cast<size_t>(c0 + t) * kReRow);
-    uint4 v[8 + 2 * kReMaskWords];  // every load issued before any is used
-#pragma unroll
-    for (uint32_t q = 0; q < 8; ++q) v[q] = 16 * q < Wn ? __ldcg(row + q) : make_uint4(~0u, ~0u, ~0u, ~0u);
-#pragma unroll
-    for (uint32_t w = 0; w < kReMaskWords; ++w) {
-      v[8 + 2 * w] = 32 * w < t ? __ldcg(row + 8 + 2 * w) : make_uint4(~0u, ~0u, ~0u, ~0u);
-      v[9 + 2 * w] = 32 * w < t ? __ldcg(row + 9 + 2 * w) : make_uint4(~0u, ~0u, ~0u, ~0u);
-    }
+    // the scorers' ballots; words of groups that had no valid slot were not written
+    const uint4 *mk = reinterpret_cast<const uint4 *>(im.masks + static_cast<size_t>(c0 + t) * kReGroups);
+    const uint4 q0 = __ldcg(mk), q1 = __ldcg(mk + 1), q2 = __ldcg(mk + 2);
+    const uint32_t win[4] = {q0.x, q0.y, q0.z, q0.w};
+    const uint32_t chk[8] = {q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
     uint32_t first = 255;
 #pragma unroll
-    for (int q = 7; q >= 0; --q) {
-      uint32_t m = usable16(v[q]);
-      if (16 * q + 16 > Wn) m &= 16 * q >= Wn ? 0u : (1u << (Wn - 16 * q)) - 1u;
-      if (m) first = 16 * q + __ffs(m) - 1;
-    }
+    for (int q = 3; q >= 0; --q)
+      if (32 * q < Wn && win[q]) first = 32 * q + __ffs(win[q]) - 1;
     meta[t] = first;
 #pragma unroll
-    for (uint32_t w = 0; w < kReMaskWords; ++w) {
-      uint32_t m = usable16(v[8 + 2 * w]) | (usable16(v[9 + 2 * w]) << 16);
-      if (32 * w + 32 > t) m &= 32 * w >= t ? 0u : (1u << (t - 32 * w)) - 1u;
-      usable[t][w] = m;
-    }
+    for (uint32_t w = 0; w < kReMaskWords; ++w) usable[w][t] = 32 * w < t ? chk[w] : 0u;
   }
   if (t < kReMaskWords) app[t] = 0;
   __syncthreads();
@@ -295,14 +276,14 @@ __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t
         uint32_t low = 0;
 #pragma unroll
         for (uint32_t v = 0; v < kReMaskWords; ++v)
-          if (v < w) low |= usable[j][v] & app[v];
+          if (v < w) low |= usable[v][j] & app[v];
         if (j >= K || low) meta[j] |= 1u << 31;  // past the chunk: never appends
       }
       __syncwarp();
       uint32_t g[32], m[32];
 #pragma unroll
       for (uint32_t i = 0; i < 32; ++i) {
-        g[i] = usable[32 * w + i][w];
+        g[i] = usable[w][32 * w + i];
         m[i] = meta[32 * w + i];
       }
       uint32_t A = 0;
@@ -343,7 +324,7 @@ __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t
       uint32_t A = lane < kReMaskWords ? app[lane] : 0u;
       uint32_t first_kept = c > kReWindow ? app_pos[c - kReWindow] : 0u;
       for (uint32_t j = j0; j < K; ++j) {
-        const uint32_t g = lane < kReMaskWords ? usable[j][lane] : 0u;
+        const uint32_t g = lane < kReMaskWords ? usable[lane][j] : 0u;
         const uint32_t keep = first_kept <= 32 * lane ? 0xFFFFFFFFu
                               : first_kept >= 32 * lane + 32 ? 0u
                                                              : 0xFFFFFFFFu << (first_kept - 32 * lane);
@@ -420,7 +401,10 @@ __global__ void __launch_bounds__(kReThreads) gst_re_score_kernel(const ReImage 
       uint32_t ep;
       bool ok;
       const uint32_t err = refit(px, word, ws, &ep, &ok);
-      if (valid) im.scores[static_cast<size_t>(b) * kReRow + (win ? s : 128 + s)] = uint8_t(score_of(err, given, ok));
+      const uint32_t sc = score_of(err, given, ok);
+      if (valid) im.scores[static_cast<size_t>(b) * kReRow + (win ? s : 128 + s)] = uint8_t(sc);
+      const uint32_t m = __ballot_sync(0xFFFFFFFFu, valid && sc < kReThreshold);
+      if (lane == 0) im.masks[static_cast<size_t>(b) * kReGroups + g] = m;
     }
   }
   __shared__ uint32_t last;

@@ -160,7 +160,7 @@ gst_status gst_prepare_planes(gst_ctx *ctx, const gst_symbol_buffers *imgs, int 
  * The search is sequential through the palette, so one call decides 256
  * blocks of every image per kernel launch: an image of B blocks takes
  * ceil(B / 256) launches, and images of a call run side by side.  It keeps
- * 492 bytes of scratch per block on the device (the context's, grown as
+ * 540 bytes of scratch per block on the device (the context's, grown as
  * needed). */
 
 /* One image: w, h multiples of 4, at most 2^24 blocks. */

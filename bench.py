@@ -64,7 +64,7 @@ def parse_args():
     p.add_argument("--impl", choices=("gst", "reference"), default="gst")
     p.add_argument("--skip-extra", action="store_true", help="headline workload only")
     p.add_argument("--cpu-sample", type=int, default=16, help="images of the batch the CPU baseline decodes")
-    p.add_argument("--only", choices=("batched", "large", "plain", "rans", "serving", "encode"),
+    p.add_argument("--only", choices=("batched", "large", "plain", "rans", "serving", "encode", "reencode"),
                    help="time one workload's decode call only (a small command for profilers)")
     p.add_argument("--rans-blocks-per-sm", type=int, default=0,
                    help="fix the rANS kernel's CTAs of 128 threads per SM (8, 12 or 16) instead of autotuning")
@@ -292,6 +292,10 @@ def run_only(args, local):
         out.update(rgb_workloads(ctx, stream, flush, device, args.steps, args.warmup))
         ctx.close()
         return {"only": "encode", **out}
+    if args.only == "reencode":
+        out = rgb_workloads(ctx, stream, flush, device, args.steps, args.warmup)
+        ctx.close()
+        return {"only": "reencode", **out}
     if args.only == "rans":
         sec = workloads.rans_section()
         if args.rans_blocks_per_sm:  # fixed configuration (profiler command lines)

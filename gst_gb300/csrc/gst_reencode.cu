@@ -236,9 +236,11 @@ __global__ void __launch_bounds__(256) gst_re_info_kernel(const ReImage *__restr
 // chunk block among the last 127 appended.
 __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t K, uint32_t P) {
   __shared__ uint32_t usable[kReMaskWords][kReChunk];  // word w, block j: chunk slots 32w.. < j below 35
-  // meta[j]: bits 0-7 the first window slot below 35 (255 if none or >= Wn);
+  // meta[j]: bits 0-7 127 - (first window slot below 35), 0 if none: the
+  // window still holds that word while fewer blocks of the chunk appended;
   // bit 31: a usable appended block in the 32-block words before j's
   __shared__ uint32_t meta[kReChunk];
+  __shared__ uint32_t own_word[kReChunk];  // the blocks' own index words
   __shared__ uint32_t app[kReMaskWords];  // appended blocks of the chunk, bit j
   __shared__ uint16_t app_pos[kReChunk];  // their positions in order (once more than 127)
   const uint32_t t = threadIdx.x;
@@ -247,13 +249,14 @@ __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t
     // the scorers' ballots; words of groups that had no valid slot were not written
     const uint4 *mk = reinterpret_cast<const uint4 *>(im.masks + static_cast<size_t>(c0 + t) * kReGroups);
     const uint4 q0 = __ldcg(mk), q1 = __ldcg(mk + 1), q2 = __ldcg(mk + 2);
+    own_word[t] = static_cast<uint32_t>(im.blocks_in[c0 + t] >> 32);
     const uint32_t win[4] = {q0.x, q0.y, q0.z, q0.w};
     const uint32_t chk[8] = {q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
     uint32_t first = 255;
 #pragma unroll
     for (int q = 3; q >= 0; --q)
       if (32 * q < Wn && win[q]) first = 32 * q + __ffs(win[q]) - 1;
-    meta[t] = first;
+    meta[t] = first < Wn ? kReWindow - first : 0u;
 #pragma unroll
     for (uint32_t w = 0; w < kReMaskWords; ++w) usable[w][t] = 32 * w < t ? chk[w] : 0u;
   }
@@ -290,7 +293,7 @@ __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t
       const uint32_t c_start = c;
 #pragma unroll
       for (uint32_t i = 0; i < 32; ++i) {
-        const bool hit = (m[i] >> 31) != 0u || (g[i] & A) != 0u || (m[i] & 0xFFu) + c < kReWindow;
+        const bool hit = (m[i] >> 31) != 0u || (g[i] & A) != 0u || c < (m[i] & 0xFFu);
         A |= static_cast<uint32_t>(!hit) << i;
         c += !hit;
       }
@@ -329,7 +332,7 @@ __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t
                               : first_kept >= 32 * lane + 32 ? 0u
                                                              : 0xFFFFFFFFu << (first_kept - 32 * lane);
         const bool hit_new = __any_sync(0xFFFFFFFFu, (g & A & keep) != 0u);
-        const bool hit_old = (meta[j] & 0xFFu) + c < kReWindow;
+        const bool hit_old = c < (meta[j] & 0xFFu);
         if (!(hit_new || hit_old)) {
           if (lane == (j >> 5)) A |= 1u << (j & 31u);
           if (lane == 0) app_pos[c] = static_cast<uint16_t>(j);
@@ -352,7 +355,7 @@ __device__ void walk_chunk(const ReImage &im, ReState *st, uint32_t c0, uint32_t
     im.pal_before[b] = k;
     if (app[wj] & bit) {
       im.pal_src[k] = b;
-      reinterpret_cast<uint32_t *>(im.palette)[k] = static_cast<uint32_t>(im.blocks_in[b] >> 32);
+      reinterpret_cast<uint32_t *>(im.palette)[k] = own_word[t];
     }
   }
   if (t == 0) {

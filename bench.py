@@ -768,6 +768,17 @@ def rgb_workloads(ctx, stream, flush, device, steps, warmup):
         ok = ok and st == 0 and host[o[k]:o[k + 1]] == want
     t_re, _ = time_steps(lambda: entropy.reencode_blocks(ctx, re_descs, stream), steps, warmup, stream, flush)
     ms, ms_re = statistics.mean(t_all), statistics.mean(t_re)
+    # host to host: the largest image through gst_compress_rgb_dxt (RGB8 and
+    # blocks copied in, the stream copied out), as a caller of CompressDXT has it
+    k = max(range(len(imgs)), key=lambda i: imgs[i][0] * imgs[i][1])
+    w, h, rgb, blocks = imgs[k]
+    s_ref = entropy.compress_rgb_dxt(ctx, w, h, rgb, blocks)
+    e2e = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        s2 = entropy.compress_rgb_dxt(ctx, w, h, rgb, blocks)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    ok = ok and s2 == s_ref == host[o[k]:o[k + 1]]
     px = sum(w * h for w, h, *_ in imgs)
     nblk = px // 16
     return {"rgb_dxt_to_gst_batched_64": {
@@ -775,6 +786,9 @@ def rgb_workloads(ctx, stream, flush, device, steps, warmup):
         "palette_search_ms": round(ms_re, 4), "palette_search_mblocks_s": round(nblk / (ms_re / 1e3) / 1e6, 1),
         "palette_words": int(h_pal.sum().item()) // 4, "blocks": nblk, "gst_bytes": int(o[-1]),
         "matches_oracle_and_decodes_to_searched_blocks": bool(ok),
+        "e2e_one_image": {"call": "gst_compress_rgb_dxt", "image": f"{w}x{h}", "ms": round(statistics.median(e2e), 3),
+                          "mblocks_s": round(w * h / 16 / (statistics.median(e2e) / 1e3) / 1e6, 2),
+                          "h2d_bytes": int(rgb.nbytes + blocks.nbytes), "d2h_bytes": len(s2)},
         "cpu_baseline": cpu_baseline_reencode(imgs)}}
 
 

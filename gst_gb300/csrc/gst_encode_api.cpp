@@ -695,7 +695,7 @@ gst_status gst_encode_normalize(gst_ctx *ctx, const uint32_t *counts, int n, uin
 }
 
 gst_status gst_reencode_blocks(gst_ctx *ctx, const gst_reencode_image *imgs, int n, void *stream) {
-  if (!ctx || !imgs || n <= 0) return GST_E_ARG;
+  if (!ctx || !imgs || n <= 0 || n > 65535) return GST_E_ARG;  // images are grid.y of every launch
   std::vector<ReIn> in(n);
   for (int i = 0; i < n; ++i)
     in[i] = {imgs[i].width,

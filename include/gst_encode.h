@@ -174,6 +174,7 @@ typedef struct gst_reencode_image {
   uint32_t *d_palette_bytes; /* device u32: the palette's bytes padded to 8192     */
 } gst_reencode_image;
 
+/* n <= 65535 images per call. */
 gst_status gst_reencode_blocks(gst_ctx *ctx, const gst_reencode_image *imgs, int n, void *stream);
 
 /* Blocking host-to-host form: RGB8 source (w*h*3 bytes) and its DXT1 blocks

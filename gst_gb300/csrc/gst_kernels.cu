@@ -432,9 +432,21 @@ __device__ __forceinline__ void rans_item(const uint8_t *__restrict__ cmp, uint8
 // MINB: CTAs of 128 threads per SM that the register allocation must allow
 // (the "blocks per SM" tuning knob: 8 leaves 64 registers, 12 about 40,
 // 16 fills the SM with 64 warps at 32).
+// Programmatic dependent launch.  The rANS kernel lets the tile kernel queued
+// right behind it launch as soon as every rANS CTA has started; tile CTAs then
+// wait in griddepcontrol.wait until the rANS grid has completed and its writes
+// are visible.  Tile CTAs can only become resident after every rANS CTA has
+// started, so they never hold resources a rANS CTA still needs.  Launched
+// without the attribute, the wait returns at once.
+__device__ __forceinline__ void pdl_release_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait_prerequisites() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <int MINB>
 __global__ void __launch_bounds__(128, MINB) gst_rans_kernel(const uint8_t *__restrict__ cmp,
                                                              uint8_t *__restrict__ scratch, GstPlanView plan) {
+  pdl_release_dependents();
   extern __shared__ __align__(16) uint8_t smem_raw[];
   const GstRansItem it = plan.rans[plan.rans_order ? plan.rans_order[blockIdx.x] : blockIdx.x];
   rans_item<0>(cmp, scratch, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
@@ -758,6 +770,7 @@ __global__ void __launch_bounds__(256, 8) gst_tile_kernel(const uint8_t *__restr
                                                        GstPlanView plan) {
   __shared__ int32_t pl[6 * kPlaneWords];
   const GstTileItem it = plan.tiles[blockIdx.x];
+  pdl_wait_prerequisites();  // the rANS kernel's symbols (launched right behind it: see launch_decode)
   tile_work<256, false, RGB>(scratch, out, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
                              plan.images[it.image], it.tile, pl);
 }
@@ -905,8 +918,24 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
     if (ev) cudaEventRecord(ev[*launches], stream);
   }
   if (plan.n_tiles) {
-    if (plan.rgb) gst_tile_kernel<true><<<plan.n_tiles, 256, 0, stream>>>(d_scratch, d_out, plan);
-    else gst_tile_kernel<false><<<plan.n_tiles, 256, 0, stream>>>(d_scratch, d_out, plan);
+    // Right behind the rANS kernel (no event between them) the tile kernel is
+    // a programmatic dependent launch: its launch and CTA setup overlap the
+    // rANS tail, and griddepcontrol.wait orders its reads after the symbols.
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(plan.n_tiles);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    const bool pdl = plan.n_rans && !ev;
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    const uint8_t *scratch = d_scratch;
+    const cudaError_t e = plan.rgb ? cudaLaunchKernelEx(&cfg, gst_tile_kernel<true>, scratch, d_out, plan)
+                                   : cudaLaunchKernelEx(&cfg, gst_tile_kernel<false>, scratch, d_out, plan);
+    if (e != cudaSuccess) return e;
     if (names) names[*launches] = plan.rgb ? "gst_tile_rgb_kernel" : "gst_tile_kernel";
     ++*launches;
     if (ev) cudaEventRecord(ev[*launches], stream);

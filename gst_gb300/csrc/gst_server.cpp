@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -146,6 +147,13 @@ struct gst_server {
   uint64_t submitted = 0, completed = 0, rejected = 0, launches = 0, launched_images = 0, pixels = 0;
   uint64_t t_stats = 0;
   size_t dev_peak = 0;
+
+  // open-loop submissions from a native thread (gst_server_schedule)
+  std::thread sched;
+  std::atomic<bool> sched_stop{false};
+  int sched_submitted = 0, sched_rejected = 0;
+  uint64_t sched_late_max = 0;
+  gst_status sched_status = GST_OK;
 
   uint64_t now() const {
     return uint64_t(std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t0).count());
@@ -409,6 +417,10 @@ gst_status gst_server_create(gst_ctx *ctx, const gst_server_config *cfg, gst_ser
 
 void gst_server_destroy(gst_server *srv) {
   if (!srv) return;
+  if (srv->sched.joinable()) {
+    srv->sched_stop = true;
+    srv->sched.join();
+  }
   if (srv->thread.joinable()) {
     {
       std::lock_guard<std::mutex> lk(srv->mu);
@@ -467,6 +479,59 @@ gst_status gst_server_submit(gst_server *srv, const void *gst, size_t len, uint6
   }
   srv->cv.notify_one();
   return GST_OK;
+}
+
+gst_status gst_server_schedule(gst_server *srv, int n, const void *const *gst, const size_t *len,
+                               const uint64_t *arrival_ns, uint64_t *ids) {
+  if (!srv || n < 0 || (n > 0 && (!gst || !len || !arrival_ns || !ids))) return GST_E_ARG;
+  if (srv->sched.joinable()) return GST_E_ARG;  // one schedule at a time: wait for the last one first
+  srv->sched_stop = false;
+  srv->sched = std::thread([srv, n, gst, len, arrival_ns, ids] {
+    int sub = 0, rej = 0;
+    uint64_t late = 0;
+    gst_status status = GST_OK;
+    int i = 0;
+    for (; i < n && !srv->sched_stop; ++i) {
+      const uint64_t at = arrival_ns[i];
+      // Sleep through long gaps, spin through short ones: yielding the core
+      // can cost a whole scheduler time slice (measured: submissions up to
+      // 30 ms late at 20k req/s).
+      for (uint64_t t = srv->now(); t < at && !srv->sched_stop; t = srv->now()) {
+        const uint64_t ahead = at - t;
+        if (ahead > 250000) std::this_thread::sleep_for(std::chrono::nanoseconds(ahead - 150000));
+      }
+      const uint64_t t = srv->now();
+      late = std::max(late, t > at ? t - at : uint64_t(0));
+      // the id is written under the server's lock, before the request can run
+      const gst_status st = gst_server_submit(srv, gst[i], len[i], at, &ids[i]);
+      if (st == GST_OK) {
+        ++sub;
+      } else if (st == GST_E_OOM) {
+        ids[i] = 0;  // staging full at its arrival, or never admissible
+        ++rej;
+      } else {
+        status = st;
+        break;
+      }
+    }
+    for (; i < n; ++i) ids[i] = 0;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->sched_submitted = sub;
+    srv->sched_rejected = rej;
+    srv->sched_late_max = late;
+    srv->sched_status = status;
+  });
+  return GST_OK;
+}
+
+gst_status gst_server_schedule_wait(gst_server *srv, int *submitted, int *rejected, uint64_t *late_max_ns) {
+  if (!srv || !srv->sched.joinable()) return GST_E_ARG;
+  srv->sched.join();
+  std::lock_guard<std::mutex> lk(srv->mu);
+  if (submitted) *submitted = srv->sched_submitted;
+  if (rejected) *rejected = srv->sched_rejected;
+  if (late_max_ns) *late_max_ns = srv->sched_late_max;
+  return srv->sched_status;
 }
 
 gst_status gst_server_poll(gst_server *srv, gst_server_result *out, int cap, int *n, int wait_us) {

@@ -49,7 +49,8 @@ EXPORTED_SYMBOLS = (
     "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times", "gst_set_option",
     "gst_status_string",
     "gst_server_create", "gst_server_destroy", "gst_server_now_ns", "gst_server_submit", "gst_server_poll",
-    "gst_server_read", "gst_server_release", "gst_server_read_stats",
+    "gst_server_read", "gst_server_release", "gst_server_read_stats", "gst_server_schedule",
+    "gst_server_schedule_wait",
     # include/gst_encode.h
     "gst_encode_section_bound", "gst_encode_stream_bound", "gst_encode_bytes", "gst_encode_streams",
     "gst_compress_symbols", "gst_encode_normalize", "gst_palette_capacity", "gst_prepare_symbols",
@@ -201,6 +202,8 @@ def load_library() -> ctypes.CDLL:
         "gst_server_read": (I, [P, ctypes.c_uint64, P, S]),
         "gst_server_release": (I, [P, ctypes.c_uint64]),
         "gst_server_read_stats": (I, [P, ctypes.POINTER(ServerStats), I]),
+        "gst_server_schedule": (I, [P, I, P, P, P, P]),
+        "gst_server_schedule_wait": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(ctypes.c_uint64)]),
         "gst_encode_section_bound": (S, [S]),
         "gst_encode_stream_bound": (S, [U32, U32, U32]),
         "gst_encode_bytes": (I, [P, I, ctypes.POINTER(P), ctypes.POINTER(S), P, S, P, P]),

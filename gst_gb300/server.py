@@ -63,6 +63,38 @@ class DecodeServer:
     def release(self, rid: int) -> None:
         _check(load_library().gst_server_release(self._h, rid), "gst_server_release")
 
+    def schedule(self, pool: Sequence[bytes], choice, offsets_ns, lead_ns: int = 1_000_000):
+        """gst_server_schedule: a native thread submits pool[choice[i]] at server
+        time start + offsets_ns[i], where start = now + lead_ns is read after
+        every array is built (so that building them makes no submission late).
+        Returns (ids, start); ids (0 = refused) is filled as the thread goes (an
+        id is written before its request can run) and is final after
+        schedule_wait()."""
+        pool = list(pool)
+        pool_ptrs = np.array([ctypes.cast(ctypes.c_char_p(b), ctypes.c_void_p).value for b in pool], dtype=np.uintp)
+        pool_lens = np.array([len(b) for b in pool], dtype=np.uintp)
+        ch = np.asarray(choice, dtype=np.intp)
+        ptrs, lens = pool_ptrs[ch], pool_lens[ch]
+        ids = np.zeros(ch.size, dtype=np.uint64)
+        offs = np.asarray(offsets_ns, dtype=np.uint64)
+        start = self.now_ns() + int(lead_ns)
+        arr = offs + np.uint64(start)
+        _check(load_library().gst_server_schedule(self._h, int(ch.size), ptrs.ctypes.data, lens.ctypes.data,
+                                                  arr.ctypes.data, ids.ctypes.data), "gst_server_schedule")
+        # the library's thread reads these until schedule_wait(): keep them (only
+        # now, so that a refused second schedule leaves the running one's alone)
+        self._sched_keep = (pool, ptrs, lens, arr, ids)
+        return ids, start
+
+    def schedule_wait(self) -> tuple[int, int, int]:
+        """gst_server_schedule_wait -> (submitted, refused, worst lateness ns)."""
+        sub, rej, late = ctypes.c_int(), ctypes.c_int(), ctypes.c_uint64()
+        st = load_library().gst_server_schedule_wait(self._h, ctypes.byref(sub), ctypes.byref(rej),
+                                                     ctypes.byref(late))
+        self._sched_keep = None  # the thread has ended
+        _check(st, "gst_server_schedule_wait")
+        return sub.value, rej.value, late.value
+
     def stats(self, reset: bool = False) -> dict:
         st = ServerStats()
         _check(load_library().gst_server_read_stats(self._h, ctypes.byref(st), int(reset)), "gst_server_read_stats")
@@ -70,8 +102,9 @@ class DecodeServer:
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
-            load_library().gst_server_destroy(self._h)
+            load_library().gst_server_destroy(self._h)  # stops and joins a running schedule first
             self._h = None
+            self._sched_keep = None
 
     def __enter__(self):
         return self
@@ -126,7 +159,7 @@ class LoadResult:
 
 def run_poisson(server: DecodeServer, requests: Sequence[tuple[bytes, np.ndarray | None]], rate: float,
                 seconds: float, seed: int = 0, verify_every: int = 0,
-                pick: Callable[[np.random.Generator], int] | None = None) -> LoadResult:
+                pick: Callable[[np.random.Generator], int] | None = None, native: bool = True) -> LoadResult:
     """Open-loop Poisson arrivals at `rate` requests/s for `seconds`.
 
     requests: (GST stream, expected DXT1 blocks as uint64 or None); `pick`
@@ -137,15 +170,87 @@ def run_poisson(server: DecodeServer, requests: Sequence[tuple[bytes, np.ndarray
     is then read back and compared with its expected blocks (reading during the
     run would stall the submitter).  Python's cyclic garbage collector is
     paused for the run (a full collection in a large process stalls the
-    submitter for tens of milliseconds)."""
+    submitter for tens of milliseconds).  With `native` (the default) the
+    library's own thread submits each stream at its arrival time
+    (gst_server_schedule), so no stall of this process delays a submission;
+    this process only polls and releases (every `verify_every`-th id is kept
+    for the check)."""
     gc_on = gc.isenabled()
     gc.collect()
     gc.disable()
     try:
-        return _run_poisson(server, requests, rate, seconds, seed, verify_every, pick)
+        run = _run_poisson_native if native else _run_poisson
+        return run(server, requests, rate, seconds, seed, verify_every, pick)
     finally:
         if gc_on:
             gc.enable()
+
+
+def _run_poisson_native(server, requests, rate, seconds, seed, verify_every, pick) -> LoadResult:
+    rng = np.random.default_rng(seed)
+    n = int(rng.poisson(rate * seconds))
+    arrivals = np.sort(rng.uniform(0.0, seconds, n))
+    choice = [pick(rng) if pick else int(rng.integers(len(requests))) for _ in range(n)]
+    res = LoadResult(rate, seconds)
+    server.poll()
+    server.stats(reset=True)
+    offsets = np.round(arrivals * 1e9).astype(np.uint64)
+    ids, t0 = server.schedule([r[0] for r in requests], choice, offsets)
+    at_last = t0 + (int(offsets[-1]) if n else 0)
+    held = {}  # id -> dxt bytes, every verify_every-th id, read back after the run
+    last_done = t0
+    deadline = None
+    while True:
+        got = server.poll(2000)
+        for r in got:
+            last_done = max(last_done, r.done_ns)
+            res.completed += 1
+            lat = (r.done_ns - r.arrival_ns) / 1e3
+            res.latencies_us.append(lat)
+            res.waits_us.append((r.launch_ns - r.arrival_ns) / 1e3)
+            if lat > res.worst.get("latency_ms", 0.0) * 1e3:
+                res.worst = {"latency_ms": round(lat / 1e3, 4), "arrival_s": round((r.arrival_ns - t0) / 1e9, 4),
+                             "wait_ms": round((r.launch_ns - r.arrival_ns) / 1e6, 4),
+                             "launch_to_done_ms": round((r.done_ns - r.launch_ns) / 1e6, 4)}
+            if r.status != GST_OK:
+                res.errors += 1
+            if verify_every and r.id % verify_every == 0:
+                held[r.id] = r.dxt_bytes
+            else:
+                server.release(r.id)
+        if deadline is None and server.now_ns() >= at_last:
+            deadline = time.monotonic() + 60.0  # every arrival is past: drain what is left
+        if deadline is not None:
+            sub = int(np.count_nonzero(ids)) if n else 0
+            if res.completed >= sub or time.monotonic() > deadline:
+                break
+    res.submitted, res.rejected, late_ns = server.schedule_wait()
+    while res.completed < res.submitted:  # after the join the count is exact
+        got = server.poll(100000)
+        if not got:
+            break
+        for r in got:
+            last_done = max(last_done, r.done_ns)
+            res.completed += 1
+            res.latencies_us.append((r.done_ns - r.arrival_ns) / 1e3)
+            res.waits_us.append((r.launch_ns - r.arrival_ns) / 1e3)
+            if verify_every and r.id % verify_every == 0:
+                held[r.id] = r.dxt_bytes
+            else:
+                server.release(r.id)
+    res.submit_lag_max_us = late_ns / 1e3
+    res.seconds = max(seconds, (last_done - t0) / 1e9)
+    res.stats = server.stats()
+    index = {int(rid): i for i, rid in enumerate(ids) if rid}
+    for rid, nbytes in held.items():
+        want = requests[choice[index[rid]]][1]
+        if want is not None:
+            got = server.read(rid, nbytes).view(np.uint64)
+            res.verified += 1
+            if not np.array_equal(got, want):
+                res.mismatched += 1
+        server.release(rid)
+    return res
 
 
 def _run_poisson(server, requests, rate, seconds, seed, verify_every, pick) -> LoadResult:

@@ -342,6 +342,21 @@ gst_status gst_server_read(gst_server *server, uint64_t id, void *dst, size_t ca
 gst_status gst_server_release(gst_server *server, uint64_t id);
 gst_status gst_server_read_stats(gst_server *server, gst_server_stats *stats, int reset);
 
+/* Open-loop load from a native thread, so that no stall of the caller delays
+ * a submission: stream i (gst[i], len[i] bytes) is submitted at server time
+ * arrival_ns[i] (gst_server_now_ns clock, nondecreasing) and stamped with
+ * it, while the caller polls and releases results.  ids[i] receives the
+ * request's id as soon as it is submitted, or 0 if it was refused (staging
+ * full at its arrival, or never admissible); the caller may read ids while
+ * the schedule runs (each entry is written once, 8-byte aligned) and keeps
+ * the streams, len, arrival_ns and ids alive until gst_server_schedule_wait,
+ * which joins the thread and returns the submitted and refused counts and the
+ * worst lateness of a submission behind its arrival.  One schedule at a time
+ * (GST_E_ARG otherwise); gst_server_destroy stops a running one. */
+gst_status gst_server_schedule(gst_server *server, int n, const void *const *gst, const size_t *len,
+                               const uint64_t *arrival_ns, uint64_t *ids);
+gst_status gst_server_schedule_wait(gst_server *server, int *submitted, int *rejected, uint64_t *late_max_ns);
+
 /* Human-readable name of a status code. */
 const char *gst_status_string(gst_status s);
 

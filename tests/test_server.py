@@ -130,3 +130,37 @@ def test_poisson_load_bit_exact(gpu_ctx):
     assert s["completed"] == s["submitted"] > 0 and s["rejected"] == 0
     assert s["verified"] > 0 and s["bit_exact"]
     assert 0 < s["p50_ms"] <= s["p99_ms"]
+
+
+def test_poisson_load_python_submitter_bit_exact(gpu_ctx):
+    """The same load with this process submitting (native=False)."""
+    imgs = mixed_images()
+    reqs = [(im.stream, im.blocks) for im in imgs]
+    with DecodeServer(gpu_ctx, device_budget_bytes=1 << 30) as srv:
+        res = run_poisson(srv, reqs, rate=2000.0, seconds=0.3, seed=2, verify_every=3, native=False)
+    s = res.summary()
+    assert s["completed"] == s["submitted"] > 0 and s["rejected"] == 0 and s["bit_exact"]
+
+
+def test_native_schedule_submits_on_time(gpu_ctx):
+    """gst_server_schedule: every stream submitted at its arrival time from
+    the library's thread, ids written before the requests run, results
+    bit-exact; a second schedule while one runs is refused."""
+    imgs = mixed_images()
+    with DecodeServer(gpu_ctx, device_budget_bytes=1 << 30) as srv:
+        n = 300
+        pool = [im.stream for im in imgs]
+        choice = [i % len(imgs) for i in range(n)]
+        offsets = np.arange(n, dtype=np.uint64) * np.uint64(200_000)  # 5k req/s for 60 ms
+        ids, _ = srv.schedule(pool, choice, offsets)
+        with pytest.raises(Exception):
+            srv.schedule(pool, choice[:1], offsets[:1])
+        got = collect(srv, n)
+        sub, rej, late_ns = srv.schedule_wait()
+        assert sub == n and rej == 0 and len(got) == n
+        assert len(set(int(x) for x in ids)) == n and 0 not in set(int(x) for x in ids)
+        assert late_ns < 50_000_000  # well within the run: the thread keeps up at 5k req/s
+        for i, rid in enumerate(ids):
+            st, dxt = got[int(rid)]
+            assert st == decoder.GST_OK
+            assert np.array_equal(dxt.view(np.uint64), imgs[i % len(imgs)].blocks)

@@ -1,7 +1,13 @@
 """Host logic of the serving load generator (gst_gb300.server.run_poisson)
 against a fake server, on the CPU: open-loop arrivals, latency from the
-scheduled arrival time, verification and release of every result."""
+scheduled arrival time, verification and release of every result, with this
+process submitting and with a submitting thread in place of the library's
+(gst_server_schedule)."""
+import threading
+import time
+
 import numpy as np
+import pytest
 
 from gst_gb300 import decoder
 from gst_gb300.server import run_poisson
@@ -18,7 +24,7 @@ class FakeServer:
     """Completes each request 100 us after its arrival; one output is wrong."""
 
     def __init__(self, bad_payload=None, capacity=None):
-        import time
+        self._lock = threading.Lock()
         self._t0 = time.monotonic_ns()
         self.next_id = 1
         self.pending = []
@@ -29,27 +35,59 @@ class FakeServer:
         self.submitted = self.completed = 0
 
     def now_ns(self):
-        import time
         return time.monotonic_ns() - self._t0
 
     def submit(self, stream, arrival_ns=0):
-        if self.capacity is not None and len(self.pending) >= self.capacity:
-            return None
-        rid = self.next_id
-        self.next_id += 1
-        self.pending.append((rid, arrival_ns, stream))
-        self.submitted += 1
-        return rid
+        with self._lock:
+            if self.capacity is not None and len(self.pending) >= self.capacity:
+                return None
+            rid = self.next_id
+            self.next_id += 1
+            self.pending.append((rid, arrival_ns, stream))
+            self.submitted += 1
+            return rid
 
     def poll(self, wait_us=0):
         out = []
-        for rid, arrival, stream in self.pending:
+        with self._lock:
+            pending, self.pending = self.pending, []
+        for rid, arrival, stream in pending:
             payload = self.bad_payload if stream == b"bad" else np.frombuffer(stream, np.uint8).copy()
             self.outputs[rid] = payload
             out.append(FakeResult(rid, arrival, arrival + 100_000, payload.size))
-        self.pending = []
         self.completed += len(out)
+        if not out and wait_us:
+            time.sleep(min(wait_us, 1000) / 1e6)
         return out
+
+    def schedule(self, pool, choice, offsets_ns, lead_ns=1_000_000):
+        """A thread submitting pool[choice[i]] at start + offsets_ns[i], as gst_server_schedule does."""
+        streams = [pool[c] for c in choice]
+        start = self.now_ns() + lead_ns
+        arrival_ns = [start + int(o) for o in offsets_ns]
+        self._ids = np.zeros(len(streams), np.uint64)
+
+        def run():
+            sub = rej = late = 0
+            for i, (st, at) in enumerate(zip(streams, arrival_ns)):
+                while self.now_ns() < int(at):
+                    time.sleep(0.0001)
+                late = max(late, self.now_ns() - int(at))
+                rid = self.submit(st, int(at))
+                if rid is None:
+                    rej += 1
+                else:
+                    self._ids[i] = rid
+                    sub += 1
+            self._sched = (sub, rej, late)
+
+        self._thread = threading.Thread(target=run)
+        self._thread.start()
+        return self._ids, start
+
+    def schedule_wait(self):
+        self._thread.join()
+        return self._sched
 
     def read(self, rid, nbytes):
         return self.outputs[rid]
@@ -68,9 +106,10 @@ def requests():
     return good
 
 
-def test_open_loop_counts_and_latency():
+@pytest.mark.parametrize("native", [True, False])
+def test_open_loop_counts_and_latency(native):
     srv = FakeServer()
-    res = run_poisson(srv, requests(), rate=4000.0, seconds=0.25, seed=5, verify_every=2)
+    res = run_poisson(srv, requests(), rate=4000.0, seconds=0.25, seed=5, verify_every=2, native=native)
     s = res.summary()
     assert abs(s["submitted"] - 1000) < 150  # Poisson(1000)
     assert s["completed"] == s["submitted"] and s["rejected"] == 0
@@ -79,12 +118,13 @@ def test_open_loop_counts_and_latency():
     assert abs(s["p50_ms"] - 0.1) < 1e-6 and abs(s["p99_ms"] - 0.1) < 1e-6
 
 
-def test_mismatch_and_rejection_are_reported():
+@pytest.mark.parametrize("native", [True, False])
+def test_mismatch_and_rejection_are_reported(native):
     reqs = requests() + [(b"bad", np.zeros(2, np.uint64))]
     srv = FakeServer(bad_payload=np.ones(16, np.uint8))
     res = run_poisson(srv, reqs, rate=2000.0, seconds=0.2, seed=6, verify_every=1,
-                      pick=lambda rng: 4)
+                      pick=lambda rng: 4, native=native)
     assert res.mismatched == res.verified > 0 and not res.summary()["bit_exact"]
     srv2 = FakeServer(capacity=0)
-    res2 = run_poisson(srv2, requests(), rate=2000.0, seconds=0.1, seed=7)
+    res2 = run_poisson(srv2, requests(), rate=2000.0, seconds=0.1, seed=7, native=native)
     assert res2.rejected > 0 and res2.submitted == 0

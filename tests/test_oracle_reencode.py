@@ -90,3 +90,46 @@ def test_oracle_matches_reference_live():
         rb, rp, rd, _ = reference_reencode(ref, w, h, rgb, blocks, False)
         ob, op, od = oracle.reencode(w, h, rgb, blocks)
         assert np.array_equal(ob, rb) and np.array_equal(op[: rp.size], rp) and np.array_equal(od, rd)
+
+
+def given_error(px48: np.ndarray, blk: int) -> int:
+    """The error of a DXT1 block as given (dxt_image.cpp:144-170, 266-285):
+    the three-colour palette, black last, when ep1 <= ep2."""
+    def rgb(v):
+        r, g, b = v >> 11, (v >> 5) & 63, v & 31
+        return np.array([(r << 3) | (r >> 2), (g << 2) | (g >> 4), (b << 3) | (b >> 2)], np.int64)
+    e1, e2, word = blk & 0xFFFF, (blk >> 16) & 0xFFFF, blk >> 32
+    a, c = rgb(e1), rgb(e2)
+    pal = [a, c, (a + c) // 2, np.zeros(3, np.int64)] if e1 <= e2 else [a, c, (2 * a + c) // 3, (a + 2 * c) // 3]
+    px = px48.reshape(16, 3).astype(np.int64)
+    err = sum(int(((px[i] - pal[(word >> (2 * i)) & 3]) ** 2).sum()) for i in range(16))
+    return err // 48
+
+
+def test_search_output_invariants(fixture):
+    """On every fixture: the index deltas rebuild each block's palette index
+    (prefix sums of delta - 128, starting at 0), the palette word there is the
+    block's word, a block either keeps its given block or carries the refit
+    of its pixels to that word with an error raise below 35, and every
+    palette word is the word of a block that kept its own block."""
+    for c in fixture:
+        w, h = c["width"], c["height"]
+        rgb = make_rgb(c)
+        given = unpack(c["blocks_in"], np.uint64)
+        out = unpack(c["blocks_out"], np.uint64)
+        words = unpack(c["palette"], np.uint8).view(np.uint32)
+        idx = np.cumsum(unpack(c["deltas"], np.uint8).astype(np.int64) - 128)
+        assert idx[0] == 0 and idx.min() >= 0 and idx.max() < words.size
+        assert np.array_equal(words[idx], (out >> np.uint64(32)).astype(np.uint32)), c["name"]
+        bw = w // 4
+        for b in np.nonzero(out != given)[0][:64]:  # a sample of the refit blocks
+            by, bx = divmod(int(b), bw)
+            px = rgb[4 * by:4 * by + 4, 4 * bx:4 * bx + 4].reshape(48)
+            err, ok, e1, e2 = oracle.reencode_candidate(px, int(out[b] >> np.uint64(32)))
+            assert ok and int(out[b]) & 0xFFFFFFFF == e1 | (e2 << 16), (c["name"], b)
+            assert err - given_error(px, int(given[b])) < 35, (c["name"], b)
+        first_use = {}
+        for b, k in enumerate(idx):
+            first_use.setdefault(int(k), b)
+        for k, b in first_use.items():  # the block that appended word k kept its own block
+            assert out[b] == given[b] and int(given[b] >> np.uint64(32)) == int(words[k]), (c["name"], k)

@@ -70,13 +70,18 @@ def parse_args():
                    help="fix the rANS kernel's CTAs of 128 threads per SM (8, 12 or 16) instead of autotuning")
     p.add_argument("--persistent", type=int, default=0, choices=(0, 1),
                    help="with --rans-blocks-per-sm: 1 = the persistent single-kernel form")
-    p.add_argument("--serve-seconds", type=float, default=2.0,
-                   help="length of each open-loop serving run (the serving config names 60 s)")
+    p.add_argument("--serve-seconds", type=float, default=60.0,
+                   help="length of each open-loop run of the batched server (the serving config's 60 s)")
+    p.add_argument("--serve-plain-seconds", type=float, default=5.0,
+                   help="length of each run of the per-request plain-decode comparison (it saturates near 10k "
+                        "req/s, so its 20k req/s queue only grows with the run)")
+    p.add_argument("--serve-bound-budget-mib", type=int, default=256,
+                   help="device budget of the extra 20k req/s run in which admission binds (0: skip it)")
     p.add_argument("--serve-rates", default="1000,5000,20000", help="Poisson arrival rates, requests/s")
     p.add_argument("--serve-class-tune", type=int, default=1,
                    help="1: tune each size class (gst_autotune_class) before the serving runs")
     p.add_argument("--serve-modes", default="batched,plain", help="serving modes to run")
-    p.add_argument("--serve-verify-every", type=int, default=50,
+    p.add_argument("--serve-verify-every", type=int, default=500,
                    help="every k-th served result stays resident until the run ends and is checked bit for bit")
     p.add_argument("--encode-hist-match", type=int, default=0, choices=(0, 1),
                    help="encoder byte counts: merge equal lanes before the atomic (1) or not (0)")
@@ -201,6 +206,66 @@ def measured_peak_hbm() -> tuple[float, str]:
 
 
 # ---------------------------------------------------------------------------
+# Benchmark inputs: the reference encoder's streams of the configured images
+# (tests/golden/ref_streams/, made by tests/golden/make_ref_streams.py), with
+# the blocks a correct decode returns computed by the checker (the oracle's
+# restatement of the reference decoder) and checked against the committed
+# digests.  Where the fixtures are missing, the project's own stream producer
+# stands in and every line says so.
+def with_expected(images, threads=None):
+    import hashlib
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    todo = [im for im in images if im.blocks is None]
+
+    def one(im, n=1):
+        st, dec = oracle.decode(im.stream, oracle.SCAN_EXACT, nthreads=n)
+        assert st == 0, f"oracle rejects a fixture stream ({im.width}x{im.height} seed {im.seed})"
+        raw = np.ascontiguousarray(dec).tobytes()
+        if hashlib.sha256(raw).hexdigest() != im.decoded_sha256:
+            raise AssertionError(f"oracle decode of {im.width}x{im.height} seed {im.seed} differs from the "
+                                 f"fixture digest")
+        im.blocks = np.frombuffer(raw, np.uint64)
+
+    big = [im for im in todo if im.pixels >= (1 << 24)]
+    for im in big:
+        one(im, threads)
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one, [im for im in todo if im not in big]))
+    return images
+
+
+_INPUTS: dict = {}
+
+
+def _cached(key, make):
+    if key not in _INPUTS:
+        _INPUTS[key] = make()
+    return _INPUTS[key]
+
+
+def bench_batch():
+    from gst_gb300 import workloads
+    if workloads.ref_available():
+        return _cached("batch", lambda: with_expected(workloads.ref_batched())), workloads.REF_ENCODER
+    return workloads.batched(64), "gst_gb300 stream producer (reference-encoded fixtures missing)"
+
+
+def bench_large():
+    from gst_gb300 import workloads
+    if workloads.ref_available():
+        return _cached("large", lambda: with_expected([workloads.ref_large()])), workloads.REF_ENCODER
+    return [workloads.large()], "gst_gb300 stream producer (reference-encoded fixtures missing)"
+
+
+def bench_plain():
+    from gst_gb300 import workloads
+    if workloads.ref_available():
+        return with_expected([workloads.ref_plain()]), workloads.REF_ENCODER
+    return [workloads.plain(0)], "gst_gb300 stream producer (reference-encoded fixtures missing)"
+
+
 class Batch:
     """Packed, device-resident batch of GST streams with its expected output."""
 
@@ -314,8 +379,7 @@ def run_only(args, local):
             t, ok, tuning = time_rans_section(ctx, sec, device, stream, flush, args.steps, args.warmup)
         units = sec.symbols.size
     else:
-        imgs = {"batched": lambda: workloads.batched(64), "large": lambda: [workloads.large()],
-                "plain": lambda: [workloads.plain(0)]}[args.only]()
+        imgs, _ = {"batched": bench_batch, "large": bench_large, "plain": bench_plain}[args.only]()
         b = Batch(imgs, device)
         rb = decoder.ResidentBatch(ctx, b.hdrs)
         tuning = tune(rb, b, stream, args)
@@ -338,7 +402,7 @@ def run_gst(args, rank, world, local):
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
     t0 = time.time()
-    images = workloads.batched(64)
+    images, encoder_name = bench_batch()
     encode_s = time.time() - t0
     batch = Batch(images, device)
     ctx = decoder.GPUContext(local)
@@ -439,6 +503,7 @@ def run_gst(args, rank, world, local):
         "config": {
             "workload": "batched: 64 synthetic images, w,h in {512,1024,2048}, seeds 1000+i, one resident-batch "
                         "graph launch per step",
+            "encoder": encoder_name,
             "images": len(images),
             "pixels_per_step": batch.pixels,
             "gst_bytes_per_step": batch.gst_bytes,
@@ -486,7 +551,7 @@ def run_gst(args, rank, world, local):
                     f"{'persistent' if best[1][2] else 'two-kernel'} decodes (pinned host layout in, pinned DXT1 out)",
             "serial_ms_per_step": round(statistics.mean(t_ser), 4),
         },
-        "encode_seconds": round(encode_s, 1),
+        "input_seconds": round(encode_s, 1),
     }
     if not args.skip_extra:
         line["workloads"] = extra_workloads(ctx, stream, flush, device, peak, args)
@@ -505,7 +570,12 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
     from gst_gb300 import decoder, workloads
     out = {}
     steps = max(5, args.steps // 2)
-    for name, imgs in (("large_8192", [workloads.large()]), ("plain_512", [workloads.plain(0)])):
+    large, large_enc = bench_large()
+    plain, plain_enc = bench_plain()
+    runs = [("large_8192", large, large_enc), ("plain_512", plain, plain_enc),
+            ("batched_64_project_encoder", workloads.batched(64),
+             "gst_gb300 stream producer (secondary input: its own DXT1 compressor and palette search)")]
+    for name, imgs, enc_name in runs:
         b = Batch(imgs, device)
         rb = decoder.ResidentBatch(ctx, b.hdrs)
         tuning = tune(rb, b, stream, args)
@@ -525,7 +595,7 @@ def extra_workloads(ctx, stream, flush, device, peak, args):
             "dxt1_gbs": round(b.out_bytes / (ms / 1e3) / 1e9, 2),
             "hbm_frac": round(b.alg_bytes / (ms / 1e3) / 1e9 / peak, 4),
             "kernels": {kk: round(v["avg_ms"], 4) for kk, v in ks.items()},
-            "gst_bytes": b.gst_bytes, "bit_exact": ok, "rans_tuning": tuning,
+            "gst_bytes": b.gst_bytes, "bit_exact": ok, "rans_tuning": tuning, "encoder": enc_name,
         }
         rb.close()
     out.update(encode_workloads(ctx, stream, flush, device, peak, steps, 3))
@@ -576,7 +646,7 @@ def encode_workloads(ctx, stream, flush, device, peak, steps, warmup):
     import torch
     from gst_gb300 import decoder, entropy, workloads
     out = {}
-    for name, imgs in (("encode_batched_64", workloads.batched(64)), ("encode_large_8192", [workloads.large()])):
+    for name, imgs in (("encode_batched_64", bench_batch()[0]), ("encode_large_8192", bench_large()[0])):
         syms = [device_symbols(ctx, im.stream, device) for im in imgs]
         hdrs = [decoder.parse_header(im.stream) for im in imgs]
         descs = [entropy.stream_symbols(h.width, h.height, h.palette_bytes, s) for h, s in zip(hdrs, syms)]
@@ -635,7 +705,7 @@ def dxt_workloads(ctx, stream, flush, device, peak, steps, warmup):
     import torch
     from gst_gb300 import decoder, entropy, workloads
     out = {}
-    for name, imgs in (("dxt_to_gst_batched_64", workloads.batched(64)), ("dxt_to_gst_large_8192", [workloads.large()])):
+    for name, imgs in (("dxt_to_gst_batched_64", bench_batch()[0]), ("dxt_to_gst_large_8192", bench_large()[0])):
         bufs, prep, hdr = [], [], []
         for im in imgs:
             B = im.width * im.height // 16
@@ -851,7 +921,13 @@ def serving(ctx, args) -> dict:
     device budget; every 50th result is read back and checked."""
     from gst_gb300 import workloads
     from gst_gb300.server import DecodeServer, run_poisson
-    pool = workloads.serving_pool(per_class=2)
+    if workloads.ref_available():
+        pool = workloads.ref_serving_pool()
+        with_expected([im for ims in pool.values() for im in ims])
+        pool_encoder = workloads.REF_ENCODER
+    else:
+        pool = workloads.serving_pool(per_class=4)
+        pool_encoder = "gst_gb300 stream producer (reference-encoded fixtures missing)"
     dims = workloads.SERVING_DIMS
     weights = np.array([0.4, 0.3, 0.2, 0.1])
     keys = [(w, h) for w in dims for h in dims]
@@ -879,7 +955,10 @@ def serving(ctx, args) -> dict:
         d_out = torch.empty(hdrs[0].dxt_bytes, dtype=torch.uint8, device="cuda")
         classes.append(decoder.autotune_class(ctx, hdrs, d_cmp, d_out, iterations=3))
     out = {"config": {"dims": list(dims), "weights": weights.tolist(), "pool_streams": len(reqs),
+                      "pool_encoder": pool_encoder,
+                      "pool_streams_per_class_min": min(len(v) for v in pool.values()),
                       "device_budget_gib": 32, "seconds_per_rate": args.serve_seconds,
+                      "plain_seconds_per_rate": args.serve_plain_seconds,
                       "verify_every": args.serve_verify_every,
                       "class_tuning": {f"class {c} ({w}x{w})": list(decoder.get_class_tuning(ctx, c))
                                        for c, w in zip(classes, dims)},
@@ -887,33 +966,112 @@ def serving(ctx, args) -> dict:
                                            "persistent); the server keeps the two-kernel form"}}
     for rate in [float(r) for r in args.serve_rates.split(",") if r]:
         row = {}
-        for mode, kw in (("batched", dict(max_inflight=4, max_batch_images=256)),
-                         ("plain", dict(max_inflight=1, max_batch_images=1))):
-            if mode not in args.serve_modes.split(","):
+        for mode, kw, secs in (("batched", dict(max_inflight=4, max_batch_images=256), args.serve_seconds),
+                               ("plain", dict(max_inflight=1, max_batch_images=1), args.serve_plain_seconds)):
+            if mode not in args.serve_modes.split(",") or secs <= 0:
                 continue
             with DecodeServer(ctx, device_budget_bytes=32 << 30, **kw) as srv:
                 run_poisson(srv, reqs, rate, 0.2, seed=7, pick=pick)  # warm-up
-                res = run_poisson(srv, reqs, rate, args.serve_seconds, seed=int(rate),
+                res = run_poisson(srv, reqs, rate, secs, seed=int(rate),
                                   verify_every=args.serve_verify_every, pick=pick)
             row[mode] = res.summary()
         out[f"{int(rate)}_req_s"] = row
+    if args.serve_bound_budget_mib > 0 and "batched" in args.serve_modes.split(","):
+        # Admission under pressure: a budget small enough that requests wait
+        # for the memory of earlier ones (compressed input + DXT1 output).
+        budget = args.serve_bound_budget_mib << 20
+        secs = min(10.0, args.serve_seconds)
+        with DecodeServer(ctx, device_budget_bytes=budget, max_inflight=4, max_batch_images=256) as srv:
+            run_poisson(srv, reqs, 20000.0, 0.2, seed=7, pick=pick)
+            res = run_poisson(srv, reqs, 20000.0, secs, seed=20001, verify_every=4 * args.serve_verify_every,
+                              pick=pick)
+        out["20000_req_s_budget_bound"] = {"device_budget_mib": args.serve_bound_budget_mib, **res.summary()}
     return out
 
 
-def cpu_baseline(images):
-    """The C oracle (restating the reference's decoder) on all host cores."""
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu part", "hardware")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def cpu_decode_rate(images, threads: int, passes: int, warmup: int, scan) -> tuple[float, list[float]]:
+    """Mpix/s of the oracle's decode (the reference decoder's arithmetic) over
+    `images`: `warmup` untimed passes, then `passes` timed ones.  With more than
+    one thread the images go one per thread (largest first), and an image
+    larger than 1/threads of the sample is itself decoded by all threads."""
+    from concurrent.futures import ThreadPoolExecutor
     import oracle
-    threads = os.cpu_count() or 1
     oracle.load()
     px = sum(im.pixels for im in images)
-    t0 = time.perf_counter()
-    for im in images:
-        st, _ = oracle.decode(im.stream, oracle.SCAN_EXACT, nthreads=threads)
+    order = sorted(images, key=lambda im: -im.pixels)
+    big = [im for im in order if threads > 1 and im.pixels * threads > px]
+    small = [im for im in order if im not in big]
+
+    def one(im, n=1):
+        st, _ = oracle.decode(im.stream, scan, nthreads=n)
         assert st == 0
-    dt = time.perf_counter() - t0
-    return {"value": round(px / dt / 1e6, 2), "unit": "Mpix/s", "cores": threads, "kind": "port",
-            "sample": f"first {len(images)} images of the batched workload ({px / 1e6:.1f} Mpix), oracle decode "
-                      f"with {threads} threads, {dt:.2f} s"}
+
+    def run_pass(ex):
+        for im in big:
+            one(im, threads)
+        if ex is None:
+            for im in small:
+                one(im)
+        else:
+            list(ex.map(one, small))
+
+    times = []
+    with ThreadPoolExecutor(threads) if threads > 1 else _null_ctx() as ex:
+        for _ in range(warmup):
+            run_pass(ex)
+        for _ in range(passes):
+            t0 = time.perf_counter()
+            run_pass(ex)
+            times.append(time.perf_counter() - t0)
+    return px * passes / sum(times) / 1e6, times
+
+
+class _null_ctx:
+    def __enter__(self):
+        return None
+
+    def __exit__(self, *exc):
+        return False
+
+
+def cpu_baseline(images, single_images=None):
+    """The C oracle (restating the reference's CPU decode path: rANS groups as
+    ans::DecodeInterleaved, the inverse wavelet as InverseWavelet2D, the index
+    scan and DXT1 assembly) on the host: an all-core leg (one image per thread)
+    and a single-thread leg, each warmed up and timed over several passes."""
+    import oracle
+    threads = os.cpu_count() or 1
+    single_images = single_images if single_images is not None else images[: max(1, len(images) // 4)]
+    v_all, t_all = cpu_decode_rate(images, threads, 5, 1, oracle.SCAN_REFERENCE)
+    v_one, t_one = cpu_decode_rate(single_images, 1, 3, 1, oracle.SCAN_REFERENCE)
+    px = sum(im.pixels for im in images)
+    px1 = sum(im.pixels for im in single_images)
+    return {"value": round(v_all, 2), "unit": "Mpix/s", "cores": threads, "kind": "port",
+            "cpu_model": cpu_model(),
+            "sample": f"first {len(images)} images of the batched workload ({px / 1e6:.1f} Mpix), oracle decode, "
+                      f"{threads} threads (one image per thread), 1 warm-up + 5 timed passes "
+                      f"({statistics.mean(t_all):.3f} s each)",
+            "single_thread": {"value": round(v_one, 2), "unit": "Mpix/s", "cores": 1,
+                              "sample": f"first {len(single_images)} images ({px1 / 1e6:.1f} Mpix), 1 warm-up + 3 "
+                                        f"timed passes ({statistics.mean(t_one):.3f} s each)"}}
 
 
 def cpu_baseline_encode(images):
@@ -956,36 +1114,31 @@ def cpu_baseline_encode(images):
 
 
 def run_reference(args, rank, world):
-    """The reference's CPU decode path (the oracle port), all host threads."""
+    """The reference's CPU decode path (the oracle port), all host threads, on
+    the same images and with the same method as the GPU arm's cpu_baseline."""
     from gst_gb300 import workloads
     import oracle
     if rank != 0:
         return None
-    images = workloads.batched(64)[: args.cpu_sample]
+    images, encoder_name = bench_batch()
+    images = images[: args.cpu_sample]
     threads = os.cpu_count() or 1
-    oracle.load()
     px = sum(im.pixels for im in images)
-    for _ in range(max(1, min(args.warmup, 2))):
-        oracle.decode(images[0].stream, oracle.SCAN_REFERENCE, nthreads=threads)
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        for im in images:
-            st, _ = oracle.decode(im.stream, oracle.SCAN_REFERENCE, nthreads=threads)
-            assert st == 0
-        times.append(time.perf_counter() - t0)
+    value, times = cpu_decode_rate(images, threads, args.steps, max(1, min(args.warmup, 2)), oracle.SCAN_REFERENCE)
     total = sum(times)
-    value = px * args.steps / total / 1e6
+    single, t_one = cpu_decode_rate(images[: max(1, len(images) // 4)], 1, 2, 1, oracle.SCAN_REFERENCE)
     sample = (f"first {len(images)} of the 64 batched images ({px / 1e6:.1f} Mpix) per step, oracle port of the "
-              f"reference decoder, {threads} threads")
+              f"reference decoder, {threads} threads (one image per thread)")
     return {
         "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": "Mpix/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": "batched: 64 synthetic images, w,h in {512,1024,2048}, seeds 1000+i",
-                   "sample_images": len(images)},
+                   "encoder": encoder_name, "sample_images": len(images)},
         "cpu_baseline": {"value": round(value, 2), "unit": "Mpix/s", "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "cpu_model": cpu_model(), "sample": sample,
+                         "single_thread": {"value": round(single, 2), "unit": "Mpix/s", "cores": 1,
+                                           "sample": f"first {max(1, len(images) // 4)} images, 2 timed passes"}},
         "e2e": {"value": round(value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

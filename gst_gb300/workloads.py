@@ -13,12 +13,29 @@ available), so every workload is made here from a seed:
 * ``serving`` -- a pool of images per (w, h) class, w and h from
                  {512, 1024, 2048, 4096} with weights 0.4/0.3/0.2/0.1.
 
-Encoded streams are cached under gst_gb300/_cache/ (git-ignored) keyed by the
-encoder sources, so a rerun on the same machine skips the CPU encoding.
+Two producers make the streams:
+
+* the reference encoder itself (its ``gentenc`` path: stb_dxt high-quality
+  blocks, the Reencode index palette search, CompressDXT), run ahead of time by
+  tests/golden/make_ref_streams.py on the same seeded images; the streams and
+  SHA-256 digests of the blocks they decode to are committed under
+  tests/golden/ref_streams/ (``ref_*`` functions below).  These are the
+  benchmark inputs.
+* this project's CPU stream producer (csrc/gst_encoder.cpp), which runs
+  anywhere: its own DXT1 compressor and a palette search that keeps each
+  block's endpoints, so its streams are about half the size of the
+  reference's.  Tests that need streams of other sizes or seeds use it, and
+  the bench reports it as a labelled secondary input.  Its streams are cached
+  under gst_gb300/_cache/ (git-ignored) keyed by the encoder sources.
+
+A fixture image carries no decoded blocks (``blocks`` is None): the checker
+that compares a decode against them computes them and checks them against
+``decoded_sha256``.
 """
 from __future__ import annotations
 
 import hashlib
+import json
 import os
 from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass
@@ -30,6 +47,8 @@ from . import encoder
 from .build import ENCODER_SOURCES, ENCODER_HEADERS
 
 CACHE = Path(__file__).resolve().parent / "_cache"
+REF_STREAMS = Path(__file__).resolve().parent.parent / "tests" / "golden" / "ref_streams"
+REF_PLAIN = Path(__file__).resolve().parent.parent / "tests" / "golden" / "synth512_s0.gst"
 
 BATCH_DIMS = (512, 1024, 2048)
 SERVING_DIMS = (512, 1024, 2048, 4096)
@@ -42,8 +61,10 @@ class EncodedImage:
     height: int
     seed: int
     stream: bytes
-    blocks: np.ndarray  # uint64 per DXT1 block: what a correct decode must return
+    blocks: np.ndarray | None  # uint64 per DXT1 block: what a correct decode must return
     clips: int = 0      # wavelet coefficients that wrapped (their tiles are lossy)
+    encoder: str = "gst_gb300 stream producer"
+    decoded_sha256: str | None = None  # reference-encoded fixtures: digest of the decoded blocks
 
     @property
     def pixels(self) -> int:
@@ -136,3 +157,64 @@ def rans_section(n: int = 1 << 26, b: float = 6.0, seed: int = 7) -> RansSection
     tmp.write_bytes(sec)
     tmp.replace(sp)
     return RansSection(sym, sec)
+
+
+# ---------------------------------------------------------------------------
+# Streams made by the reference encoder (tests/golden/make_ref_streams.py).
+REF_ENCODER = "reference gentenc (stb_dxt HIGHQUAL + Reencode + CompressDXT)"
+
+
+def ref_available() -> bool:
+    return (REF_STREAMS / "manifest.json").exists()
+
+
+def ref_manifest() -> dict:
+    p = REF_STREAMS / "manifest.json"
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: run tests/golden/make_ref_streams.py where the reference is mounted")
+    return json.loads(p.read_text())
+
+
+def _ref_image(entry: dict) -> EncodedImage:
+    stream = (REF_STREAMS / entry["name"]).read_bytes()
+    if hashlib.sha256(stream).hexdigest() != entry["stream_sha256"]:
+        raise ValueError(f"{entry['name']}: stream does not match its manifest digest")
+    return EncodedImage(entry["width"], entry["height"], entry["seed"], stream, None,
+                        encoder=REF_ENCODER, decoded_sha256=entry["decoded_sha256"])
+
+
+def ref_batched() -> list[EncodedImage]:
+    """The 64 batched images (w, h in {512, 1024, 2048}, seeds 1000 + i), in
+    batch order, as the reference encoder wrote them."""
+    ents = [e for e in ref_manifest()["streams"] if e["kind"] == "batched"]
+    ents.sort(key=lambda e: e["seed"])
+    return [_ref_image(e) for e in ents]
+
+
+def ref_large() -> EncodedImage:
+    """The 8192x8192 texture with 10 % of its area in 1-8 px checker regions."""
+    (e,) = [e for e in ref_manifest()["streams"] if e["kind"] == "large"]
+    return _ref_image(e)
+
+
+def ref_plain() -> EncodedImage:
+    """The 512x512 image of seed 0 (tests/golden/synth512_s0.gst)."""
+    m = ref_manifest()["plain"]
+    gold = json.loads((REF_PLAIN.parent / "golden.json").read_text())["streams"][REF_PLAIN.name]
+    return EncodedImage(m["width"], m["height"], m["seed"], REF_PLAIN.read_bytes(), None, encoder=REF_ENCODER,
+                        decoded_sha256=gold["blocks_sha256"])
+
+
+def ref_serving_pool() -> dict[tuple[int, int], list[EncodedImage]]:
+    """Every (w, h) class, w and h in {512, 1024, 2048, 4096}: the serving
+    fixtures plus the batched images of that class (at least four each)."""
+    pool: dict[tuple[int, int], list[EncodedImage]] = {}
+    for e in ref_manifest()["streams"]:
+        if e["kind"] in ("batched", "serving"):
+            pool.setdefault((e["width"], e["height"]), []).append(_ref_image(e))
+    return pool
+
+
+def ref_rans_digest() -> dict:
+    """SHA-256 of the reference ByteEncoder's section for rans_section()'s symbols."""
+    return ref_manifest()["rans_2pow26"]

@@ -11,7 +11,7 @@
 //     slot), then each warp decodes one group of 32 interleaved streams x 256
 //     symbols: the 32 lanes are the 32 streams, a warp ballot + popcount gives
 //     each renormalising lane its read offset (the reference uses local-memory
-//     atomics and two barriers per symbol, ans_decode.cl:126-145).  Symbols go
+//     atomics and two barriers per symbol, ans_decode.cl:43-65).  Symbols go
 //     out 16 at a time as 128-bit stores.  Warps of the index section also
 //     produce the palette-index prefix sums at 32-block granularity; the last
 //     index warp of an image turns the per-group sums into group prefixes
@@ -218,7 +218,7 @@ __device__ __forceinline__ uint32_t mul_hi(uint32_t a, uint32_t b) {
 //   e' = e mod 2^24 (the freq << 11 term cancels), and the slot's byte offset
 //   4x - 8192 q, all as multiply-adds.  Renormalising lanes read consecutive
 //   words below the read pointer, the lowest lane the lowest address
-//   (ans_decode.cl:133-140): lane l's word lies popc(renormalising lanes >= l)
+//   (ans_decode.cl:50-57): lane l's word lies popc(renormalising lanes >= l)
 //   words below the pointer, and only those lanes load it from the stage.
 // For a valid stream the read pointer never goes below the staged words; a
 // malformed one is caught at the end of a 16-step run (the pointer is then
@@ -279,7 +279,7 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
       }
       s2 = mad_lo(static_cast<uint32_t>(__popc(m)), 0u - 2u, s2);
       // Steps 16k..16k+15 are positions 255-16k .. 240-16k of this stream
-      // (ans_decode.cl:154-155 stores the symbols in reverse).
+      // (ans_decode.cl:71-72 stores the symbols in reverse).
       if constexpr (INDEX) {
         const uint32_t part = static_cast<uint32_t>(crun) & 0xFFFFu;
         crun += static_cast<int32_t>(e >> 24) - 128;
@@ -953,10 +953,9 @@ namespace gst {
 //
 // Who needs it: callers that must not allocate device memory at decode time.
 // cudaMalloc and cudaFree can synchronise the whole device, which a render or
-// texture-streaming thread with a per-frame time budget cannot afford; neither
-// call may be made while the caller's stream is being captured into a CUDA
-// graph; and some engines hand out all device memory from their own fixed pools
-// and forbid anyone else to allocate.  Such callers cannot create a gst_ctx
+// texture-streaming thread with a per-frame time budget cannot afford; and
+// some engines hand out all device memory from their own fixed pools and
+// forbid anyone else to allocate.  Such callers cannot create a gst_ctx
 // (it allocates its scratch, plan buffers and events), so this entry point
 // needs no context: its scratch is g_static_scratch below, a file-scope device
 // array that is part of this library's image and is held by every GPU that
@@ -967,6 +966,8 @@ namespace gst {
 //    + B/8 + 8*B/8192 bytes must fit (B = w*h/16); that is at most 2048x2048
 //    with a typical palette.  Larger images are rejected with GST_E_ARG before
 //    anything is enqueued.
+//  * Malformed payloads are reported only through device_status: with it null
+//    the kernels' error bits stay in the array and the call returns GST_OK.
 //  * Every call uses the same array and leaves its contents behind.  Each call
 //    clears, on its stream, the words that must start at zero (the device
 //    status word and the index-group counter); the rest is fully rewritten
@@ -1018,6 +1019,7 @@ __global__ void __launch_bounds__(256) gst_tile_static_kernel(const uint8_t *bas
 #include <mutex>
 
 #include "gst_decoder.h"
+#include "gst_host.h"
 
 namespace {
 
@@ -1052,18 +1054,11 @@ extern "C" gst_status gst_load_compressed_dxt_static(const gst_header *hdr, cons
   if (!hdr || !d_cmp || !d_out) return GST_E_ARG;
   if ((reinterpret_cast<uintptr_t>(d_cmp) & 15) || (reinterpret_cast<uintptr_t>(d_out) & 7)) return GST_E_ARG;
   const gst_header &h = *hdr;
-  // The header rules of gst_parse_header (README.md:67-71 of the reference).
-  if (h.width == 0 || h.height == 0 || h.width % 128 || h.height % 128) return GST_E_FORMAT;
-  const uint64_t px = uint64_t(h.width) * h.height;
-  if (px % (16u * 256u * 32u)) return GST_E_FORMAT;
-  const uint64_t B = px / 16;
-  if (h.palette_bytes == 0 || h.palette_bytes % kSymsPerGroup) return GST_E_FORMAT;
+  // The header rules every decode call applies (gst_parse_header's).
+  if (host::check_header(h) != GST_OK) return GST_E_FORMAT;
+  const uint64_t B = uint64_t(h.width) * h.height / 16;
   const uint32_t lens[4] = {h.y_cmp_sz, h.chroma_cmp_sz, h.palette_sz, h.indices_sz};
   const uint64_t syms[4] = {2 * B, 4 * B, h.palette_bytes, B};
-  for (int s = 0; s < 4; ++s) {
-    const uint64_t G = syms[s] / kSymsPerGroup;
-    if (lens[s] % 4 || G * (4 + 4 * kStreamsPerGroup) > lens[s]) return GST_E_FORMAT;
-  }
   // Scratch inside the static array: symbols, chunk prefixes, group sums.
   auto up = [](uint64_t x) { return (x + 255) / 256 * 256; };
   const uint64_t sym_bytes = up(8 * B + h.palette_bytes), chunk_bytes = up(B / 32 * 4);
@@ -1100,11 +1095,23 @@ extern "C" gst_status gst_load_compressed_dxt_static(const gst_header *hdr, cons
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // Words that must start at zero: the status word and the index-group counter.
+  // Each call below reports its own error (a launch through cudaLaunchKernelEx
+  // returns the launch's status), so an error left pending by unrelated earlier
+  // work is neither cleared nor reported as this call's.
   if (cudaMemsetAsync(base, 0, 8, s) != cudaSuccess) return GST_E_CUDA;
-  gst_rans_static_kernel<<<rans_ctas, 128, rans_smem_bytes(kDefaultStageWords), s>>>(
-      static_cast<const uint8_t *>(d_cmp), base, im);
-  gst_tile_static_kernel<<<uint32_t(B / 1024), 256, 0, s>>>(base, static_cast<uint8_t *>(d_out), im);
-  if (cudaGetLastError() != cudaSuccess) return GST_E_CUDA;
+  cudaLaunchConfig_t cfg = {};
+  cfg.stream = s;
+  cfg.gridDim = dim3(rans_ctas);
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = rans_smem_bytes(kDefaultStageWords);
+  const uint8_t *cmp = static_cast<const uint8_t *>(d_cmp);
+  if (cudaLaunchKernelEx(&cfg, gst_rans_static_kernel, cmp, base, im) != cudaSuccess) return GST_E_CUDA;
+  cfg.gridDim = dim3(uint32_t(B / 1024));
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  const uint8_t *cbase = base;
+  if (cudaLaunchKernelEx(&cfg, gst_tile_static_kernel, cbase, static_cast<uint8_t *>(d_out), im) != cudaSuccess)
+    return GST_E_CUDA;
   if (device_status) {
     if (cudaStreamSynchronize(s) != cudaSuccess) return GST_E_CUDA;
     uint32_t bits = 0;

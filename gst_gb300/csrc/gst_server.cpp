@@ -144,11 +144,13 @@ struct gst_server {
 
   // statistics since the last reset
   std::vector<double> lat_us;
-  uint64_t submitted = 0, completed = 0, rejected = 0, launches = 0, launched_images = 0, pixels = 0;
+  uint64_t submitted = 0, completed = 0, rejected = 0, cancelled = 0, launches = 0, launched_images = 0, pixels = 0;
   uint64_t t_stats = 0;
   size_t dev_peak = 0;
 
-  // open-loop submissions from a native thread (gst_server_schedule)
+  // open-loop submissions from a native thread (gst_server_schedule); sched_mu
+  // guards the thread object against concurrent schedule / schedule_wait calls
+  std::mutex sched_mu;
   std::thread sched;
   std::atomic<bool> sched_stop{false};
   int sched_submitted = 0, sched_rejected = 0;
@@ -417,9 +419,12 @@ gst_status gst_server_create(gst_ctx *ctx, const gst_server_config *cfg, gst_ser
 
 void gst_server_destroy(gst_server *srv) {
   if (!srv) return;
-  if (srv->sched.joinable()) {
-    srv->sched_stop = true;
-    srv->sched.join();
+  {
+    std::lock_guard<std::mutex> sl(srv->sched_mu);
+    if (srv->sched.joinable()) {
+      srv->sched_stop = true;
+      srv->sched.join();
+    }
   }
   if (srv->thread.joinable()) {
     {
@@ -484,6 +489,7 @@ gst_status gst_server_submit(gst_server *srv, const void *gst, size_t len, uint6
 gst_status gst_server_schedule(gst_server *srv, int n, const void *const *gst, const size_t *len,
                                const uint64_t *arrival_ns, uint64_t *ids) {
   if (!srv || n < 0 || (n > 0 && (!gst || !len || !arrival_ns || !ids))) return GST_E_ARG;
+  std::lock_guard<std::mutex> sl(srv->sched_mu);
   if (srv->sched.joinable()) return GST_E_ARG;  // one schedule at a time: wait for the last one first
   srv->sched_stop = false;
   srv->sched = std::thread([srv, n, gst, len, arrival_ns, ids] {
@@ -525,7 +531,9 @@ gst_status gst_server_schedule(gst_server *srv, int n, const void *const *gst, c
 }
 
 gst_status gst_server_schedule_wait(gst_server *srv, int *submitted, int *rejected, uint64_t *late_max_ns) {
-  if (!srv || !srv->sched.joinable()) return GST_E_ARG;
+  if (!srv) return GST_E_ARG;
+  std::lock_guard<std::mutex> sl(srv->sched_mu);
+  if (!srv->sched.joinable()) return GST_E_ARG;
   srv->sched.join();
   std::lock_guard<std::mutex> lk(srv->mu);
   if (submitted) *submitted = srv->sched_submitted;
@@ -586,6 +594,32 @@ gst_status gst_server_release(gst_server *srv, uint64_t id) {
   return GST_OK;
 }
 
+gst_status gst_server_cancel(gst_server *srv, uint64_t id) {
+  if (!srv) return GST_E_ARG;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto it = srv->reqs.find(id);
+    if (it == srv->reqs.end()) return GST_E_ARG;
+    Request &r = it->second;
+    std::deque<uint64_t> *q = nullptr;
+    if (r.state == State::kQueued) q = &srv->queued;
+    else if (r.state == State::kAdmitted) q = &srv->admitted;
+    else return GST_E_ARG;  // launched or done: it completes normally
+    auto pos = std::find(q->begin(), q->end(), id);
+    if (pos == q->end()) return GST_E_ARG;
+    q->erase(pos);
+    if (r.state == State::kAdmitted) {
+      srv->dev_arena.release(r.in_off, r.len);
+      srv->dev_arena.release(r.out_off, dxt_bytes(r.hdr));
+    }
+    srv->host_arena.release(r.host_off, r.len);
+    srv->reqs.erase(it);
+    ++srv->cancelled;
+  }
+  srv->cv.notify_one();  // staging or budget freed: the scheduler may admit more
+  return GST_OK;
+}
+
 gst_status gst_server_read_stats(gst_server *srv, gst_server_stats *st, int reset) {
   if (!srv || !st) return GST_E_ARG;
   std::lock_guard<std::mutex> lk(srv->mu);
@@ -593,6 +627,7 @@ gst_status gst_server_read_stats(gst_server *srv, gst_server_stats *st, int rese
   st->submitted = srv->submitted;
   st->completed = srv->completed;
   st->rejected = srv->rejected;
+  st->cancelled = srv->cancelled;
   st->launches = srv->launches;
   st->launched_images = srv->launched_images;
   st->pixels = srv->pixels;
@@ -617,7 +652,8 @@ gst_status gst_server_read_stats(gst_server *srv, gst_server_stats *st, int rese
   }
   if (reset) {
     srv->lat_us.clear();
-    srv->submitted = srv->completed = srv->rejected = srv->launches = srv->launched_images = srv->pixels = 0;
+    srv->submitted = srv->completed = srv->rejected = srv->cancelled = srv->launches = srv->launched_images =
+        srv->pixels = 0;
     srv->dev_peak = srv->dev_arena.used();
     srv->t_stats = t;
   }

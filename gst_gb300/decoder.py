@@ -49,7 +49,7 @@ EXPORTED_SYMBOLS = (
     "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times", "gst_set_option",
     "gst_status_string",
     "gst_server_create", "gst_server_destroy", "gst_server_now_ns", "gst_server_submit", "gst_server_poll",
-    "gst_server_read", "gst_server_release", "gst_server_read_stats", "gst_server_schedule",
+    "gst_server_read", "gst_server_release", "gst_server_cancel", "gst_server_read_stats", "gst_server_schedule",
     "gst_server_schedule_wait",
     # include/gst_encode.h
     "gst_encode_section_bound", "gst_encode_stream_bound", "gst_encode_bytes", "gst_encode_streams",
@@ -86,7 +86,8 @@ class ServerStats(ctypes.Structure):
                                                 "pixels", "queued")] + \
                [("device_bytes_in_use", ctypes.c_size_t), ("device_bytes_peak", ctypes.c_size_t)] + \
                [(n, ctypes.c_double) for n in ("seconds", "latency_mean_us", "latency_p50_us", "latency_p99_us",
-                                                "latency_max_us")]
+                                                "latency_max_us")] + \
+               [("cancelled", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -201,6 +202,7 @@ def load_library() -> ctypes.CDLL:
         "gst_server_poll": (I, [P, ctypes.POINTER(ServerResult), I, ctypes.POINTER(I), I]),
         "gst_server_read": (I, [P, ctypes.c_uint64, P, S]),
         "gst_server_release": (I, [P, ctypes.c_uint64]),
+        "gst_server_cancel": (I, [P, ctypes.c_uint64]),
         "gst_server_read_stats": (I, [P, ctypes.POINTER(ServerStats), I]),
         "gst_server_schedule": (I, [P, I, P, P, P, P]),
         "gst_server_schedule_wait": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(ctypes.c_uint64)]),

@@ -95,6 +95,12 @@ class DecodeServer:
         _check(st, "gst_server_schedule_wait")
         return sub.value, rej.value, late.value
 
+    def cancel(self, rid: int) -> bool:
+        """Withdraws a request that has not been launched yet; False if it
+        already was (it then completes normally) or the id is unknown."""
+        st = load_library().gst_server_cancel(self._h, rid)
+        return st == GST_OK
+
     def stats(self, reset: bool = False) -> dict:
         st = ServerStats()
         _check(load_library().gst_server_read_stats(self._h, ctypes.byref(st), int(reset)), "gst_server_read_stats")

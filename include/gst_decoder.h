@@ -194,9 +194,8 @@ gst_status gst_autotune_class(gst_ctx *ctx, const gst_header *hdrs, int n, const
  * the reference, which allocates its decoder scratch per call or through
  * PreallocateDecompressor.  For callers that must not allocate device memory
  * while they decode: a render or streaming thread that cannot absorb the
- * device-wide synchronisation cudaMalloc/cudaFree may cause, code running while
- * its stream is being captured into a CUDA graph, or an engine that owns all
- * device memory through its own pools.  It needs no gst_ctx (creating one
+ * device-wide synchronisation cudaMalloc/cudaFree may cause, or an engine that
+ * owns all device memory through its own pools.  It needs no gst_ctx (creating one
  * allocates).  Input and output are the caller's, as for
  * gst_load_compressed_dxt; the scratch is a 4 MiB array built into the library,
  * held by every GPU that loads the library until the process exits.
@@ -209,7 +208,9 @@ gst_status gst_autotune_class(gst_ctx *ctx, const gst_header *hdrs, int n, const
  *   - The first call on a device looks up the array's address on that device;
  *     make it before any stream capture there.
  *   - With device_status non-null the call waits for `stream` and stores the
- *     kernels' error bits there (0 when the stream was well formed). */
+ *     kernels' error bits there (0 when the stream was well formed).  With
+ *     device_status null nothing reports a malformed payload: the call returns
+ *     GST_OK once the work is enqueued and the output is then undefined. */
 gst_status gst_load_compressed_dxt_static(const gst_header *hdr, const void *d_cmp, void *d_out, void *stream,
                                           uint32_t *device_status);
 
@@ -305,6 +306,11 @@ gst_status gst_set_option(gst_ctx *ctx, const char *name, int value);
  *     the first); each result's DXT1 blocks stay resident on the device at
  *     d_dxt until gst_server_release, which returns its memory to the budget.
  *     gst_server_read copies one result to host memory (blocking).
+ *   - gst_server_cancel withdraws a request that has not been launched yet
+ *     (queued, or admitted and waiting for a slot): its staging and device
+ *     memory return at once and it never appears in gst_server_poll.
+ *     GST_E_ARG for an unknown id or a request already launched (that one
+ *     completes normally and is released after polling).
  *   - gst_server_read_stats reports counts and submit-to-finish latency
  *     percentiles since the last reset (reset != 0 starts a new period).
  *   - gst_server_destroy waits for the launches in flight and drops requests
@@ -332,6 +338,7 @@ typedef struct {
   size_t device_bytes_in_use, device_bytes_peak;
   double seconds; /* length of the statistics period */
   double latency_mean_us, latency_p50_us, latency_p99_us, latency_max_us;
+  uint64_t cancelled; /* requests withdrawn by gst_server_cancel */
 } gst_server_stats;
 gst_status gst_server_create(gst_ctx *ctx, const gst_server_config *cfg, gst_server **server);
 void gst_server_destroy(gst_server *server);
@@ -340,6 +347,7 @@ gst_status gst_server_submit(gst_server *server, const void *gst, size_t len, ui
 gst_status gst_server_poll(gst_server *server, gst_server_result *out, int cap, int *n, int wait_us);
 gst_status gst_server_read(gst_server *server, uint64_t id, void *dst, size_t cap);
 gst_status gst_server_release(gst_server *server, uint64_t id);
+gst_status gst_server_cancel(gst_server *server, uint64_t id);
 gst_status gst_server_read_stats(gst_server *server, gst_server_stats *stats, int reset);
 
 /* Open-loop load from a native thread, so that no stall of the caller delays
@@ -352,7 +360,8 @@ gst_status gst_server_read_stats(gst_server *server, gst_server_stats *stats, in
  * the streams, len, arrival_ns and ids alive until gst_server_schedule_wait,
  * which joins the thread and returns the submitted and refused counts and the
  * worst lateness of a submission behind its arrival.  One schedule at a time
- * (GST_E_ARG otherwise); gst_server_destroy stops a running one. */
+ * (GST_E_ARG otherwise; concurrent calls from several threads are safe);
+ * gst_server_destroy stops a running one. */
 gst_status gst_server_schedule(gst_server *server, int n, const void *const *gst, const size_t *len,
                                const uint64_t *arrival_ns, uint64_t *ids);
 gst_status gst_server_schedule_wait(gst_server *server, int *submitted, int *rejected, uint64_t *late_max_ns);

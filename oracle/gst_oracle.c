@@ -282,7 +282,7 @@ static void scan_reference(const uint8_t *deltas, uint32_t n, int32_t *out_i) {
     const uint32_t lsize = num < 128 ? num : 128;
     const uint32_t idx_offset = 1u << (stage * 7);
     /* Work-groups run one after another in id order (one legal interleaving;
-     * for the sizes where the kernel's writes alias, decode_indices.cl:217-255
+     * for the sizes where the kernel's writes alias, decode_indices.cl:58-63
      * gives no ordering guarantee). */
     for (uint32_t g0 = 0; g0 < gsize; g0 += lsize) {
       uint32_t s[128];
@@ -599,7 +599,7 @@ int gsto_decode_batch(const uint8_t *const *gst, const size_t *lens, int n_strea
   return status;
 }
 
-/* ans_decode.cl:185-204 */
+/* ans_decode.cl:104-121 (the binary search of ans_decode_multiple) */
 uint32_t gsto_section_search(const uint32_t *oo, uint32_t num_offsets, uint32_t wg) {
   const uint32_t id = wg * GSTO_STREAMS_PER_GROUP * GSTO_SYMS_PER_STREAM;
   uint32_t low = 0, high = num_offsets - 1, x = (high + low) / 2;

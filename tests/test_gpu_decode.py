@@ -47,6 +47,29 @@ def test_decompress_dxt_golden(gpu_ctx, golden, name):
     assert np.array_equal(out, ref)
 
 
+@pytest.mark.skipif(not workloads.ref_available(), reason="reference-encoded fixtures not present")
+def test_reference_encoded_workloads(gpu_ctx):
+    """The benchmark inputs as the reference encoder (gentenc's path) wrote
+    them: the 64-image batch in one call (two-kernel and persistent forms),
+    the 8192x8192 texture, and every serving-pool stream alone, each
+    bit-exact against the digest of the reference decoder's blocks."""
+    imgs = workloads.ref_batched()
+    for persistent in (0, 1):
+        gpu_ctx.set_option("persistent", persistent)
+        try:
+            st, outs = batch_decode(gpu_ctx, [im.stream for im in imgs])
+        finally:
+            gpu_ctx.set_option("persistent", 0)
+        assert st == decoder.GST_OK
+        for im, o in zip(imgs, outs):
+            assert SHA(o) == im.decoded_sha256, (im.width, im.height, im.seed, persistent)
+    big = workloads.ref_large()
+    assert SHA(decoder.decompress_dxt(gpu_ctx, big.stream)) == big.decoded_sha256
+    for ims in workloads.ref_serving_pool().values():
+        for im in ims:
+            assert SHA(decoder.decompress_dxt(gpu_ctx, im.stream)) == im.decoded_sha256
+
+
 def test_non_power_of_two_block_count_matches_encoder(gpu_ctx, golden):
     # The GPU computes the exact index prefix sum: it reproduces the encoder's
     # blocks, where the reference's staged scan differs in the last block.

@@ -113,7 +113,7 @@ def _search_mismatches(oo, total):
 
 @pytest.mark.parametrize("n", [1, 2, 4, 8, 16, 32, 64])
 def test_section_search_exact_for_power_of_two_batches(n):
-    # ans_decode.cl:185-204 assigns every work-group its true section when the
+    # ans_decode.cl:104-121 assigns every work-group its true section when the
     # batch has a power-of-two number of images (the 64-image workload).
     rng = np.random.default_rng(n)
     for _ in range(5):
@@ -226,7 +226,7 @@ def test_rans_stage_matches_reference_decode_interleaved(ref):
 
 
 def test_wavelet_matches_reference_inverse_wavelet2d(ref):
-    # Per 32x32 block: oracle == InverseWavelet2D at dims 2..32 (codec/wavelet.cpp:159-181)
+    # Per 32x32 block: oracle == InverseWavelet2D at dims 2..32 (codec/wavelet.cpp:133-155)
     # on valid coefficient data (where the reference's int16 never overflows).
     s = golden_stream("synth512_s0.gst")
     st, syms = oracle.decode_symbols(s)

@@ -85,6 +85,38 @@ def test_admission_waits_for_released_memory(gpu_ctx):
         assert srv.stats()["device_bytes_peak"] <= budget
 
 
+def test_cancel_queued_request(gpu_ctx):
+    """gst_server_cancel withdraws a request that waits for device memory: its
+    memory returns at once, it never completes, the rest decode bit-exactly;
+    a request already launched cannot be cancelled."""
+    im = workloads.encode_image(2048, 2048, 950)
+    need = -(-len(im.stream) // 256) * 256 + im.blocks.size * 8
+    budget = 2 * need + 1024  # room for two requests, not three
+    with DecodeServer(gpu_ctx, device_budget_bytes=budget, max_inflight=2, max_batch_images=4) as srv:
+        ids = [srv.submit(im.stream) for _ in range(5)]
+        assert None not in ids
+        first = []
+        deadline = time.monotonic() + 30
+        while len(first) < 2 and time.monotonic() < deadline:
+            first += srv.poll(20000)
+        assert len(first) == 2 and srv.stats()["queued"] == 3
+        done_ids = {r.id for r in first}
+        assert not srv.cancel(first[0].id)  # done: not cancellable
+        queued = [i for i in ids if i not in done_ids]
+        assert srv.cancel(queued[1])
+        assert not srv.cancel(queued[1])  # gone
+        st = srv.stats()
+        assert st["queued"] == 2 and st["cancelled"] == 1
+        for r in first:
+            srv.release(r.id)
+        rest = collect(srv, 2)
+        assert set(rest) == {queued[0], queued[2]}
+        for status, out in rest.values():
+            assert status == decoder.GST_OK and np.array_equal(out.view(np.uint64), im.blocks)
+        time.sleep(0.05)
+        assert srv.poll(0) == [] and srv.stats()["completed"] == 4
+
+
 def _device_detected_corruption():
     # A payload flip that passes host validation and that the oracle reports
     # as malformed (a read leaves its group or the palette).

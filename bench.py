@@ -75,7 +75,7 @@ def parse_args():
     p.add_argument("--serve-plain-seconds", type=float, default=5.0,
                    help="length of each run of the per-request plain-decode comparison (it saturates near 10k "
                         "req/s, so its 20k req/s queue only grows with the run)")
-    p.add_argument("--serve-bound-budget-mib", type=int, default=256,
+    p.add_argument("--serve-bound-budget-mib", type=int, default=24,
                    help="device budget of the extra 20k req/s run in which admission binds (0: skip it)")
     p.add_argument("--serve-rates", default="1000,5000,20000", help="Poisson arrival rates, requests/s")
     p.add_argument("--serve-class-tune", type=int, default=1,

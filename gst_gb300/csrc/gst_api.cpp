@@ -10,8 +10,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "gst_host.h"
@@ -565,6 +568,10 @@ gst_status gst_init(int device, gst_ctx **out) {
     gst_destroy(ctx);
     return GST_E_CUDA;
   }
+  // A persisted per-size-class table, where one is named and matches this
+  // device; a missing or foreign table leaves the built-in configuration.
+  const char *table = std::getenv("GST_TUNING_TABLE");
+  if (table && *table) gst_load_class_tuning(ctx, table);
   *out = ctx;
   return GST_OK;
 }
@@ -821,6 +828,7 @@ gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const
   // each chunk's plan travels with its data instead of behind later chunks.
   // 1. Copy in each chunk's tables, sections (two contiguous ranges) and plan.
   PlanBuf *pbs[kPlanRing] = {};
+  nvtxRangePushA("gst copy in");
   for (int c = 0; c < nc && e == cudaSuccess; ++c) {
     const int i0 = cut[c], i1 = cut[c + 1], m = i1 - i0;
     const size_t t0 = page + size_t(i0) * 4 * kFreqTableBytes, t1 = page + size_t(i1) * 4 * kFreqTableBytes;
@@ -836,13 +844,18 @@ gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const
       oa[k] = reinterpret_cast<uint64_t>(ctx->hs_out_d + out[i0 + k]);
     }
     st = acquire_plan(ctx, lay[c].bytes, ctx->hs_in, false, &pbs[c]);
-    if (st != GST_OK) return st;
+    if (st != GST_OK) {
+      nvtxRangePop();
+      return st;
+    }
     write_plan(lay[c], hdrs + i0, m, pbs[c]->h, fa.data(), ba.data(), oa.data());
     e = cudaMemcpyAsync(pbs[c]->d, pbs[c]->h, lay[c].bytes, cudaMemcpyHostToDevice, ctx->hs_in);
     if (e == cudaSuccess) e = cudaEventRecord(pbs[c]->copied, ctx->hs_in);
     if (e == cudaSuccess) e = cudaEventRecord(ctx->hs_copied[c], ctx->hs_in);
   }
+  nvtxRangePop();
   // 2. Decode each chunk once it is in.
+  nvtxRangePushA("gst decode");
   for (int c = 0; c < nc && e == cudaSuccess; ++c) {
     e = cudaStreamWaitEvent(ctx->hs_comp, ctx->hs_copied[c], 0);
     if (e != cudaSuccess) break;
@@ -856,7 +869,9 @@ gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const
     pbs[c]->used = true;
     if (e == cudaSuccess) e = cudaEventRecord(ctx->hs_decoded[c], ctx->hs_comp);
   }
+  nvtxRangePop();
   // 3. Copy each chunk's blocks out once decoded.
+  nvtxRangePushA("gst copy out");
   for (int c = 0; c < nc && e == cudaSuccess; ++c) {
     const int i0 = cut[c], i1 = cut[c + 1];
     e = cudaStreamWaitEvent(ctx->hs_out, ctx->hs_decoded[c], 0);
@@ -864,6 +879,7 @@ gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const
       e = cudaMemcpyAsync(ho + out[i0], ctx->hs_out_d + out[i0], out[i1] - out[i0], cudaMemcpyDeviceToHost,
                           ctx->hs_out);
   }
+  nvtxRangePop();
   if (e != cudaSuccess) return cuda_status(e);
   cudaEventRecord(ctx->scratch_done, ctx->hs_comp);
   ctx->scratch_stream = ctx->hs_comp;
@@ -897,11 +913,18 @@ gst_status gst_decompress_dxt(gst_ctx *ctx, const uint8_t *gst, size_t len, uint
   cudaStreamSynchronize(s);  // the pinned staging buffers may still feed the previous call
   memset(ctx->cmp_h, 0, 512);
   memcpy(ctx->cmp_h + 512, gst + 28, body - 28);
-  cudaError_t e = cudaMemcpyAsync(ctx->cmp_d, ctx->cmp_h, cmp_bytes, cudaMemcpyHostToDevice, s);
+  cudaError_t e;
+  {
+    NvtxRange range("gst copy in");
+    e = cudaMemcpyAsync(ctx->cmp_d, ctx->cmp_h, cmp_bytes, cudaMemcpyHostToDevice, s);
+  }
   if (e != cudaSuccess) return cuda_status(e);
   st = decode_batch(ctx, &h, 1, ctx->cmp_d, ctx->out_d, s);
   if (st != GST_OK) return st;
-  e = cudaMemcpyAsync(ctx->out_h, ctx->out_d, out_bytes, cudaMemcpyDeviceToHost, s);
+  {
+    NvtxRange range("gst copy out");
+    e = cudaMemcpyAsync(ctx->out_h, ctx->out_d, out_bytes, cudaMemcpyDeviceToHost, s);
+  }
   if (e != cudaSuccess) return cuda_status(e);
   st = read_device_status(ctx, s);
   memcpy(dxt_out, ctx->out_h, out_bytes);
@@ -1146,6 +1169,7 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
     if (e == cudaSuccess) e = cudaEventRecord(fork, cs);
     for (cudaStream_t s : {si, sc, so})
       if (e == cudaSuccess) e = cudaStreamWaitEvent(s, fork, 0);
+    nvtxRangePushA("gst copy in");
     for (int c = 0; c < nc && e == cudaSuccess; ++c) {
       const int i0 = b->hm_cut[c], i1 = b->hm_cut[c + 1];
       const size_t t0 = page + size_t(i0) * 4 * kFreqTableBytes, t1 = page + size_t(i1) * 4 * kFreqTableBytes;
@@ -1154,6 +1178,8 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
         e = cudaMemcpyAsync(b->hm_cmp + body[i0], hc + body[i0], body[i1] - body[i0], cudaMemcpyHostToDevice, si);
       if (e == cudaSuccess) e = cudaEventRecord(evs[c], si);
     }
+    nvtxRangePop();
+    nvtxRangePushA("gst decode");
     for (int c = 0; c < nc && e == cudaSuccess; ++c) {
       e = cudaStreamWaitEvent(sc, evs[c], 0);
       GstPlanView view = plan_view(b->hm_lay[c], b->hm_plans + b->hm_plan_off[c], ctx->status_d);
@@ -1163,12 +1189,15 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
       if (e == cudaSuccess) e = launch_decode(nullptr, b->scratch, nullptr, view, sc, &launches, nullptr, tuning);
       if (e == cudaSuccess) e = cudaEventRecord(evs[nc + c], sc);
     }
+    nvtxRangePop();
+    nvtxRangePushA("gst copy out");
     for (int c = 0; c < nc && e == cudaSuccess; ++c) {
       const int i0 = b->hm_cut[c], i1 = b->hm_cut[c + 1];
       e = cudaStreamWaitEvent(so, evs[nc + c], 0);
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(ho + out[i0], b->hm_out + out[i0], out[i1] - out[i0], cudaMemcpyDeviceToHost, so);
     }
+    nvtxRangePop();
     if (e == cudaSuccess) e = cudaEventRecord(end_i, si);
     if (e == cudaSuccess) e = cudaEventRecord(end_c, sc);
     if (e == cudaSuccess) e = cudaEventRecord(end_o, so);
@@ -1300,7 +1329,137 @@ gst_status gst_autotune_class(gst_ctx *ctx, const gst_header *hdrs, int n, const
   if (st != GST_OK) return st;
   st = gst_set_class_tuning(ctx, c, bps, words, pers);
   if (st == GST_OK && size_class_out) *size_class_out = c;
+  // The winner goes into the persisted table as well, where one is named.
+  const char *table = std::getenv("GST_TUNING_TABLE");
+  if (st == GST_OK && table && *table) st = gst_save_class_tuning(ctx, table);
   return st;
+}
+
+// ---------------------------------------------------------------------------
+// The per-size-class tuning as a JSON table, so that the autotuner's choices
+// outlive the process:
+//   {"format": "gst_gb300 class tuning", "version": 1, "device": "<name>",
+//    "classes": [{"class": c, "max_blocks": m, "blocks_per_sm": b,
+//                 "stage_words": w, "persistent": p}, ...]}
+// Only the classes that are set are written ("max_blocks" is informative:
+// the class's upper bound in DXT1 blocks, 0 for the open-ended last one).
+namespace {
+
+std::string device_name(int device) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return "";
+  std::string n;
+  for (const char *c = prop.name; *c; ++c)
+    if (*c != '"' && *c != '\\') n += *c;  // kept JSON-safe
+  return n;
+}
+
+// The text after `"key":` (spaces skipped) in [at, end), or nullptr.
+const char *json_value(const char *at, const char *end, const char *key) {
+  const std::string k = std::string("\"") + key + "\"";
+  const char *p = std::search(at, end, k.begin(), k.end());
+  if (p == end) return nullptr;
+  p += k.size();
+  while (p < end && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r')) ++p;
+  if (p == end || *p != ':') return nullptr;
+  ++p;
+  while (p < end && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r')) ++p;
+  return p < end ? p : nullptr;
+}
+
+bool json_int(const char *at, const char *end, const char *key, long *out) {
+  const char *p = json_value(at, end, key);
+  if (!p) return false;
+  char *q = nullptr;
+  const long v = std::strtol(p, &q, 10);
+  if (q == p || q > end) return false;
+  *out = v;
+  return true;
+}
+
+}  // namespace
+
+gst_status gst_save_class_tuning(gst_ctx *ctx, const char *path) {
+  if (!ctx || !path) return GST_E_ARG;
+  std::string out = "{\"format\": \"gst_gb300 class tuning\", \"version\": 1, \"device\": \"" +
+                    device_name(ctx->device) + "\",\n \"classes\": [";
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    bool first = true;
+    for (int c = 0; c < kSizeClasses; ++c) {
+      if (!ctx->class_set[c]) continue;
+      const GstTuning &t = ctx->class_tuning[c];
+      const unsigned long long max_blocks = c == kSizeClasses - 1 ? 0ull : (1ull << 14) << (2 * c);
+      char line[256];
+      std::snprintf(line, sizeof(line),
+                    "%s\n  {\"class\": %d, \"max_blocks\": %llu, \"blocks_per_sm\": %d, \"stage_words\": %u, "
+                    "\"persistent\": %d}",
+                    first ? "" : ",", c, max_blocks, t.blocks_per_sm, t.stage_words, t.persistent);
+      out += line;
+      first = false;
+    }
+  }
+  out += "\n ]}\n";
+  // Written to a temporary file and renamed, so that a reader never sees half a table.
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE *f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return GST_E_ARG;
+  const bool ok = std::fwrite(out.data(), 1, out.size(), f) == out.size();
+  if (std::fclose(f) != 0 || !ok || std::rename(tmp.c_str(), path) != 0) {
+    std::remove(tmp.c_str());
+    return GST_E_ARG;
+  }
+  return GST_OK;
+}
+
+gst_status gst_load_class_tuning(gst_ctx *ctx, const char *path) {
+  if (!ctx || !path) return GST_E_ARG;
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return GST_E_ARG;
+  std::string text;
+  char buf[4096];
+  size_t n;
+  while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0 && text.size() < (1u << 20)) text.append(buf, n);
+  std::fclose(f);
+  const char *b = text.data(), *e = b + text.size();
+  const char *fmt = json_value(b, e, "format");
+  const std::string want_fmt = "\"gst_gb300 class tuning\"";
+  if (!fmt || size_t(e - fmt) < want_fmt.size() || std::string(fmt, want_fmt.size()) != want_fmt) return GST_E_FORMAT;
+  long version = 0;
+  if (!json_int(b, e, "version", &version) || version != 1) return GST_E_FORMAT;
+  const char *dev = json_value(b, e, "device");
+  const std::string want_dev = "\"" + device_name(ctx->device) + "\"";
+  if (!dev || size_t(e - dev) < want_dev.size() || std::string(dev, want_dev.size()) != want_dev)
+    return GST_E_ARG;  // measured on another kind of GPU: not applied
+  const char *cls = json_value(b, e, "classes");
+  if (!cls || *cls != '[') return GST_E_FORMAT;
+  // Every entry is validated before any is applied.
+  GstTuning t[kSizeClasses];
+  bool set[kSizeClasses] = {};
+  const char *p = cls + 1;
+  for (;;) {
+    const char *o = std::find(p, e, '{'), *close = std::find(p, e, ']');
+    if (close < o) break;  // end of the list
+    if (o == e) return GST_E_FORMAT;
+    const char *oe = std::find(o, e, '}');
+    if (oe == e) return GST_E_FORMAT;
+    long c = -1, bps = 0, words = 0, pers = 0;
+    if (!json_int(o, oe, "class", &c) || !json_int(o, oe, "blocks_per_sm", &bps) ||
+        !json_int(o, oe, "stage_words", &words) || !json_int(o, oe, "persistent", &pers))
+      return GST_E_FORMAT;
+    if (c < 0 || c >= kSizeClasses || !valid_tuning(int(bps), int(words), int(pers))) return GST_E_FORMAT;
+    t[c].blocks_per_sm = int(bps);
+    t[c].stage_words = uint32_t(words);
+    t[c].persistent = int(pers);
+    set[c] = true;
+    p = oe + 1;
+  }
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  for (int c = 0; c < kSizeClasses; ++c) {
+    ctx->class_set[c] = set[c];
+    if (set[c]) ctx->class_tuning[c] = t[c];
+  }
+  return GST_OK;
 }
 
 gst_status gst_batch_autotune(gst_batch *b, const void *d_cmp, void *d_out, void *stream, int iterations,

@@ -9,11 +9,24 @@
 #include <mutex>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "gst_decoder.h"
 #include "gst_encode_plan.h"
 #include "gst_plan.h"
 
 namespace gst {
+
+// An NVTX range over the host-side enqueue of one stage (rANS, tile, copy in,
+// copy out, a server launch), so that a timeline tool shows each stage
+// against the kernels and copies it issued.  NVTX is header-only: without an
+// attached tool a range costs a few nanoseconds.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // gst_encode.cu
 // Enqueues the encoder kernels of one plan (histogram, normalisation, rANS

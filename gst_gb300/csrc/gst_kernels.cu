@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <atomic>
 
+#include "gst_host.h"
 #include "gst_plan.h"
 
 namespace gst {
@@ -894,6 +895,7 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
   plan.stage_words = tuning.stage_words;
   if (ev) cudaEventRecord(ev[0], stream);
   if (tuning.persistent && plan.sync && !plan.rgb && plan.n_rans + plan.n_tiles > 0) {
+    NvtxRange range("gst persistent decode");
     const size_t smem = persistent_smem_bytes(plan.stage_words);
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -909,6 +911,7 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
     return cudaGetLastError();
   }
   if (plan.n_rans) {
+    NvtxRange range("gst rANS");
     const size_t smem = rans_smem_bytes(plan.stage_words);
     if (tuning.blocks_per_sm >= 14) gst_rans_kernel<16><<<plan.n_rans, 128, smem, stream>>>(d_cmp, d_scratch, plan);
     else if (tuning.blocks_per_sm >= 10) gst_rans_kernel<12><<<plan.n_rans, 128, smem, stream>>>(d_cmp, d_scratch, plan);
@@ -918,6 +921,7 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
     if (ev) cudaEventRecord(ev[*launches], stream);
   }
   if (plan.n_tiles) {
+    NvtxRange range(plan.rgb ? "gst tile (RGB)" : "gst tile");
     // Right behind the rANS kernel (no event between them) the tile kernel is
     // a programmatic dependent launch: its launch and CTA setup overlap the
     // rANS tail, and griddepcontrol.wait orders its reads after the symbols.

@@ -253,6 +253,7 @@ bool gst_server::launch(Slot &s, std::unique_lock<std::mutex> &lk) {
   lk.unlock();
 
   const int n = int(s.ids.size());
+  NvtxRange range("gst server launch");
   const PlanLayout L = plan_layout(s.hdrs.data(), n);
   gst_status st = grow(&s.scratch, nullptr, &s.scratch_cap, L.scratch_bytes);
   if (st == GST_OK && s.plan_cap < L.bytes) {

@@ -45,7 +45,8 @@ EXPORTED_SYMBOLS = (
     "gst_batch_layout_bytes", "gst_pack_batch", "gst_decode_rans_groups",
     "gst_batch_create", "gst_batch_destroy", "gst_batch_device_bytes", "gst_batch_launch",
     "gst_batch_graph_launch", "gst_batch_host_launch", "gst_batch_autotune", "gst_size_class",
-    "gst_set_class_tuning", "gst_get_class_tuning", "gst_autotune_class", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
+    "gst_set_class_tuning", "gst_get_class_tuning", "gst_autotune_class", "gst_save_class_tuning",
+    "gst_load_class_tuning", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
     "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times", "gst_set_option",
     "gst_status_string",
     "gst_server_create", "gst_server_destroy", "gst_server_now_ns", "gst_server_submit", "gst_server_poll",
@@ -188,6 +189,8 @@ def load_library() -> ctypes.CDLL:
         "gst_set_class_tuning": (I, [P, I, I, I, I]),
         "gst_get_class_tuning": (I, [P, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]),
         "gst_autotune_class": (I, [P, HP, I, P, P, P, I, ctypes.POINTER(I)]),
+        "gst_save_class_tuning": (I, [P, ctypes.c_char_p]),
+        "gst_load_class_tuning": (I, [P, ctypes.c_char_p]),
         "gst_load_compressed_dxt_static": (I, [HP, P, P, P, ctypes.POINTER(U32)]),
         "gst_sync_status": (I, [P, P]),
         "gst_last_launch_count": (I, [P]),
@@ -488,6 +491,16 @@ def set_class_tuning(ctx: GPUContext, size_class_index: int, blocks_per_sm: int,
                      persistent: int = 0) -> None:
     _check(load_library().gst_set_class_tuning(ctx.handle, size_class_index, blocks_per_sm, stage_words, persistent),
            "gst_set_class_tuning")
+
+
+def save_class_tuning(ctx: GPUContext, path) -> None:
+    """gst_save_class_tuning: the classes that are set, as a JSON table."""
+    _check(load_library().gst_save_class_tuning(ctx.handle, str(path).encode()), "gst_save_class_tuning")
+
+
+def load_class_tuning(ctx: GPUContext, path) -> None:
+    """gst_load_class_tuning: replaces the context's class table with the file's."""
+    _check(load_library().gst_load_class_tuning(ctx.handle, str(path).encode()), "gst_load_class_tuning")
 
 
 def get_class_tuning(ctx: GPUContext, size_class_index: int) -> tuple[int, int, int]:

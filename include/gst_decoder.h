@@ -190,6 +190,22 @@ gst_status gst_set_class_tuning(gst_ctx *ctx, int size_class, int blocks_per_sm,
 gst_status gst_autotune_class(gst_ctx *ctx, const gst_header *hdrs, int n, const void *d_cmp, void *d_out,
                               void *stream, int iterations, int *size_class);
 
+/* The per-size-class configurations as a JSON table on disk (no counterpart
+ * in the reference), so that tuning outlives the process:
+ *   {"format": "gst_gb300 class tuning", "version": 1, "device": "<GPU name>",
+ *    "classes": [{"class": c, "max_blocks": m, "blocks_per_sm": b,
+ *                 "stage_words": w, "persistent": p}, ...]}
+ * gst_save_class_tuning writes the classes that are set (atomically: a
+ * temporary file renamed into place); gst_load_class_tuning replaces the
+ * context's class table with the file's after validating every entry
+ * (GST_E_FORMAT for a malformed table, GST_E_ARG for a missing file or one
+ * written on another kind of GPU; nothing changes on error).  With the
+ * environment variable GST_TUNING_TABLE naming a file, gst_init loads it when
+ * it exists and matches the device, and gst_autotune_class saves the table
+ * there after each run. */
+gst_status gst_save_class_tuning(gst_ctx *ctx, const char *path);
+gst_status gst_load_class_tuning(gst_ctx *ctx, const char *path);
+
 /* One-image device-resident decode that allocates nothing -- no counterpart in
  * the reference, which allocates its decoder scratch per call or through
  * PreallocateDecompressor.  For callers that must not allocate device memory

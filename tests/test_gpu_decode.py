@@ -470,3 +470,52 @@ def test_class_tuning_applies_and_stays_bit_exact():
         ctx.set_profiling(False)
     finally:
         ctx.close()
+
+
+def test_class_tuning_table_persists(tmp_path, monkeypatch):
+    """The per-size-class table as JSON: saved and loaded back, loaded by a new
+    context from GST_TUNING_TABLE, rewritten by gst_autotune_class; malformed
+    tables and tables of another GPU are refused and change nothing."""
+    import json
+    path = tmp_path / "tuning.json"
+    ctx = decoder.GPUContext(0)
+    try:
+        decoder.set_class_tuning(ctx, 1, 8, 2040, 0)
+        decoder.set_class_tuning(ctx, 4, 12, 1016, 1)
+        decoder.save_class_tuning(ctx, path)
+        table = json.loads(path.read_text())
+        assert table["format"] == "gst_gb300 class tuning" and table["version"] == 1
+        assert table["device"] == torch.cuda.get_device_name(0)
+        assert [(c["class"], c["blocks_per_sm"], c["stage_words"], c["persistent"]) for c in table["classes"]] == \
+            [(1, 8, 2040, 0), (4, 12, 1016, 1)]
+        decoder.set_class_tuning(ctx, 1, 0, 0, 0)
+        decoder.set_class_tuning(ctx, 4, 0, 0, 0)
+        decoder.load_class_tuning(ctx, path)
+        assert decoder.get_class_tuning(ctx, 1) == (8, 2040, 0) and decoder.get_class_tuning(ctx, 4) == (12, 1016, 1)
+        before = [decoder.get_class_tuning(ctx, c) for c in range(7)]
+        bad = dict(table, classes=[dict(table["classes"][0], stage_words=1001)])
+        for text, status in ((json.dumps(bad), decoder.GST_E_FORMAT), ("{}", decoder.GST_E_FORMAT),
+                             (json.dumps(dict(table, device="some other GPU")), decoder.GST_E_ARG)):
+            (tmp_path / "bad.json").write_text(text)
+            with pytest.raises(decoder.GstError) as ei:
+                decoder.load_class_tuning(ctx, tmp_path / "bad.json")
+            assert ei.value.status == status
+        assert [decoder.get_class_tuning(ctx, c) for c in range(7)] == before
+    finally:
+        ctx.close()
+    # A new context loads the named table; autotuning a class rewrites it.
+    monkeypatch.setenv("GST_TUNING_TABLE", str(path))
+    ctx = decoder.GPUContext(0)
+    try:
+        assert decoder.get_class_tuning(ctx, 1) == (8, 2040, 0)
+        im = workloads.plain(0)
+        hdrs, packed = decoder.pack_batch([im.stream])
+        d_cmp = torch.from_numpy(packed).cuda()
+        d_out = torch.zeros(hdrs[0].dxt_bytes, dtype=torch.uint8, device="cuda")
+        c = decoder.autotune_class(ctx, hdrs, d_cmp, d_out, iterations=1)
+        classes = {e["class"]: e for e in json.loads(path.read_text())["classes"]}
+        assert set(classes) == {0, 1, 4}
+        assert (classes[0]["blocks_per_sm"], classes[0]["stage_words"], classes[0]["persistent"]) == \
+            decoder.get_class_tuning(ctx, c)
+    finally:
+        ctx.close()

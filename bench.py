@@ -75,7 +75,7 @@ def parse_args():
     p.add_argument("--serve-plain-seconds", type=float, default=5.0,
                    help="length of each run of the per-request plain-decode comparison (it saturates near 10k "
                         "req/s, so its 20k req/s queue only grows with the run)")
-    p.add_argument("--serve-bound-budget-mib", type=int, default=24,
+    p.add_argument("--serve-bound-budget-mib", type=int, default=48,
                    help="device budget of the extra 20k req/s run in which admission binds (0: skip it)")
     p.add_argument("--serve-rates", default="1000,5000,20000", help="Poisson arrival rates, requests/s")
     p.add_argument("--serve-class-tune", type=int, default=1,
@@ -979,12 +979,14 @@ def serving(ctx, args) -> dict:
     if args.serve_bound_budget_mib > 0 and "batched" in args.serve_modes.split(","):
         # Admission under pressure: a budget small enough that requests wait
         # for the memory of earlier ones (compressed input + DXT1 output).
+        # Checked results are read and released as they arrive: held outputs
+        # would otherwise take the budget.
         budget = args.serve_bound_budget_mib << 20
         secs = min(10.0, args.serve_seconds)
         with DecodeServer(ctx, device_budget_bytes=budget, max_inflight=4, max_batch_images=256) as srv:
-            run_poisson(srv, reqs, 20000.0, 0.2, seed=7, pick=pick)
-            res = run_poisson(srv, reqs, 20000.0, secs, seed=20001, verify_every=4 * args.serve_verify_every,
-                              pick=pick)
+            run_poisson(srv, reqs, 20000.0, 0.2, seed=7, pick=pick, hold=False)
+            res = run_poisson(srv, reqs, 20000.0, secs, seed=20001, verify_every=args.serve_verify_every // 5 or 1,
+                              pick=pick, hold=False)
         out["20000_req_s_budget_bound"] = {"device_budget_mib": args.serve_bound_budget_mib, **res.summary()}
     return out
 

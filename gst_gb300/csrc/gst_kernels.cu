@@ -245,6 +245,7 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
   bool bad = false;
   int32_t crun = 0, tot = 0;  // INDEX: running sum within the chunk, and over the chunks done
   int32_t s0 = 0, s1 = 0, s2_ = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0;
+  uint4 even_run = make_uint4(0, 0, 0, 0);  // symbols of the last even run, stored with the next odd one
 #pragma unroll 1
   for (int k = 0; k < 16; ++k) {
     if (ptr - 16 * 32 < static_cast<int>(stage_lo >> 1) && static_cast<int>(stage_lo) > static_cast<int>(lo) &&
@@ -300,8 +301,15 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
         o[0] = make_uint4(ew[0], ew[1], ew[2], ew[3]);
         o[1] = make_uint4(ew[4], ew[5], ew[6], ew[7]);
       }
-    } else {
-      if (active) *reinterpret_cast<uint4 *>(out + 240 - 16 * k) = make_uint4(w0, w1, w2, w3);
+    } else if (!(k & 1)) {
+      even_run = make_uint4(w0, w1, w2, w3);
+    } else if (active) {
+      // Runs k - 1 and k fill positions 224 - 16(k - 1) .. 255 - 16(k - 1),
+      // one aligned 32-byte sector: written whole, so that no sector of the
+      // output reaches L2 in two halves.
+      uint4 *o = reinterpret_cast<uint4 *>(out + 240 - 16 * k);
+      o[0] = make_uint4(w0, w1, w2, w3);
+      o[1] = even_run;
     }
     if (INDEX && (k & 1)) {
       const int mm = k >> 1;

@@ -165,7 +165,8 @@ class LoadResult:
 
 def run_poisson(server: DecodeServer, requests: Sequence[tuple[bytes, np.ndarray | None]], rate: float,
                 seconds: float, seed: int = 0, verify_every: int = 0,
-                pick: Callable[[np.random.Generator], int] | None = None, native: bool = True) -> LoadResult:
+                pick: Callable[[np.random.Generator], int] | None = None, native: bool = True,
+                hold: bool = True) -> LoadResult:
     """Open-loop Poisson arrivals at `rate` requests/s for `seconds`.
 
     requests: (GST stream, expected DXT1 blocks as uint64 or None); `pick`
@@ -180,19 +181,23 @@ def run_poisson(server: DecodeServer, requests: Sequence[tuple[bytes, np.ndarray
     library's own thread submits each stream at its arrival time
     (gst_server_schedule), so no stall of this process delays a submission;
     this process only polls and releases (every `verify_every`-th id is kept
-    for the check)."""
+    for the check).  With `hold` False (native submitter only) a checked
+    result is read and compared as soon as it is polled and then released, so
+    that no held output occupies the device budget (a run whose budget binds
+    would otherwise stall on the held outputs)."""
     gc_on = gc.isenabled()
     gc.collect()
     gc.disable()
     try:
-        run = _run_poisson_native if native else _run_poisson
-        return run(server, requests, rate, seconds, seed, verify_every, pick)
+        if native:
+            return _run_poisson_native(server, requests, rate, seconds, seed, verify_every, pick, hold)
+        return _run_poisson(server, requests, rate, seconds, seed, verify_every, pick)
     finally:
         if gc_on:
             gc.enable()
 
 
-def _run_poisson_native(server, requests, rate, seconds, seed, verify_every, pick) -> LoadResult:
+def _run_poisson_native(server, requests, rate, seconds, seed, verify_every, pick, hold=True) -> LoadResult:
     rng = np.random.default_rng(seed)
     n = int(rng.poisson(rate * seconds))
     arrivals = np.sort(rng.uniform(0.0, seconds, n))
@@ -204,6 +209,32 @@ def _run_poisson_native(server, requests, rate, seconds, seed, verify_every, pic
     ids, t0 = server.schedule([r[0] for r in requests], choice, offsets)
     at_last = t0 + (int(offsets[-1]) if n else 0)
     held = {}  # id -> dxt bytes, every verify_every-th id, read back after the run
+    index = {}  # id -> position in the schedule (ids are written in schedule order)
+    scan = 0
+
+    def position(rid):
+        nonlocal scan
+        while rid not in index and scan < n:
+            v = int(ids[scan])
+            if v:
+                index[v] = scan
+            scan += 1
+        return index[rid]
+
+    def checked(r):  # every verify_every-th result: held to the end, or read now
+        if not (verify_every and r.id % verify_every == 0):
+            return False
+        if hold:
+            held[r.id] = r.dxt_bytes
+            return True
+        want = requests[choice[position(r.id)]][1]
+        if want is not None:
+            res.verified += 1
+            if not np.array_equal(server.read(r.id, r.dxt_bytes).view(np.uint64), want):
+                res.mismatched += 1
+        server.release(r.id)
+        return True
+
     last_done = t0
     deadline = None
     while True:
@@ -220,9 +251,7 @@ def _run_poisson_native(server, requests, rate, seconds, seed, verify_every, pic
                              "launch_to_done_ms": round((r.done_ns - r.launch_ns) / 1e6, 4)}
             if r.status != GST_OK:
                 res.errors += 1
-            if verify_every and r.id % verify_every == 0:
-                held[r.id] = r.dxt_bytes
-            else:
+            if not checked(r):
                 server.release(r.id)
         if deadline is None and server.now_ns() >= at_last:
             deadline = time.monotonic() + 60.0  # every arrival is past: drain what is left
@@ -240,16 +269,13 @@ def _run_poisson_native(server, requests, rate, seconds, seed, verify_every, pic
             res.completed += 1
             res.latencies_us.append((r.done_ns - r.arrival_ns) / 1e3)
             res.waits_us.append((r.launch_ns - r.arrival_ns) / 1e3)
-            if verify_every and r.id % verify_every == 0:
-                held[r.id] = r.dxt_bytes
-            else:
+            if not checked(r):
                 server.release(r.id)
     res.submit_lag_max_us = late_ns / 1e3
     res.seconds = max(seconds, (last_done - t0) / 1e9)
     res.stats = server.stats()
-    index = {int(rid): i for i, rid in enumerate(ids) if rid}
     for rid, nbytes in held.items():
-        want = requests[choice[index[rid]]][1]
+        want = requests[choice[position(rid)]][1]
         if want is not None:
             got = server.read(rid, nbytes).view(np.uint64)
             res.verified += 1

@@ -128,3 +128,18 @@ def test_mismatch_and_rejection_are_reported(native):
     srv2 = FakeServer(capacity=0)
     res2 = run_poisson(srv2, requests(), rate=2000.0, seconds=0.1, seed=7, native=native)
     assert res2.rejected > 0 and res2.submitted == 0
+
+
+def test_inline_checks_release_every_result_at_once():
+    """hold=False: a checked result is read, compared and released as soon as it
+    is polled (a run whose device budget binds cannot wait for held outputs);
+    a wrong output is still counted."""
+    srv = FakeServer()
+    res = run_poisson(srv, requests(), rate=4000.0, seconds=0.25, seed=8, verify_every=2, hold=False)
+    s = res.summary()
+    assert s["completed"] == s["submitted"] > 0 and len(srv.released) == s["completed"]
+    assert s["verified"] == s["submitted"] // 2 and s["bit_exact"]
+    reqs = requests() + [(b"bad", np.zeros(2, np.uint64))]
+    srv = FakeServer(bad_payload=np.ones(16, np.uint8))
+    res = run_poisson(srv, reqs, rate=2000.0, seconds=0.2, seed=9, verify_every=1, pick=lambda rng: 4, hold=False)
+    assert res.mismatched == res.verified > 0 and len(srv.released) == res.completed

@@ -181,6 +181,17 @@ __device__ __forceinline__ void stage_range(uint8_t *buf, const uint8_t *a, cons
   __syncwarp();
 }
 
+__device__ __forceinline__ uint32_t lds_u32(uint32_t a) {
+  uint32_t v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ uint32_t lds_u16(uint32_t a) {
+  uint16_t v;
+  asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(a));
+  return v;
+}
+
 // Integer multiply-adds, kept as such so that they issue to the FMA pipe and
 // leave the integer ALU pipe to the shifts, logic and warp votes.
 __device__ __forceinline__ uint32_t mad_lo(uint32_t a, uint32_t b, uint32_t c) {
@@ -229,8 +240,8 @@ template <bool INDEX>
 __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, uint32_t lo, uint32_t top,
                                              const uint32_t *__restrict__ tbl, uint16_t *stage, uint32_t stage_words,
                                              int lane, bool active, uint8_t *__restrict__ out, int32_t suf[8]) {
-  const uint8_t *tbl_bytes = reinterpret_cast<const uint8_t *>(tbl);
-  const uint8_t *stage_bytes = reinterpret_cast<const uint8_t *>(stage);
+
+
   const int lo16 = static_cast<int>(lo >> 1);
   uint32_t stage_lo = (top - lo > 2u * stage_words) ? top - 2u * stage_words : lo;
   stage_range(reinterpret_cast<uint8_t *>(stage), sec + stage_lo, sec + top, lane);
@@ -240,7 +251,9 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
                 static_cast<int>((reinterpret_cast<uintptr_t>(sec + stage_lo) & 15) >> 1);
   uint32_t x = active ? reinterpret_cast<const uint32_t *>(sec + top)[lane] : kRansL;
   int ptr = static_cast<int>(top >> 1);      // word index of the section
-  uint32_t s2 = 2u * (ptr - sbase16);        // byte offset of word ptr in the stage
+  const uint32_t stage_s = static_cast<uint32_t>(__cvta_generic_to_shared(stage));
+  const uint32_t tbl_c = static_cast<uint32_t>(__cvta_generic_to_shared(tbl)) - (1u << 24);
+  uint32_t s2 = stage_s + 2u * (ptr - sbase16);  // shared address of word ptr in the stage
   const uint32_t ge = ~lanemask_lt();
   bool bad = false;
   int32_t crun = 0, tot = 0;  // INDEX: running sum within the chunk, and over the chunks done
@@ -256,27 +269,27 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
       stage_range(reinterpret_cast<uint8_t *>(stage), sec + stage_lo, sec + new_top, lane);
       sbase16 = static_cast<int>(stage_lo >> 1) -
                 static_cast<int>((reinterpret_cast<uintptr_t>(sec + stage_lo) & 15) >> 1);
-      s2 = 2u * (ptr - sbase16);
+      s2 = stage_s + 2u * (ptr - sbase16);
     }
-    if (static_cast<int>(s2) < 0) {  // only a malformed stream gets here
+    if (static_cast<int>(s2 - stage_s) < 0) {  // only a malformed stream gets here
       bad = true;
-      s2 = 0;
+      s2 = stage_s;
     }
     uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
     uint32_t ew[8];  // INDEX: 16 int16 partial sums, slot 15 - j for step j
     if (INDEX && !(k & 1)) crun = 0;
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      const uint32_t qm = mad_hi(x, 1u << 21, 0u - 2048u);                          // q - 2048
-      const uint32_t off = mad_lo(qm, 0u - 8192u, mad_lo(x, 4u, 0u - (1u << 24)));  // 4 (x mod 2048)
-      const uint32_t e = *reinterpret_cast<const uint32_t *>(tbl_bytes + off);
+      const uint32_t qm = mad_hi(x, 1u << 21, 0u - 2048u);            // q - 2048
+      const uint32_t ea = mad_lo(qm, 0u - 8192u, mad_lo(x, 4u, tbl_c));  // table + 4 (x mod 2048)
+      const uint32_t e = lds_u32(ea);
       const uint32_t ec = e & 0xFFFFFFu;
       x = mad_lo(mul_hi(ec, 1u << 21), qm, ec);
       const bool need = active && x < kRansL;
       const uint32_t m = __ballot_sync(0xFFFFFFFFu, need);
       if (need) {
         const uint32_t depth2 = 2u * static_cast<uint32_t>(__popc(m & ge));
-        const uint32_t v = *reinterpret_cast<const uint16_t *>(stage_bytes + static_cast<int>(s2 - depth2));
+        const uint32_t v = lds_u16(s2 - depth2);
         x = mad_lo(x, 65536u, v);
       }
       s2 = mad_lo(static_cast<uint32_t>(__popc(m)), 0u - 2u, s2);
@@ -294,7 +307,7 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
         else w0 = __byte_perm(w0, e, 0x2107);
       }
     }
-    ptr = static_cast<int>(s2 >> 1) + sbase16;
+    ptr = static_cast<int>((s2 - stage_s) >> 1) + sbase16;
     if constexpr (INDEX) {
       if (active) {
         uint4 *o = reinterpret_cast<uint4 *>(out + 2 * (240 - 16 * k));

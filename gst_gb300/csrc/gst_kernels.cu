@@ -259,7 +259,7 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
   int32_t crun = 0, tot = 0;  // INDEX: running sum within the chunk, and over the chunks done
   int32_t s0 = 0, s1 = 0, s2_ = 0, s3 = 0, s4 = 0, s5 = 0, s6 = 0, s7 = 0;
   uint4 even_run = make_uint4(0, 0, 0, 0);  // symbols of the last even run, stored with the next odd one
-#pragma unroll 1
+#pragma unroll 2
   for (int k = 0; k < 16; ++k) {
     if (ptr - 16 * 32 < static_cast<int>(stage_lo >> 1) && static_cast<int>(stage_lo) > static_cast<int>(lo) &&
         ptr > lo16) {

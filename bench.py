@@ -487,6 +487,27 @@ def run_gst(args, rank, world, local):
     rb.set_tuning(tuning["blocks_per_sm"], tuning["stage_words"], tuning["persistent"])
     t_ser, _ = time_steps(step_e2e_serial, max(3, args.steps // 2), args.warmup, stream, flush)
 
+    # The host link's floor for the same bytes: the step's copy in and copy
+    # out alone, issued at the same time on two streams (no decode).
+    d_link = torch.empty_like(batch.d_cmp)
+    side = torch.cuda.Stream(device)
+
+    def step_link():
+        fork = torch.cuda.Event()
+        fork.record(stream)
+        side.wait_event(fork)
+        with torch.cuda.stream(side):
+            d_link.copy_(batch.h_cmp, non_blocking=True)
+        with torch.cuda.stream(stream):
+            batch.h_out.copy_(batch.d_out, non_blocking=True)
+        join = torch.cuda.Event()
+        join.record(side)
+        stream.wait_event(join)
+
+    t_link, _ = time_steps(step_link, max(3, args.steps // 2), args.warmup, stream, flush)
+    link_ms = statistics.mean(t_link)
+    del d_link
+
     line = {
         "metric": METRIC,
         "value": round(value, 2),
@@ -550,6 +571,10 @@ def run_gst(args, rank, world, local):
             "call": f"gst_batch_host_launch (one graph launch per call), {chunks} chunks, "
                     f"{'persistent' if best[1][2] else 'two-kernel'} decodes (pinned host layout in, pinned DXT1 out)",
             "serial_ms_per_step": round(statistics.mean(t_ser), 4),
+            "link_floor_ms": round(link_ms, 4),
+            "link_floor_note": "the same copy in and copy out alone, concurrently, without a decode: "
+                               "the host link's time for the step's bytes",
+            "link_frac": round(link_ms / (e2e_total / args.steps), 3),
         },
         "input_seconds": round(encode_s, 1),
     }

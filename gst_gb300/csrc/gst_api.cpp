@@ -502,7 +502,8 @@ struct gst_batch {
   std::vector<int> hm_cut;
   std::vector<PlanLayout> hm_lay;
   std::vector<size_t> hm_plan_off;
-  cudaStream_t hm_stream[3] = {};
+  std::vector<size_t> hm_scr_off;  // chunk c's scratch: b->scratch + hm_scr_off[c], disjoint per chunk
+  cudaStream_t hm_stream[4] = {};  // copy in, decode (even chunks), copy out, decode (odd chunks)
   cudaGraphExec_t hm_graph = nullptr;
   const void *hm_graph_cmp = nullptr;
   void *hm_graph_out = nullptr;
@@ -1139,13 +1140,20 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
     e = cudaMemcpy(b->hm_plans, ph.data(), off[nc], cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_status(e);
     b->hm_cut = cut;
+    b->hm_scr_off.assign(nc + 1, 0);
+    for (int c = 0; c < nc; ++c) b->hm_scr_off[c + 1] = b->hm_scr_off[c] + lay[c].scratch_bytes;
+    if (b->hm_scr_off[nc] > b->layout.scratch_bytes) return GST_E_ARG;  // cannot happen: same images
     b->hm_lay = std::move(lay);
     b->hm_plan_off = std::move(off);
     b->hm_chunks = chunks;
   }
   if (!b->hm_graph || b->hm_graph_cmp != h_cmp || b->hm_graph_out != h_out || b->hm_graph_tuning != tuning) {
-    // Capture the copies in, decodes and copies out of every chunk on three
-    // streams, enqueued in three passes as gst_load_host_dxts does.
+    // Capture the copies in, decodes and copies out of every chunk, enqueued
+    // in three passes as gst_load_host_dxts does.  Consecutive chunks decode
+    // on two streams, each into its own part of the batch's scratch: a decode
+    // is bound by its rANS chains' latency more than by its size, so the next
+    // chunk's decode starts as soon as its copy in lands instead of after the
+    // previous decode, and the copies out (the slowest stage) wait less.
     {
       std::lock_guard<std::mutex> lock(ctx->mu);
       launch_decode(nullptr, nullptr, nullptr, GstPlanView{}, nullptr, &ctx->last_launches, nullptr,
@@ -1154,8 +1162,9 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
     const int nc = int(b->hm_cut.size()) - 1;
     const uint8_t *hc = static_cast<const uint8_t *>(h_cmp);
     uint8_t *ho = static_cast<uint8_t *>(h_out);
-    cudaStream_t cs = nullptr, si = b->hm_stream[0], sc = b->hm_stream[1], so = b->hm_stream[2];
-    std::vector<cudaEvent_t> evs(2 * nc + 4, nullptr);
+    cudaStream_t cs = nullptr, si = b->hm_stream[0], so = b->hm_stream[2];
+    const cudaStream_t sc[2] = {b->hm_stream[1], b->hm_stream[3]};
+    std::vector<cudaEvent_t> evs(2 * nc + 5, nullptr);
     e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     for (auto &ev : evs)
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -1166,8 +1175,9 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
       capturing_now = e == cudaSuccess;
     }
     cudaEvent_t fork = evs[2 * nc], end_i = evs[2 * nc + 1], end_c = evs[2 * nc + 2], end_o = evs[2 * nc + 3];
+    cudaEvent_t end_c2 = evs[2 * nc + 4];
     if (e == cudaSuccess) e = cudaEventRecord(fork, cs);
-    for (cudaStream_t s : {si, sc, so})
+    for (cudaStream_t s : {si, sc[0], sc[1], so})
       if (e == cudaSuccess) e = cudaStreamWaitEvent(s, fork, 0);
     nvtxRangePushA("gst copy in");
     for (int c = 0; c < nc && e == cudaSuccess; ++c) {
@@ -1181,13 +1191,15 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
     nvtxRangePop();
     nvtxRangePushA("gst decode");
     for (int c = 0; c < nc && e == cudaSuccess; ++c) {
-      e = cudaStreamWaitEvent(sc, evs[c], 0);
+      const cudaStream_t s = sc[c & 1];
+      e = cudaStreamWaitEvent(s, evs[c], 0);
       GstPlanView view = plan_view(b->hm_lay[c], b->hm_plans + b->hm_plan_off[c], ctx->status_d);
       view.image_err = nullptr;
       view.wait_limit_ns = ctx->wait_limit_ns;
       int launches = 0;
-      if (e == cudaSuccess) e = launch_decode(nullptr, b->scratch, nullptr, view, sc, &launches, nullptr, tuning);
-      if (e == cudaSuccess) e = cudaEventRecord(evs[nc + c], sc);
+      if (e == cudaSuccess)
+        e = launch_decode(nullptr, b->scratch + b->hm_scr_off[c], nullptr, view, s, &launches, nullptr, tuning);
+      if (e == cudaSuccess) e = cudaEventRecord(evs[nc + c], s);
     }
     nvtxRangePop();
     nvtxRangePushA("gst copy out");
@@ -1199,9 +1211,10 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
     }
     nvtxRangePop();
     if (e == cudaSuccess) e = cudaEventRecord(end_i, si);
-    if (e == cudaSuccess) e = cudaEventRecord(end_c, sc);
+    if (e == cudaSuccess) e = cudaEventRecord(end_c, sc[0]);
+    if (e == cudaSuccess) e = cudaEventRecord(end_c2, sc[1]);
     if (e == cudaSuccess) e = cudaEventRecord(end_o, so);
-    for (cudaEvent_t ev : {end_i, end_c, end_o})
+    for (cudaEvent_t ev : {end_i, end_c, end_c2, end_o})
       if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev, 0);
     if (capturing_now) {
       const cudaError_t e2 = cudaStreamEndCapture(cs, &g);

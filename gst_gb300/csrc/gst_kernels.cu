@@ -56,15 +56,18 @@ __device__ __forceinline__ void flag_error(uint32_t *err, uint32_t *image_err, u
 // ---------------------------------------------------------------------------
 // Decode table (ans/build_table.cl:12-83).  Slot s in [0, 2048) belongs to the
 // symbol x with cum[x] <= s < cum[x] + freq[x]; the table stores
-// (s - cum) | freq << 11 | x << 24 (11, 12 and 8 bits) so that one lookup
+// x | (s - cum) << 8 | freq << 19 (8, 11 and 12 bits) so that one lookup
 // gives the next state, x' = (x >> 11) * freq + (s - cum), equal to the
 // reference's (x >> 11) * freq - cum + s in u32 arithmetic, and the symbol as
-// the entry's top byte.
+// the entry's low byte.  Both shifted fields come out of the entry with one
+// independent shift each (entry >> 19 = freq, entry >> 8 = freq * 2048 +
+// s - cum), so the state update is one dependent step shorter than with a
+// masked field.
 //
 // Built without searching: each symbol with freq > 0 marks its first slot,
 // and since those first slots increase with x, a running maximum of the marks
-// over the slots gives every slot's symbol.  Entry = (freq << 11 | x << 24) -
-// cum + s, from one per-symbol word.  Run by 128 threads (t = 0..127) that
+// over the slots gives every slot's symbol.  Entry = (freq << 19 | x) -
+// (cum << 8) + (s << 8), from one per-symbol word.  Run by 128 threads (t = 0..127) that
 // synchronise on named barrier BAR; `work` is 3 KB of shared scratch
 // (per-symbol words, slot marks) that is free again on return.  Returns false
 // (uniformly over the 128 threads) if the frequencies do not sum to 2048.
@@ -90,8 +93,8 @@ __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t 
   const uint32_t total = wred[0] + wred[1] + wred[2] + wred[3];
   const uint32_t c0 = woff + v - f0 - f1, c1 = c0 + f0;
   const uint32_t x0 = 2 * t, x1 = 2 * t + 1;
-  sym_word[x0] = ((f0 << 11) | (x0 << 24)) - c0;
-  sym_word[x1] = ((f1 << 11) | (x1 << 24)) - c1;
+  sym_word[x0] = ((f0 << 19) | x0) - (c0 << 8);
+  sym_word[x1] = ((f1 << 19) | x1) - (c1 << 8);
   if (total == kTableSize) {  // then every marked slot c < cum + freq <= 2048
     if (f0) marks[c0] = static_cast<uint8_t>(x0);
     if (f1) marks[c1] = static_cast<uint8_t>(x1);
@@ -123,7 +126,7 @@ __device__ bool build_decode_table(const uint16_t *__restrict__ freqs, uint32_t 
     if (w < warp) excl = max(excl, wred[4 + w]);
   uint32_t e[16];
 #pragma unroll
-  for (int k = 0; k < 16; ++k) e[k] = sym_word[max(own[k], excl)] + static_cast<uint32_t>(16 * t + k);
+  for (int k = 0; k < 16; ++k) e[k] = sym_word[max(own[k], excl)] + (static_cast<uint32_t>(16 * t + k) << 8);
   uint4 *dst = reinterpret_cast<uint4 *>(tbl) + 4 * t;
   dst[0] = make_uint4(e[0], e[1], e[2], e[3]);
   dst[1] = make_uint4(e[4], e[5], e[6], e[7]);
@@ -226,9 +229,9 @@ __device__ __forceinline__ uint32_t mul_hi(uint32_t a, uint32_t b) {
 // groups that fit never re-stage).
 //
 // One step, with q = x >> 11 and the table entry e of slot x mod 2048:
-//   x' = q * freq + (s - cum), computed as (q - 2048) * (e' >> 11) + e' with
-//   e' = e mod 2^24 (the freq << 11 term cancels), and the slot's byte offset
-//   4x - 8192 q, all as multiply-adds.  Renormalising lanes read consecutive
+//   x' = q * freq + (s - cum), computed as (q - 2048) * (e >> 19) + (e >> 8)
+//   (e >> 8 = freq * 2048 + s - cum: the freq * 2048 term cancels), and the
+//   slot's byte offset 4x - 8192 q as multiply-adds.  Renormalising lanes read consecutive
 //   words below the read pointer, the lowest lane the lowest address
 //   (ans_decode.cl:50-57): lane l's word lies popc(renormalising lanes >= l)
 //   words below the pointer, and only those lanes load it from the stage.
@@ -283,8 +286,7 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
       const uint32_t qm = mad_hi(x, 1u << 21, 0u - 2048u);            // q - 2048
       const uint32_t ea = mad_lo(qm, 0u - 8192u, mad_lo(x, 4u, tbl_c));  // table + 4 (x mod 2048)
       const uint32_t e = lds_u32(ea);
-      const uint32_t ec = e & 0xFFFFFFu;
-      x = mad_lo(mul_hi(ec, 1u << 21), qm, ec);
+      x = mad_lo(e >> 19, qm, e >> 8);
       const bool need = active && x < kRansL;
       const uint32_t m = __ballot_sync(0xFFFFFFFFu, need);
       if (need) {
@@ -297,14 +299,14 @@ __device__ __forceinline__ bool decode_group(const uint8_t *__restrict__ sec, ui
       // (ans_decode.cl:71-72 stores the symbols in reverse).
       if constexpr (INDEX) {
         const uint32_t part = static_cast<uint32_t>(crun) & 0xFFFFu;
-        crun += static_cast<int32_t>(e >> 24) - 128;
+        crun += static_cast<int32_t>(e & 0xFFu) - 128;
         if (j & 1) ew[7 - (j >> 1)] |= part;  // slot 15 - j, even: low half
         else ew[7 - (j >> 1)] = part << 16;   // odd slot: high half
       } else {
-        if (j < 4) w3 = __byte_perm(w3, e, 0x2107);
-        else if (j < 8) w2 = __byte_perm(w2, e, 0x2107);
-        else if (j < 12) w1 = __byte_perm(w1, e, 0x2107);
-        else w0 = __byte_perm(w0, e, 0x2107);
+        if (j < 4) w3 = __byte_perm(w3, e, 0x2104);
+        else if (j < 8) w2 = __byte_perm(w2, e, 0x2104);
+        else if (j < 12) w1 = __byte_perm(w1, e, 0x2104);
+        else w0 = __byte_perm(w0, e, 0x2104);
       }
     }
     ptr = static_cast<int>((s2 - stage_s) >> 1) + sbase16;

@@ -395,7 +395,7 @@ def test_load_host_dxts_pipelined(gpu_ctx, chunks):
         assert np.array_equal(h_out.numpy().view(np.uint64), want)
 
 
-@pytest.mark.parametrize("chunks,persistent", [(1, 0), (3, 0), (5, 1)])
+@pytest.mark.parametrize("chunks,persistent", [(1, 0), (3, 0), (5, 1), (6, 0)])
 def test_batch_host_launch_graph(gpu_ctx, chunks, persistent):
     # gst_batch_host_launch: the pipelined host-to-host decode replayed from a
     # captured graph; repeated calls (outputs cleared in between), a new

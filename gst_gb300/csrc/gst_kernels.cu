@@ -570,13 +570,15 @@ __device__ __forceinline__ void inv53_level_group(int32_t *pl) {
   bar_sync(BAR, NG);
 }
 
-// assemble.cl:39-62: YCoCg667 -> RGB565 on int values of signed chars.
+// assemble.cl:39-62: YCoCg667 -> RGB565 on int values of signed chars.  The
+// reference's ushort endpoint is the low 16 bits of the result (the caller
+// keeps only those).
 __device__ __forceinline__ uint32_t ycocg_to_565(int y, int co, int cg) {
   const int t = y - cg / 2;
   const int g = cg + t;
   const int b = (t - co) / 2;
   const int r = b + co;
-  return ((static_cast<uint32_t>(r) << 11) | (static_cast<uint32_t>(g) << 5) | static_cast<uint32_t>(b)) & 0xFFFFu;
+  return (static_cast<uint32_t>(r) << 11) | (static_cast<uint32_t>(g) << 5) | static_cast<uint32_t>(b);
 }
 
 // assemble.cl:83-129 (assemble_rgb): an endpoint as 8-bit R, G, B by bit
@@ -772,18 +774,21 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
   for (int i = 0; i < kRows; ++i) {
     const int r = warp + kWarps * i;
     const uint32_t p = (ty * 32 + r) * im.bx + tx * 32 + lane;
-    const int32_t *row = pl + r * kPlanePitch + lane;
-    const int y1 = static_cast<int8_t>(row[0]), y2 = static_cast<int8_t>(row[kPlaneWords]);
-    const int co1 = static_cast<int8_t>(row[2 * kPlaneWords]), cg1 = static_cast<int8_t>(row[3 * kPlaneWords]);
-    const int co2 = static_cast<int8_t>(row[4 * kPlaneWords]), cg2 = static_cast<int8_t>(row[5 * kPlaneWords]);
+    // Each value as the reference's signed char: the low byte of the int32
+    // coefficient, loaded sign-extended.
+    const int8_t *row = reinterpret_cast<const int8_t *>(pl + r * kPlanePitch + lane);
+    constexpr int kPB = 4 * kPlaneWords;  // plane stride in bytes
+    const int y1 = row[0], y2 = row[kPB];
+    const int co1 = row[2 * kPB], cg1 = row[3 * kPB];
+    const int co2 = row[4 * kPB], cg2 = row[5 * kPB];
     if constexpr (RGB) {
       const size_t pitch = static_cast<size_t>(im.bx) * 12;  // W * 3 bytes
       uint8_t *o = out + im.out_off + pitch * 4 * (ty * 32 + r) + 12 * static_cast<size_t>(tx * 32 + lane);
       store_rgb_block(o, pitch, y1, co1, cg1, y2, co2, cg2, word[i]);
     } else {
-      const uint32_t ep1 = ycocg_to_565(y1, co1, cg1), ep2 = ycocg_to_565(y2, co2, cg2);
-      *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) =
-          make_uint2(ep1 | (ep2 << 16), word[i]);
+      // The low 16 bits of each endpoint, packed by one byte permute.
+      const uint32_t ep = __byte_perm(ycocg_to_565(y1, co1, cg1), ycocg_to_565(y2, co2, cg2), 0x5410);
+      *reinterpret_cast<uint2 *>(out + im.out_off + static_cast<size_t>(p) * 8) = make_uint2(ep, word[i]);
     }
   }
   if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) flag_error(err, image_err, kErrPalette);

@@ -139,6 +139,7 @@ struct gst_ctx {
   bool hs_used = false;
   gst::host::EncodeState *enc = nullptr;  // encoder calls (gst_encode_api.cpp)
   bool enc_hist_match = false;            // encoder byte counts: merge equal lanes before the atomic
+  bool balance_items = true;              // cut rANS items to fill one wave where that pays (plan_layout)
   bool inject_encode_stall = false;       // fault injection for tests: group 1 never publishes its size
 };
 
@@ -257,20 +258,62 @@ gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, const
   return GST_OK;
 }
 
-PlanLayout plan_layout(const gst_header *hdrs, int n) {
+uint64_t total_blocks(const gst_header *hdrs, int n) {
+  uint64_t b = 0;
+  for (int i = 0; i < n; ++i) b += image_blocks(hdrs[i]);
+  return b;
+}
+
+PlanLayout plan_layout(const gst_header *hdrs, int n, uint32_t capacity) {
   PlanLayout L;
   L.lay.resize(n);
   L.scratch_bytes = 0;
   L.n_rans = L.n_tiles = 0;
+  L.items.assign(4 * size_t(n), 0);
+  std::vector<uint32_t> groups(4 * size_t(n));
+  uint64_t total_groups = 0, min_items = 0;
   for (int i = 0; i < n; ++i) {
     L.lay[i] = scratch_layout(hdrs[i]);
     L.scratch_bytes += L.lay[i].total;
     const uint64_t B = image_blocks(hdrs[i]);
-    const uint64_t groups[4] = {2 * B / kSymsPerGroup, 4 * B / kSymsPerGroup, hdrs[i].palette_bytes / kSymsPerGroup,
-                                B / kSymsPerGroup};
-    for (uint64_t G : groups) L.n_rans += uint32_t((G + kGroupsPerRansCta - 1) / kGroupsPerRansCta);
+    const uint64_t g[4] = {2 * B / kSymsPerGroup, 4 * B / kSymsPerGroup, hdrs[i].palette_bytes / kSymsPerGroup,
+                           B / kSymsPerGroup};
+    for (int s = 0; s < 4; ++s) {
+      groups[4 * size_t(i) + s] = uint32_t(g[s]);
+      L.items[4 * size_t(i) + s] = uint32_t((g[s] + kGroupsPerRansCta - 1) / kGroupsPerRansCta);
+      total_groups += g[s];
+      min_items += L.items[4 * size_t(i) + s];
+    }
     L.n_tiles += uint32_t(B / 1024);
   }
+  // Runs of 4 groups leave the last SMs of a one-wave launch with a CTA more
+  // than the others (1083 CTAs of a 8192x8192 texture on 8 x 152 places:
+  // 19 SMs hold 8 CTAs, the rest 7, and those 19 end the kernel several
+  // microseconds late).  Where the work fills the wave with items of 3.5
+  // groups or more, cut the sections into exactly `capacity` items instead:
+  // one more item at a time to the section whose items are largest on
+  // average.  (Smaller items cost more than the balance gains: the 64-image
+  // batch at 3.2 groups an item measured slower.)
+  if (capacity > 0 && min_items < capacity && 2 * total_groups >= 7 * uint64_t(capacity)) {
+    // Max-heap of sections by average item size: section a ranks below b
+    // when G_a / k_a < G_b / k_b.
+    auto below = [&](size_t a, size_t b) {
+      return uint64_t(groups[a]) * L.items[b] < uint64_t(groups[b]) * L.items[a];
+    };
+    std::vector<size_t> heap;
+    for (size_t k = 0; k < groups.size(); ++k)
+      if (groups[k] > L.items[k]) heap.push_back(k);
+    std::make_heap(heap.begin(), heap.end(), below);
+    for (uint64_t extra = capacity - min_items; extra > 0 && !heap.empty(); --extra) {
+      std::pop_heap(heap.begin(), heap.end(), below);
+      const size_t k = heap.back();
+      ++L.items[k];
+      if (groups[k] > L.items[k]) std::push_heap(heap.begin(), heap.end(), below);
+      else heap.pop_back();
+    }
+    L.balanced = true;
+  }
+  for (uint32_t k : L.items) L.n_rans += k;
   L.off_images = align_up(sizeof(GstPlanHead), 128);
   L.off_rans = L.off_images + sizeof(GstImageDesc) * n;
   L.off_tiles = align_up(L.off_rans + sizeof(GstRansItem) * L.n_rans, 16);
@@ -331,9 +374,14 @@ void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph,
       in += lens[s];
       o += syms[s];
       by_section.push_back({uint64_t(lens[s]) * 16 / std::max<uint32_t>(1u, d.sec_groups[s]), ri, 0});
-      for (uint32_t g = 0; g < d.sec_groups[s]; g += kGroupsPerRansCta)
-        rans[ri++] = {uint32_t(i), uint32_t(s), g, uint16_t(std::min(kGroupsPerRansCta, d.sec_groups[s] - g)),
-                      uint16_t(kStreamsPerGroup)};
+      // L.items[4 i + s] items of near-equal size (runs of 4 groups and a
+      // shorter last one when the layout is not balanced).
+      const uint32_t G = d.sec_groups[s], k = L.items[4 * size_t(i) + s];
+      for (uint32_t j = 0, g = 0; j < k; ++j) {
+        const uint32_t m = L.balanced ? G / k + (j < G % k ? 1u : 0u) : std::min(kGroupsPerRansCta, G - g);
+        rans[ri++] = {uint32_t(i), uint32_t(s), g, uint16_t(m), uint16_t(kStreamsPerGroup)};
+        g += m;
+      }
       by_section.back().count = ri - by_section.back().first;
     }
     d.bx = h.width / 4;
@@ -358,6 +406,10 @@ void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph,
   uint32_t k = 0;
   for (const SectionItems &sec : by_section)
     for (uint32_t j = 0; j < sec.count; ++j) order[k++] = sec.first + j;
+  // Balanced items: the larger first (by cost within a size), so that the
+  // launch's rounds of CTAs over the SMs deal every SM the same mix.
+  if (L.balanced)
+    std::stable_sort(order, order + k, [&](uint32_t a, uint32_t b) { return rans[a].ngroups > rans[b].ngroups; });
 }
 
 GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) {
@@ -383,7 +435,7 @@ GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) 
 gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8_t *d_cmp, uint8_t *d_out,
                         cudaStream_t stream, bool rgb = false) {
   const bool cap = capturing(stream);
-  const PlanLayout L = plan_layout(hdrs, n);
+  const PlanLayout L = plan_layout(hdrs, n, plan_capacity(ctx, tuning_for_locked(ctx, total_blocks(hdrs, n))));
   gst_status st = acquire_scratch(ctx, L.scratch_bytes, stream, cap);
   if (st != GST_OK) return st;
   PlanBuf *pb = nullptr;
@@ -465,6 +517,9 @@ void ctx_set_timed(gst_ctx *ctx, int kernels, int launches) {
 }
 const char **ctx_timed_names(gst_ctx *ctx) { return ctx->timed_names; }
 bool ctx_enc_hist_match(gst_ctx *ctx) { return ctx->enc_hist_match; }
+uint32_t plan_capacity(const gst_ctx *ctx, const GstTuning &t) {
+  return ctx->balance_items ? rans_wave_capacity(t) : 0;
+}
 bool ctx_inject_encode_stall(gst_ctx *ctx) { return ctx->inject_encode_stall; }
 GstTuning ctx_tuning(gst_ctx *ctx) {
   std::lock_guard<std::mutex> lock(ctx->mu);
@@ -488,6 +543,8 @@ struct gst_batch {
   uint8_t *scratch = nullptr;
   bool tuned = false;  // tuning set by gst_batch_autotune / gst_batch_set_tuning
   GstTuning tuning;
+  uint32_t plan_cap = 0;       // the one-wave capacity the plan's rANS items were cut for
+  size_t plan_alloc = 0;       // bytes allocated at plan_d
   cudaGraphExec_t graph = nullptr;
   const void *graph_cmp = nullptr;
   void *graph_out = nullptr;
@@ -502,6 +559,7 @@ struct gst_batch {
   std::vector<int> hm_cut;
   std::vector<PlanLayout> hm_lay;
   std::vector<size_t> hm_plan_off;
+  uint32_t hm_cap = 0;  // the one-wave capacity the per-chunk plans were cut for
   std::vector<size_t> hm_scr_off;  // chunk c's scratch: b->scratch + hm_scr_off[c], disjoint per chunk
   cudaStream_t hm_stream[4] = {};  // copy in, decode (even chunks), copy out, decode (odd chunks)
   cudaGraphExec_t hm_graph = nullptr;
@@ -521,10 +579,52 @@ bool valid_tuning(int blocks_per_sm, int stage_words, int persistent = 0) {
          stage_words <= int(kMaxStageWords) && (stage_words & 7) == 0 && (persistent == 0 || persistent == 1);
 }
 
-// Launches the batch's kernels under `t`; the caller holds ctx->mu.
+// Re-cuts the batch's rANS items for the one-wave capacity of tuning `t` when
+// that differs from the one the plan was cut for (any cut decodes correctly;
+// a balanced one is faster).  Waits for the device first, since earlier
+// launches may still read the plan, and drops the captured graph (its rANS
+// grid has the old item count).  The caller holds ctx->mu.
+cudaError_t ensure_plan_locked(gst_batch *b, const GstTuning &t) {
+  const uint32_t cap = plan_capacity(b->ctx, t);
+  if (cap == b->plan_cap) return cudaSuccess;
+  const int n = int(b->hdrs.size());
+  PlanLayout L = plan_layout(b->hdrs.data(), n, cap);
+  b->plan_cap = cap;
+  if (L.balanced == b->layout.balanced && L.items == b->layout.items) return cudaSuccess;  // the same cut
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess && L.bytes > b->plan_alloc) {
+    cudaFree(b->plan_d);
+    b->plan_d = nullptr;
+    b->plan_alloc = 0;
+    e = cudaMalloc(reinterpret_cast<void **>(&b->plan_d), L.bytes);
+    if (e == cudaSuccess) b->plan_alloc = L.bytes;
+  }
+  if (e != cudaSuccess) {
+    b->plan_cap = ~0u;  // retried on the next launch
+    return e;
+  }
+  std::vector<uint8_t> plan(L.bytes);
+  write_plan(L, b->hdrs.data(), n, plan.data(), nullptr, nullptr, nullptr);
+  e = cudaMemcpy(b->plan_d, plan.data(), L.bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    b->plan_cap = ~0u;
+    return e;
+  }
+  b->layout = std::move(L);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  return cudaSuccess;
+}
+
+// Launches the batch's kernels under `t`; the caller holds ctx->mu.  Outside
+// stream capture the plan is first re-cut for `t` where that pays.
 cudaError_t batch_launch_locked(gst_batch *b, const void *d_cmp, void *d_out, cudaStream_t st, const GstTuning &t,
                                 cudaEvent_t *ev) {
   gst_ctx *ctx = b->ctx;
+  if (!capturing(st)) {
+    const cudaError_t e = ensure_plan_locked(b, t);
+    if (e != cudaSuccess) return e;
+  }
   GstPlanView view = plan_view(b->layout, b->plan_d, ctx->status_d);
   view.wait_limit_ns = ctx->wait_limit_ns;
   return launch_decode(static_cast<const uint8_t *>(d_cmp), b->scratch, static_cast<uint8_t *>(d_out), view, st,
@@ -808,7 +908,9 @@ gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const
   size_t scratch = 0;
   std::vector<PlanLayout> lay(nc);
   for (int c = 0; c < nc; ++c) {
-    lay[c] = plan_layout(hdrs + cut[c], cut[c + 1] - cut[c]);
+    const int m = cut[c + 1] - cut[c];
+    const uint32_t cap = plan_capacity(ctx, tuning_for_locked(ctx, total_blocks(hdrs + cut[c], m)));
+    lay[c] = plan_layout(hdrs + cut[c], m, cap);
     scratch = std::max(scratch, lay[c].scratch_bytes);
   }
   // A previous call's copies out of the mirrors must be done before this
@@ -989,12 +1091,14 @@ gst_status gst_batch_create(gst_ctx *ctx, const gst_header *hdrs, int n, gst_bat
   gst_batch *b = new gst_batch();
   b->ctx = ctx;
   b->hdrs.assign(hdrs, hdrs + n);
-  b->layout = plan_layout(hdrs, n);
+  b->plan_cap = plan_capacity(ctx, tuning_for_locked(ctx, total_blocks(hdrs, n)));
+  b->layout = plan_layout(hdrs, n, b->plan_cap);
   b->compressed_bytes = gst_batch_layout_bytes(hdrs, n);
   for (int i = 0; i < n; ++i) b->out_bytes += size_t(image_blocks(hdrs[i])) * 8;
   std::vector<uint8_t> plan(b->layout.bytes);
   write_plan(b->layout, hdrs, n, plan.data(), nullptr, nullptr, nullptr);
   cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&b->plan_d), b->layout.bytes);
+  if (e == cudaSuccess) b->plan_alloc = b->layout.bytes;
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void **>(&b->scratch), std::max<size_t>(b->layout.scratch_bytes, 256));
   if (e == cudaSuccess) e = cudaMemcpy(b->plan_d, plan.data(), b->layout.bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -1021,6 +1125,8 @@ void gst_batch_destroy(gst_batch *b) {
   delete b;
 }
 
+int gst_batch_rans_items(const gst_batch *b) { return b ? int(b->layout.n_rans) : 0; }
+
 size_t gst_batch_device_bytes(const gst_batch *b) {
   return b ? b->layout.bytes + b->layout.scratch_bytes : 0;
 }
@@ -1043,6 +1149,11 @@ gst_status gst_batch_graph_launch(gst_batch *b, const void *d_cmp, void *d_out, 
   if (!b || !d_cmp || !d_out) return GST_E_ARG;
   gst_ctx *ctx = b->ctx;
   cudaSetDevice(ctx->device);
+  if (!capturing(static_cast<cudaStream_t>(stream))) {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    const cudaError_t e = ensure_plan_locked(b, batch_tuning(b));  // may drop the graph: captured again below
+    if (e != cudaSuccess) return cuda_status(e);
+  }
   if (!b->graph || b->graph_cmp != d_cmp || b->graph_out != d_out || b->graph_tuning != batch_tuning(b)) {
     // Capture the launch sequence once per (input, output) pair.
     cudaStream_t cs = nullptr;
@@ -1108,14 +1219,16 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
       if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_status(e);
   }
-  if (b->hm_chunks != chunks) {
-    // Per-chunk plans with absolute addresses in the mirrors, uploaded once.
+  const uint32_t hm_cap = plan_capacity(ctx, tuning);
+  if (b->hm_chunks != chunks || b->hm_cap != hm_cap) {
+    // Per-chunk plans with absolute addresses in the mirrors, uploaded once
+    // per chunk count and one-wave capacity.
     const std::vector<int> cut = chunk_cuts(hdrs, n, chunks, blocks);
     const int nc = int(cut.size()) - 1;
     std::vector<PlanLayout> lay(nc);
     std::vector<size_t> off(nc + 1, 0);
     for (int c = 0; c < nc; ++c) {
-      lay[c] = plan_layout(hdrs + cut[c], cut[c + 1] - cut[c]);
+      lay[c] = plan_layout(hdrs + cut[c], cut[c + 1] - cut[c], hm_cap);
       off[c + 1] = align_up(off[c] + lay[c].bytes, 256);
     }
     if (b->hm_graph) cudaGraphExecDestroy(b->hm_graph);
@@ -1146,6 +1259,7 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
     b->hm_lay = std::move(lay);
     b->hm_plan_off = std::move(off);
     b->hm_chunks = chunks;
+    b->hm_cap = hm_cap;
   }
   if (!b->hm_graph || b->hm_graph_cmp != h_cmp || b->hm_graph_out != h_out || b->hm_graph_tuning != tuning) {
     // Capture the copies in, decodes and copies out of every chunk, enqueued
@@ -1261,6 +1375,11 @@ gst_status gst_set_option(gst_ctx *ctx, const char *name, int value) {
   if (strcmp(name, "persistent_wait_us") == 0) {
     if (value < 0 || value > 2000000) return GST_E_ARG;
     ctx->wait_limit_ns = uint64_t(value) * 1000u;
+    return GST_OK;
+  }
+  if (strcmp(name, "balance_rans_items") == 0) {
+    if (value != 0 && value != 1) return GST_E_ARG;
+    ctx->balance_items = value != 0;
     return GST_OK;
   }
   if (strcmp(name, "encode_hist_match") == 0) {

@@ -54,6 +54,11 @@ cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_o
                           cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning,
                           const char **names = nullptr);
 
+// CTAs of the two-kernel form's rANS kernel that the device holds at once
+// under `t` (SMs x resident CTAs per SM, from the occupancy calculator); 0 for
+// the persistent form.
+uint32_t rans_wave_capacity(const GstTuning &t);
+
 namespace host {
 
 size_t align_up(size_t x, size_t a);
@@ -61,6 +66,7 @@ gst_status cuda_status(cudaError_t e);
 // Dimension and size rules a header must meet before anything is launched.
 gst_status check_header(const gst_header &h);
 uint64_t image_blocks(const gst_header &h);
+uint64_t total_blocks(const gst_header *hdrs, int n);
 uint64_t section_bytes(const gst_header &h);
 
 // Scratch layout of one image: decoded symbols, chunk prefixes, group sums.
@@ -76,14 +82,27 @@ struct PlanLayout {
   uint32_t n_rans, n_tiles;
   size_t scratch_bytes;
   std::vector<ScratchLayout> lay;
+  // rANS items of image i's section s at [4 i + s]; `balanced` when their
+  // sizes were evened out to fill a launch's one-wave capacity exactly.
+  std::vector<uint32_t> items;
+  bool balanced = false;
 };
-PlanLayout plan_layout(const gst_header *hdrs, int n);
+// `capacity`: how many rANS CTAs of the intended launch are resident at once
+// (rans_wave_capacity), or 0.  Where the work fills that one wave with items
+// of 3.5 groups or more on average, the sections are cut into exactly
+// `capacity` items of near-equal size instead of runs of 4 groups, so that
+// every SM holds the same number of CTAs and of groups.
+PlanLayout plan_layout(const gst_header *hdrs, int n, uint32_t capacity = 0);
 // out_block_bytes: output bytes per block, 8 (DXT1) or 48 (RGB8).
 void write_plan(const PlanLayout &L, const gst_header *hdrs, int n, uint8_t *ph, const uint64_t *freq_at,
                 const uint64_t *body_at, const uint64_t *out_at, uint32_t out_block_bytes = 8);
 GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d);
 
 int ctx_device(const gst_ctx *ctx);
+// The one-wave capacity plan_layout balances rANS items for under tuning `t`
+// (rans_wave_capacity), or 0 where the context's "balance_rans_items" option
+// is off.
+uint32_t plan_capacity(const gst_ctx *ctx, const GstTuning &t);
 GstTuning ctx_tuning(gst_ctx *ctx);
 // The configuration of a launch of `blocks` DXT1 blocks: its size class's
 // entry where one is set, else the context's.

@@ -30,6 +30,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
 
 #include "gst_host.h"
 #include "gst_plan.h"
@@ -900,6 +902,37 @@ __global__ void __launch_bounds__(kPersistentThreads, 8) gst_persistent_kernel(c
 // the first kernel and ev[i + 1] after kernel i (instrumentation).  `tuning`
 // selects the form (two kernels, or the persistent kernel where the plan has
 // its sync words), the rANS kernel's register budget and the staging depth.
+uint32_t rans_wave_capacity(const GstTuning &t) {
+  if (t.persistent || t.stage_words < kMinStageWords || t.stage_words > kMaxStageWords) return 0;
+  const int minb = t.blocks_per_sm >= 14 ? 16 : t.blocks_per_sm >= 10 ? 12 : 8;  // as launch_decode picks
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  const uint64_t key = (uint64_t(dev) << 40) | (uint64_t(minb) << 32) | t.stage_words;
+  static std::mutex mu;
+  static std::map<uint64_t, uint32_t> cache;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  int sms = 0, per_sm = 0;
+  const size_t smem = rans_smem_bytes(t.stage_words);
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) {
+    if (minb == 16) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gst_rans_kernel<16>, 128, smem);
+    else if (minb == 12) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gst_rans_kernel<12>, 128, smem);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gst_rans_kernel<8>, 128, smem);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // a failed query leaves the layout unbalanced, nothing else
+    return 0;
+  }
+  const uint32_t cap = uint32_t(std::max(0, sms * per_sm));
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = cap;
+  return cap;
+}
+
 cudaError_t launch_decode(const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, GstPlanView plan,
                           cudaStream_t stream, int *launches, cudaEvent_t *ev, const GstTuning &tuning,
                           const char **names) {

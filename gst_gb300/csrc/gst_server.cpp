@@ -254,7 +254,9 @@ bool gst_server::launch(Slot &s, std::unique_lock<std::mutex> &lk) {
 
   const int n = int(s.ids.size());
   NvtxRange range("gst server launch");
-  const PlanLayout L = plan_layout(s.hdrs.data(), n);
+  GstTuning tuning = ctx_tuning_for(ctx, total_blocks(s.hdrs.data(), n));
+  tuning.persistent = 0;
+  const PlanLayout L = plan_layout(s.hdrs.data(), n, plan_capacity(ctx, tuning));
   gst_status st = grow(&s.scratch, nullptr, &s.scratch_cap, L.scratch_bytes);
   if (st == GST_OK && s.plan_cap < L.bytes) {
     cudaFree(s.plan_d);
@@ -281,8 +283,6 @@ bool gst_server::launch(Slot &s, std::unique_lock<std::mutex> &lk) {
     // The launch's size class gives CTAs per SM and staging depth; launches
     // on different slots run side by side, so the two-kernel form is kept
     // (a persistent launch fills every SM and would hold the others back).
-    GstTuning tuning = ctx_tuning_for(ctx, uint64_t(L.n_tiles) * 1024);
-    tuning.persistent = 0;
     if (e == cudaSuccess)
       e = launch_decode(nullptr, s.scratch, nullptr, plan_view(L, s.plan_d, s.status_d), s.stream, &nl, nullptr,
                         tuning);

@@ -43,8 +43,8 @@ EXPORTED_SYMBOLS = (
     "gst_decompress_dxt", "gst_load_compressed_dxt", "gst_load_compressed_dxts", "gst_load_rgb", "gst_load_rgbs",
     "gst_load_host_dxts",
     "gst_batch_layout_bytes", "gst_pack_batch", "gst_decode_rans_groups",
-    "gst_batch_create", "gst_batch_destroy", "gst_batch_device_bytes", "gst_batch_launch",
-    "gst_batch_graph_launch", "gst_batch_host_launch", "gst_batch_autotune", "gst_size_class",
+    "gst_batch_create", "gst_batch_destroy", "gst_batch_device_bytes", "gst_batch_rans_items",
+    "gst_batch_launch", "gst_batch_graph_launch", "gst_batch_host_launch", "gst_batch_autotune", "gst_size_class",
     "gst_set_class_tuning", "gst_get_class_tuning", "gst_autotune_class", "gst_save_class_tuning",
     "gst_load_class_tuning", "gst_batch_set_tuning", "gst_load_compressed_dxt_static",
     "gst_sync_status", "gst_last_launch_count", "gst_set_profiling", "gst_kernel_times", "gst_set_option",
@@ -180,6 +180,7 @@ def load_library() -> ctypes.CDLL:
         "gst_batch_create": (I, [P, HP, I, ctypes.POINTER(P)]),
         "gst_batch_destroy": (None, [P]),
         "gst_batch_device_bytes": (S, [P]),
+        "gst_batch_rans_items": (I, [P]),
         "gst_batch_launch": (I, [P, P, P, P]),
         "gst_batch_autotune": (I, [P, P, P, P, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)]),
         "gst_batch_set_tuning": (I, [P, I, I, I]),
@@ -329,6 +330,11 @@ class ResidentBatch:
     @property
     def device_bytes(self) -> int:
         return int(load_library().gst_batch_device_bytes(self._h))
+
+    @property
+    def rans_items(self) -> int:
+        """gst_batch_rans_items: rANS CTAs of the next two-kernel launch."""
+        return int(load_library().gst_batch_rans_items(self._h))
 
     def launch(self, cmp_data, output, stream=None, graph: bool = False) -> None:
         fn = load_library().gst_batch_graph_launch if graph else load_library().gst_batch_launch

@@ -143,6 +143,11 @@ typedef struct gst_batch gst_batch;
 gst_status gst_batch_create(gst_ctx *ctx, const gst_header *hdrs, int n, gst_batch **batch);
 void gst_batch_destroy(gst_batch *batch);
 size_t gst_batch_device_bytes(const gst_batch *batch);
+/* rANS CTAs of the batch's next two-kernel launch (its plan's rANS items):
+ * runs of up to 4 groups of one section, or -- where the batch's groups fill
+ * the launch's one wave of CTAs with 3.5 groups an item or more -- exactly
+ * that wave's capacity of near-equal items.  0 for a null batch. */
+int gst_batch_rans_items(const gst_batch *batch);
 gst_status gst_batch_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
 gst_status gst_batch_graph_launch(gst_batch *batch, const void *d_cmp, void *d_out, void *stream);
 
@@ -286,6 +291,14 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
  *                         of an encoder group's look-back wait for the sizes
  *                         before it, microseconds (0 = 2 s, at most
  *                         2,000,000).
+ *   "balance_rans_items"  1 (default): where a launch's rANS groups fill its
+ *                         one wave of CTAs (SMs x resident CTAs per SM of the
+ *                         two-kernel form) with 3.5 groups an item or more,
+ *                         the plan cuts them into exactly that many items of
+ *                         near-equal size, so that every SM holds the same
+ *                         work; 0: runs of 4 groups of one section always.
+ *                         Resident batches re-cut their plan at their next
+ *                         launch outside stream capture.
  *   "encode_hist_match"   encoder byte counts (gst_encode.h): 0 (default)
  *                         issues one shared-memory atomic per byte; 1 merges
  *                         the lanes of a warp holding the same byte first

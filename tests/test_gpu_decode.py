@@ -70,6 +70,45 @@ def test_reference_encoded_workloads(gpu_ctx):
             assert SHA(decoder.decompress_dxt(gpu_ctx, im.stream)) == im.decoded_sha256
 
 
+def test_balanced_rans_items_follow_the_tuning():
+    """The 8192x8192 texture's 4331 groups fill 8 CTAs x 152 SMs with items of
+    3.56 groups: at 8 CTAs per SM its plan is cut into equal items, at 12 it
+    is not (2.4 groups an item), and switching the tuning re-cuts the resident
+    plan; every form decodes to the reference decoder's blocks, direct, from
+    the captured graph and through the host pipeline."""
+    big = workloads.ref_large()
+    ctx = decoder.GPUContext(0)
+    try:
+        hdrs, packed = decoder.pack_batch([big.stream])
+        d_cmp = torch.from_numpy(packed).cuda()
+        d_out = torch.empty(hdrs[0].dxt_bytes, dtype=torch.uint8, device="cuda")
+        rb = decoder.ResidentBatch(ctx, hdrs)
+        s = torch.cuda.Stream()
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        for bps, words in [(8, 1528), (12, 1016), (8, 1528)]:
+            rb.set_tuning(bps, words, 0)
+            for graph in (False, True):
+                d_out.zero_()
+                rb.launch(d_cmp, d_out, s, graph=graph)
+                s.synchronize()
+                assert decoder.sync_status(ctx, s) == decoder.GST_OK
+                assert SHA(d_out.cpu().numpy()) == big.decoded_sha256, (bps, words, graph)
+                # runs of 4 groups: 1083 items; balanced (8 CTAs per SM): one item
+                # per place of the wave
+                if bps == 8:
+                    assert 1083 < rb.rans_items <= 8 * sms, rb.rans_items
+                else:
+                    assert rb.rans_items == 1083, rb.rans_items
+        h_cmp = torch.from_numpy(packed).pin_memory()
+        h_out = torch.zeros(hdrs[0].dxt_bytes, dtype=torch.uint8).pin_memory()
+        rb.host_launch(h_cmp, h_out, 1, s)
+        s.synchronize()
+        assert SHA(h_out.numpy()) == big.decoded_sha256
+        rb.close()
+    finally:
+        ctx.close()
+
+
 def test_non_power_of_two_block_count_matches_encoder(gpu_ctx, golden):
     # The GPU computes the exact index prefix sum: it reproduces the encoder's
     # blocks, where the reference's staged scan differs in the last block.

@@ -50,8 +50,8 @@ METRIC = "decoded Mpix/s & DXT1 GB/s, batched vs per-image, bit-exact; p50/p99 l
 # cold-cache bytes: the tile kernel's reads are the rANS kernel's symbols,
 # which in an unprofiled launch stay in L2).
 NCU_TRAFFIC_BATCHED = {
-    "gst_rans_kernel": 16.78e6 + 1.98e6,
-    "gst_tile_kernel": 53.90e6 + 6.30e6,
+    "gst_rans_kernel": 16.78e6 + 2.94e6,
+    "gst_tile_kernel": 53.90e6 + 6.52e6,
 }
 FLUSH_BYTES = 256 << 20
 
@@ -1079,7 +1079,7 @@ class _null_ctx:
         return False
 
 
-CPU_PASSES = 10          # timed passes of the all-core leg (each pass decodes every sample image once)
+CPU_PASSES = 30          # timed passes of the all-core leg (each pass decodes every sample image once)
 CPU_SINGLE_PASSES = 5   # timed passes of the single-thread leg, over a quarter of the sample
 
 

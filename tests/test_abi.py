@@ -114,6 +114,7 @@ def test_init_without_gpu_fails_cleanly():
     assert lib.gst_init(0, ctypes.byref(h)) == GST_E_CUDA
     assert lib.gst_load_compressed_dxts(None, None, 0, None, None, None) == GST_E_ARG
     assert lib.gst_decompress_dxt(None, None, 0, None, 0) == GST_E_ARG
+    assert lib.gst_batch_rans_items(None) == 0 and lib.gst_batch_device_bytes(None) == 0
     assert lib.gst_status_string(GST_OK) == b"ok"
 
 

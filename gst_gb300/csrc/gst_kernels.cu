@@ -518,6 +518,31 @@ __device__ __forceinline__ void inv53_line(int32_t *p, int step) {
   for (int k = 0; k < L; ++k) p[k * step] = d[k];
 }
 
+// A row of L coefficients (8-byte aligned: even pitch, even plane stride),
+// moved two at a time.
+template <int L>
+__device__ __forceinline__ void inv53_row(int32_t *p) {
+  int32_t s[L], d[L];
+  int2 *q = reinterpret_cast<int2 *>(p);
+#pragma unroll
+  for (int k = 0; k < L / 2; ++k) {
+    const int2 v = q[k];
+    s[2 * k] = v.x;
+    s[2 * k + 1] = v.y;
+  }
+  inv53_lift<L>(s, d);
+#pragma unroll
+  for (int k = 0; k < L / 2; ++k) q[k] = make_int2(d[2 * k], d[2 * k + 1]);
+}
+
+// A row segment of N values from registers to (8-byte aligned) shared memory.
+template <int N>
+__device__ __forceinline__ void store_row(int32_t *p, const int32_t *v) {
+  int2 *q = reinterpret_cast<int2 *>(p);
+#pragma unroll
+  for (int k = 0; k < N / 2; ++k) q[k] = make_int2(v[2 * k], v[2 * k + 1]);
+}
+
 // The 16 coefficients (byte - 128) of a 16-byte chunk: the byte with its top
 // bit flipped, sign-extended by one byte permute.
 __device__ __forceinline__ void unpack16(uint4 cv, int32_t *dst) {
@@ -531,7 +556,11 @@ __device__ __forceinline__ void unpack16(uint4 cv, int32_t *dst) {
   }
 }
 
-constexpr int kPlanePitch = 33;  // row pitch in words: rows and columns both bank-conflict free
+// Row pitch in words: even, so that a thread moves its row two words at a
+// time (8-byte accesses by 16 rows of a half-warp start on 16 different even
+// banks), and columns stay bank-conflict free (a warp's 32 columns of one row
+// are consecutive words).
+constexpr int kPlanePitch = 34;
 // Planes 16 banks apart, so that half-warps working on two planes at once do
 // not collide.
 constexpr int kPlaneWords = 32 * kPlanePitch + 16;
@@ -543,7 +572,7 @@ __device__ __forceinline__ void inv53_level(int32_t *pl) {
 #pragma unroll
   for (int t = threadIdx.x; t < 6 * L; t += NT) {
     const int p = t / L, r = t % L;
-    inv53_line<L>(pl + p * kPlaneWords + r * kPlanePitch, 1);
+    inv53_row<L>(pl + p * kPlaneWords + r * kPlanePitch);
   }
   __syncthreads();
 #pragma unroll
@@ -561,7 +590,7 @@ __device__ __forceinline__ void inv53_level_group(int32_t *pl) {
 #pragma unroll
   for (int t = threadIdx.x; t < 6 * L; t += NG) {
     const int p = t / L, r = t % L;
-    inv53_line<L>(pl + p * kPlaneWords + r * kPlanePitch, 1);
+    inv53_row<L>(pl + p * kPlaneWords + r * kPlanePitch);
   }
   bar_sync(BAR, NG);
 #pragma unroll
@@ -704,8 +733,7 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
         unpack16(raw_lo[k], v);
         const int q = l & 63;
         int32_t *dst = pl + (l >> 6) * kPlaneWords + (q >> 1) * kPlanePitch + (q & 1) * 16;
-#pragma unroll
-        for (int j = 0; j < 16; ++j) dst[j] = v[j];
+        store_row<16>(dst, v);
       }
     }
   }
@@ -742,27 +770,28 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
       const int p = 2 * warp + (lane >> 4), r = lane & 15;
       int32_t *row = pl + p * kPlaneWords + r * kPlanePitch;
       unpack16(raw_lo[0], sv);
-#pragma unroll
-      for (int j = 0; j < 16; ++j) row[j] = sv[j];
+      store_row<16>(row, sv);
       bar_sync(1, 96);
       inv53_level_group<2, 96, 1>(pl);
       inv53_level_group<4, 96, 1>(pl);
       inv53_level_group<8, 96, 1>(pl);
       inv53_level_group<16, 96, 1>(pl);
 #pragma unroll
-      for (int j = 0; j < 16; ++j) sv[j] = row[j];
+      for (int j = 0; j < 8; ++j) {
+        const int2 v = reinterpret_cast<const int2 *>(row)[j];
+        sv[2 * j] = v.x;
+        sv[2 * j + 1] = v.y;
+      }
       unpack16(raw_hi[0], sv + 16);
       inv53_lift<32>(sv, dv);
-#pragma unroll
-      for (int j = 0; j < 32; ++j) row[j] = dv[j];
+      store_row<32>(row, dv);
     } else if (t < 192) {
       const int w = warp - 3, p = 2 * w + (lane >> 4), r = 16 + (lane & 15);
       int32_t *row = pl + p * kPlaneWords + r * kPlanePitch;
       unpack16(raw_lo[0], sv);
       unpack16(raw_hi[0], sv + 16);
       inv53_lift<32>(sv, dv);
-#pragma unroll
-      for (int j = 0; j < 32; ++j) row[j] = dv[j];
+      store_row<32>(row, dv);
     }
     __syncthreads();
 #pragma unroll
@@ -799,7 +828,7 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
 template <bool RGB>
 __global__ void __launch_bounds__(256, 8) gst_tile_kernel(const uint8_t *__restrict__ scratch, uint8_t *__restrict__ out,
                                                        GstPlanView plan) {
-  __shared__ int32_t pl[6 * kPlaneWords];
+  __shared__ __align__(16) int32_t pl[6 * kPlaneWords];  // 8-byte row accesses
   const GstTileItem it = plan.tiles[blockIdx.x];
   pdl_wait_prerequisites();  // the rANS kernel's symbols (launched right behind it: see launch_decode)
   tile_work<256, false, RGB>(scratch, out, plan.err, plan.image_err ? plan.image_err + it.image : nullptr,
@@ -1073,7 +1102,7 @@ __global__ void __launch_bounds__(128) gst_rans_static_kernel(const uint8_t *__r
 // tile is blockIdx.x.
 __global__ void __launch_bounds__(256) gst_tile_static_kernel(const uint8_t *base, uint8_t *__restrict__ out,
                                                               GstImageDesc im) {
-  __shared__ int32_t pl[6 * kPlaneWords];
+  __shared__ __align__(16) int32_t pl[6 * kPlaneWords];  // 8-byte row accesses
   uint32_t *err = reinterpret_cast<uint32_t *>(const_cast<uint8_t *>(base));
   tile_work<256, false>(base + kStaticHeaderBytes, out, err, nullptr, im, blockIdx.x, pl);
 }

@@ -99,6 +99,13 @@ def test_balanced_rans_items_follow_the_tuning():
                     assert 1083 < rb.rans_items <= 8 * sms, rb.rans_items
                 else:
                     assert rb.rans_items == 1083, rb.rans_items
+        # the context's option turns the cut off: runs of 4 again, same blocks
+        ctx.set_option("balance_rans_items", 0)
+        d_out.zero_()
+        rb.launch(d_cmp, d_out, s, graph=True)
+        s.synchronize()
+        assert rb.rans_items == 1083 and SHA(d_out.cpu().numpy()) == big.decoded_sha256
+        ctx.set_option("balance_rans_items", 1)
         h_cmp = torch.from_numpy(packed).pin_memory()
         h_out = torch.zeros(hdrs[0].dxt_bytes, dtype=torch.uint8).pin_memory()
         rb.host_launch(h_cmp, h_out, 1, s)

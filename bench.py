@@ -86,7 +86,7 @@ def parse_args():
     p.add_argument("--encode-hist-match", type=int, default=0, choices=(0, 1),
                    help="encoder byte counts: merge equal lanes before the atomic (1) or not (0)")
     p.add_argument("--rans-stage-words", type=int, default=1016,
-                   help="staging depth with --rans-blocks-per-sm (a multiple of 8 in [520, 2816])")
+                   help="staging depth with --rans-blocks-per-sm (a multiple of 8 in [520, 4352])")
     return p.parse_args()
 
 

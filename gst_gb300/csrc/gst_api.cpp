@@ -1606,7 +1606,7 @@ gst_status gst_batch_autotune(gst_batch *b, const void *d_cmp, void *d_out, void
   // shallower ones.  The persistent kernel (8 CTAs of 128 threads per SM):
   // its tile buffers hold 2040-word stages.
   static const GstTuning kCandidates[] = {
-      {16, 520, 0}, {12, 520, 0}, {12, 1016, 0}, {8, 1528, 0}, {8, 2040, 0}, {8, 2816, 0},
+      {16, 520, 0}, {12, 520, 0}, {12, 1016, 0}, {8, 1528, 0}, {8, 2040, 0}, {8, 2816, 0}, {8, 4352, 0},
       {8, 1016, 1}, {8, 2040, 1},
   };
   std::lock_guard<std::mutex> lock(ctx->mu);

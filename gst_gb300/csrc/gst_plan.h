@@ -27,7 +27,7 @@ constexpr uint32_t kGroupsPerRansCta = 4;
 // warp's stage starts 16-byte aligned).  Sixteen steps read at most 512 words
 // and a re-stage starts at most one word above the read pointer, so 520 words
 // always cover the next sixteen steps; 2816 keeps seven CTAs per SM.
-constexpr uint32_t kMinStageWords = 520, kMaxStageWords = 2816, kDefaultStageWords = 1016;
+constexpr uint32_t kMinStageWords = 520, kMaxStageWords = 4352, kDefaultStageWords = 1016;
 
 // Launch configuration of a decode.
 constexpr int kSizeClasses = 7;  // launch size classes: up to 2^14 blocks, then x4 each, the last open-ended

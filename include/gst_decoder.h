@@ -277,10 +277,13 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
  *                         (twelve, default) or 14-16 (sixteen).  The
  *                         persistent kernel always runs 8 per SM.
  *   "rans_stage_words"    16-bit renormalisation words each warp stages in
- *                         shared memory: a multiple of 8 in [520, 2816];
+ *                         shared memory: a multiple of 8 in [520, 4352];
  *                         default 1016.  Deeper stages re-stage less often
  *                         but leave room for fewer CTAs per SM (16 CTAs at
- *                         520 words, 13 at 1016, 8 at 2040).
+ *                         520 words, 13 at 1016, 8 at 2040, 5 at 4352, which
+ *                         holds any group whole: for launches of a few
+ *                         groups, where the re-stages are on the critical
+ *                         path).
  *   "persistent"          0 (default): a rANS kernel, then a tile kernel;
  *                         1: one persistent kernel whose CTAs take rANS
  *                         items, then tiles, from a work queue in the plan

@@ -316,8 +316,8 @@ def test_resident_batch_launch_and_graph_replay(gpu_ctx):
     b.close()
 
 
-AUTOTUNED = [(16, 520, 0), (12, 520, 0), (12, 1016, 0), (8, 1528, 0), (8, 2040, 0), (8, 2816, 0), (8, 1016, 1),
-             (8, 2040, 1)]
+AUTOTUNED = [(16, 520, 0), (12, 520, 0), (12, 1016, 0), (8, 1528, 0), (8, 2040, 0), (8, 2816, 0), (8, 4352, 0),
+             (8, 1016, 1), (8, 2040, 1)]
 TUNINGS = AUTOTUNED + [(10, 904, 0), (12, 2816, 1)]
 
 
@@ -381,7 +381,7 @@ def test_batch_autotune_and_tuning_validation(gpu_ctx):
             b.launch(d_cmp, d_out, side, graph=graph)
             assert decoder.sync_status(gpu_ctx, side) == decoder.GST_OK, (tuning, graph)
             assert np.array_equal(d_out.cpu().numpy().view(np.uint64), want), (tuning, graph)
-    for bad in ((12, 512, 0), (12, 1001, 0), (12, 2824, 0), (17, 1016, 0), (0, 1016, 0), (12, 1016, 2)):
+    for bad in ((12, 512, 0), (12, 1001, 0), (12, 4360, 0), (17, 1016, 0), (0, 1016, 0), (12, 1016, 2)):
         with pytest.raises(decoder.GstError) as ei:
             b.set_tuning(*bad)
         assert ei.value.status == decoder.GST_E_ARG

@@ -116,6 +116,58 @@ def test_balanced_rans_items_follow_the_tuning():
         ctx.close()
 
 
+EDGE_DIMS = [(512, 256), (256, 512), (128, 1024), (1024, 128), (8192, 128), (128, 8192)]
+
+
+def test_smallest_and_thinnest_images(gpu_ctx):
+    """The smallest images the format admits (one index group: 8192 blocks)
+    and one-tile-wide or one-tile-high strips, alone, in one mixed batch, and
+    as RGB8, against the oracle."""
+    imgs = [workloads.encode_image(w, h, 40 + k) for k, (w, h) in enumerate(EDGE_DIMS)]
+    want = []
+    for im in imgs:
+        st, dec = oracle.decode(im.stream, oracle.SCAN_EXACT)
+        assert st == 0
+        want.append(np.ascontiguousarray(dec).reshape(-1).view(np.uint8))
+        assert np.array_equal(decoder.decompress_dxt(gpu_ctx, im.stream).reshape(-1), want[-1]), (im.width, im.height)
+    st, outs = batch_decode(gpu_ctx, [im.stream for im in imgs])
+    assert st == decoder.GST_OK
+    for im, o, w in zip(imgs, outs, want):
+        assert np.array_equal(o, w), (im.width, im.height)
+    im = imgs[-1]
+    hdrs, packed = decoder.pack_batch([im.stream])
+    rgb = torch.zeros(im.width * im.height * 3, dtype=torch.uint8, device="cuda")
+    decoder.load_rgb(gpu_ctx, hdrs[0], torch.from_numpy(packed).cuda(), rgb)
+    assert decoder.sync_status(gpu_ctx) == decoder.GST_OK
+    assert np.array_equal(rgb.cpu().numpy(), oracle.decode_rgb(im.stream, oracle.SCAN_EXACT)[1])
+
+
+def test_16384_square_round_trip(gpu_ctx):
+    """A 16384x16384 texture (16.8 M blocks, 134 MB of DXT1; four times the
+    8192x8192 configuration): smooth endpoints and indices drawn from 256
+    words, made into a GST stream by the GPU stream producer, decoded on the
+    GPU, checked against the oracle and against the blocks it came from."""
+    from gst_gb300 import entropy
+    side = 16384
+    n = side // 4
+    rng = np.random.default_rng(16384)
+    y, x = np.mgrid[0:n, 0:n].astype(np.int64)
+    r = (x * 31) // n
+    g = (y * 63) // n
+    b = ((x + y) * 31) // (2 * n)
+    ep1 = (r << 11) | (g << 5) | b
+    ep2 = (np.minimum(r + 2, 31) << 11) | (np.maximum(g - 3, 0) << 5) | np.minimum(b + 1, 31)
+    words = rng.integers(0, 1 << 32, 256, dtype=np.uint64)
+    blocks = (ep1.astype(np.uint64) | (ep2.astype(np.uint64) << np.uint64(16)) |
+              (words[rng.integers(0, 256, n * n)].reshape(n, n) << np.uint64(32))).reshape(-1)
+    stream = entropy.compress_dxt(gpu_ctx, side, side, blocks)
+    got = decoder.decompress_dxt(gpu_ctx, stream)
+    st, want = oracle.decode(stream, oracle.SCAN_EXACT, nthreads=8)
+    assert st == 0
+    assert np.array_equal(got.view(np.uint64), np.ascontiguousarray(want).reshape(-1).view(np.uint64))
+    assert np.array_equal(got.view(np.uint64), blocks)
+
+
 def test_non_power_of_two_block_count_matches_encoder(gpu_ctx, golden):
     # The GPU computes the exact index prefix sum: it reproduces the encoder's
     # blocks, where the reference's staged scan differs in the last block.

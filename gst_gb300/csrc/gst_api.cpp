@@ -140,6 +140,7 @@ struct gst_ctx {
   gst::host::EncodeState *enc = nullptr;  // encoder calls (gst_encode_api.cpp)
   bool enc_hist_match = false;            // encoder byte counts: merge equal lanes before the atomic
   bool balance_items = true;              // cut rANS items to fill one wave where that pays (plan_layout)
+  bool tuning_explicit = false;           // the tuning options were set: untuned launches use ctx->tuning
   bool inject_encode_stall = false;       // fault injection for tests: group 1 never publishes its size
 };
 
@@ -157,6 +158,32 @@ int size_class(uint64_t blocks) {
 GstTuning tuning_for_locked(const gst_ctx *ctx, uint64_t blocks) {
   const int c = size_class(blocks);
   return ctx->class_set[c] ? ctx->class_tuning[c] : ctx->tuning;
+}
+
+// The configuration of a launch of these images: their size class's entry
+// where one is set, else the context's where its tuning options were set.
+// Otherwise the deepest stages whose one wave of CTAs still holds the
+// launch's rANS items: a launch of a few images needs no more CTAs per SM
+// than that, and each re-stage it avoids lies on its critical path (64
+// one-image calls of the batch: 2.35 ms at 8 CTAs/SM with 4352-word stages,
+// 2.72 ms at 12 with 1016).  Larger launches keep the context's default.
+GstTuning launch_tuning_locked(const gst_ctx *ctx, const gst_header *hdrs, int n) {
+  const int c = size_class(total_blocks(hdrs, n));
+  if (ctx->class_set[c]) return ctx->class_tuning[c];
+  if (ctx->tuning_explicit) return ctx->tuning;
+  uint64_t items = 0;  // runs of 4 groups
+  for (int i = 0; i < n; ++i) {
+    const uint64_t B = image_blocks(hdrs[i]);
+    for (uint64_t G : {2 * B / kSymsPerGroup, 4 * B / kSymsPerGroup, uint64_t(hdrs[i].palette_bytes) / kSymsPerGroup,
+                       B / kSymsPerGroup})
+      items += (G + kGroupsPerRansCta - 1) / kGroupsPerRansCta;
+  }
+  static const GstTuning kFew[] = {{8, 4352, 0}, {8, 1528, 0}};
+  for (const GstTuning &t : kFew) {
+    const uint32_t cap = rans_wave_capacity(t);
+    if (cap > 0 && items <= cap) return t;
+  }
+  return ctx->tuning;
 }
 
 gst_status cuda_status(cudaError_t e) {
@@ -238,14 +265,13 @@ gst_status acquire_scratch(gst_ctx *ctx, size_t bytes, cudaStream_t stream, bool
 // `view`, whose pointers lie in pb->d.
 gst_status upload_and_launch(gst_ctx *ctx, PlanBuf *pb, size_t plan_bytes, const GstPlanView &view,
                              const uint8_t *d_cmp, uint8_t *d_scratch, uint8_t *d_out, cudaStream_t stream,
-                             bool cap) {
+                             bool cap, const GstTuning &tuning) {
   cudaError_t e = cudaMemcpyAsync(pb->d, pb->h, plan_bytes, cudaMemcpyHostToDevice, stream);
   if (e != cudaSuccess) return cuda_status(e);
   if (!cap) cudaEventRecord(pb->copied, stream);
   cudaEvent_t *ev = (ctx->profiling && !cap) ? ctx->ev : nullptr;
   GstPlanView v = view;
   v.wait_limit_ns = ctx->wait_limit_ns;
-  const GstTuning tuning = tuning_for_locked(ctx, uint64_t(v.n_tiles) * 1024);
   if (ctx->inject_drop_rans && tuning.persistent && v.sync) v.n_rans = 0;
   e = launch_decode(d_cmp, d_scratch, d_out, v, stream, &ctx->last_launches, ev, tuning, ctx->timed_names);
   ctx->timed_kernels = ev ? ctx->last_launches : 0;
@@ -435,7 +461,8 @@ GstPlanView plan_view(const PlanLayout &L, uint8_t *plan_d, uint32_t *status_d) 
 gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8_t *d_cmp, uint8_t *d_out,
                         cudaStream_t stream, bool rgb = false) {
   const bool cap = capturing(stream);
-  const PlanLayout L = plan_layout(hdrs, n, plan_capacity(ctx, tuning_for_locked(ctx, total_blocks(hdrs, n))));
+  const GstTuning tuning = launch_tuning_locked(ctx, hdrs, n);
+  const PlanLayout L = plan_layout(hdrs, n, plan_capacity(ctx, tuning));
   gst_status st = acquire_scratch(ctx, L.scratch_bytes, stream, cap);
   if (st != GST_OK) return st;
   PlanBuf *pb = nullptr;
@@ -445,7 +472,7 @@ gst_status decode_batch(gst_ctx *ctx, const gst_header *hdrs, int n, const uint8
   GstPlanView view = plan_view(L, pb->d, ctx->status_d);
   view.image_err = nullptr;  // the context reports per call
   view.rgb = rgb ? 1 : 0;
-  st = upload_and_launch(ctx, pb, L.bytes, view, d_cmp, ctx->scratch, d_out, stream, cap);
+  st = upload_and_launch(ctx, pb, L.bytes, view, d_cmp, ctx->scratch, d_out, stream, cap, tuning);
   if (st != GST_OK) return st;
   if (!cap) {
     cudaEventRecord(ctx->scratch_done, stream);
@@ -525,9 +552,9 @@ GstTuning ctx_tuning(gst_ctx *ctx) {
   std::lock_guard<std::mutex> lock(ctx->mu);
   return ctx->tuning;
 }
-GstTuning ctx_tuning_for(gst_ctx *ctx, uint64_t blocks) {
+GstTuning ctx_tuning_for(gst_ctx *ctx, const gst_header *hdrs, int n) {
   std::lock_guard<std::mutex> lock(ctx->mu);
-  return tuning_for_locked(ctx, blocks);
+  return launch_tuning_locked(ctx, hdrs, n);
 }
 }  // namespace host
 }  // namespace gst
@@ -571,7 +598,7 @@ struct gst_batch {
 namespace {
 
 GstTuning batch_tuning(const gst_batch *b) {
-  return b->tuned ? b->tuning : tuning_for_locked(b->ctx, uint64_t(b->layout.n_tiles) * 1024);
+  return b->tuned ? b->tuning : launch_tuning_locked(b->ctx, b->hdrs.data(), int(b->hdrs.size()));
 }
 
 bool valid_tuning(int blocks_per_sm, int stage_words, int persistent = 0) {
@@ -909,7 +936,7 @@ gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const
   std::vector<PlanLayout> lay(nc);
   for (int c = 0; c < nc; ++c) {
     const int m = cut[c + 1] - cut[c];
-    const uint32_t cap = plan_capacity(ctx, tuning_for_locked(ctx, total_blocks(hdrs + cut[c], m)));
+    const uint32_t cap = plan_capacity(ctx, launch_tuning_locked(ctx, hdrs + cut[c], m));
     lay[c] = plan_layout(hdrs + cut[c], m, cap);
     scratch = std::max(scratch, lay[c].scratch_bytes);
   }
@@ -965,7 +992,7 @@ gst_status gst_load_host_dxts(gst_ctx *ctx, const gst_header *hdrs, int n, const
     GstPlanView view = plan_view(lay[c], pbs[c]->d, ctx->status_d);
     view.image_err = nullptr;
     e = launch_decode(nullptr, ctx->scratch, nullptr, view, ctx->hs_comp, &ctx->last_launches, nullptr,
-                      tuning_for_locked(ctx, uint64_t(lay[c].n_tiles) * 1024),
+                      launch_tuning_locked(ctx, hdrs + cut[c], cut[c + 1] - cut[c]),
                       ctx->timed_names);
     if (e == cudaSuccess) e = cudaEventRecord(pbs[c]->done, ctx->hs_comp);
     pbs[c]->stream = ctx->hs_comp;
@@ -1076,7 +1103,7 @@ gst_status gst_decode_rans_groups(gst_ctx *ctx, const void *d_freqs, const void 
   view.counters = reinterpret_cast<uint32_t *>(pb->d + off_counters);
   view.n_images = 1;
   view.n_rans = n_rans;  // no sync words: always the rANS kernel alone
-  return upload_and_launch(ctx, pb, plan_bytes, view, nullptr, nullptr, nullptr, st, cap);
+  return upload_and_launch(ctx, pb, plan_bytes, view, nullptr, nullptr, nullptr, st, cap, tuning_for_locked(ctx, 0));
 }
 
 gst_status gst_batch_create(gst_ctx *ctx, const gst_header *hdrs, int n, gst_batch **out) {
@@ -1091,7 +1118,7 @@ gst_status gst_batch_create(gst_ctx *ctx, const gst_header *hdrs, int n, gst_bat
   gst_batch *b = new gst_batch();
   b->ctx = ctx;
   b->hdrs.assign(hdrs, hdrs + n);
-  b->plan_cap = plan_capacity(ctx, tuning_for_locked(ctx, total_blocks(hdrs, n)));
+  b->plan_cap = plan_capacity(ctx, launch_tuning_locked(ctx, hdrs, n));
   b->layout = plan_layout(hdrs, n, b->plan_cap);
   b->compressed_bytes = gst_batch_layout_bytes(hdrs, n);
   for (int i = 0; i < n; ++i) b->out_bytes += size_t(image_blocks(hdrs[i])) * 8;
@@ -1360,16 +1387,19 @@ gst_status gst_set_option(gst_ctx *ctx, const char *name, int value) {
   if (strcmp(name, "rans_blocks_per_sm") == 0) {
     if (!valid_tuning(value, int(ctx->tuning.stage_words))) return GST_E_ARG;
     ctx->tuning.blocks_per_sm = value;
+    ctx->tuning_explicit = true;
     return GST_OK;
   }
   if (strcmp(name, "rans_stage_words") == 0) {
     if (!valid_tuning(ctx->tuning.blocks_per_sm, value)) return GST_E_ARG;
     ctx->tuning.stage_words = uint32_t(value);
+    ctx->tuning_explicit = true;
     return GST_OK;
   }
   if (strcmp(name, "persistent") == 0) {
     if (value != 0 && value != 1) return GST_E_ARG;
     ctx->tuning.persistent = value;
+    ctx->tuning_explicit = true;
     return GST_OK;
   }
   if (strcmp(name, "persistent_wait_us") == 0) {

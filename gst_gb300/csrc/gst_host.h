@@ -104,9 +104,11 @@ int ctx_device(const gst_ctx *ctx);
 // is off.
 uint32_t plan_capacity(const gst_ctx *ctx, const GstTuning &t);
 GstTuning ctx_tuning(gst_ctx *ctx);
-// The configuration of a launch of `blocks` DXT1 blocks: its size class's
-// entry where one is set, else the context's.
-GstTuning ctx_tuning_for(gst_ctx *ctx, uint64_t blocks);
+// The configuration of a launch of these images: their size class's entry
+// where one is set, else the context's where its tuning options were set,
+// else the deepest stages whose one wave holds the launch (few images) or
+// the context's default.
+GstTuning ctx_tuning_for(gst_ctx *ctx, const gst_header *hdrs, int n);
 int size_class(uint64_t blocks);
 
 // Context state of the encoder calls (gst_encode_api.cpp), created on first use.

@@ -254,7 +254,7 @@ bool gst_server::launch(Slot &s, std::unique_lock<std::mutex> &lk) {
 
   const int n = int(s.ids.size());
   NvtxRange range("gst server launch");
-  GstTuning tuning = ctx_tuning_for(ctx, total_blocks(s.hdrs.data(), n));
+  GstTuning tuning = ctx_tuning_for(ctx, s.hdrs.data(), n);
   tuning.persistent = 0;
   const PlanLayout L = plan_layout(s.hdrs.data(), n, plan_capacity(ctx, tuning));
   gst_status st = grow(&s.scratch, nullptr, &s.scratch_cap, L.scratch_bytes);

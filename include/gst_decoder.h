@@ -182,11 +182,17 @@ gst_status gst_batch_set_tuning(gst_batch *batch, int blocks_per_sm, int stage_w
  * class 6 above 2^24.  Per-image and batched context calls, the server's
  * launches, the pipelined host calls and batches without their own tuning
  * use their class's configuration where one is set, else the context's
- * ("rans_blocks_per_sm" / "rans_stage_words" / "persistent" options).
+ * ("rans_blocks_per_sm" / "rans_stage_words" / "persistent" options) once
+ * any of those options was set.  With neither, a launch whose rANS items
+ * (runs of 4 groups) fit one wave of 8 CTAs per SM with 4352-word stages
+ * uses that configuration, else one that fits at 1528 words, else the
+ * context's default (12, 1016, two kernels): a launch of a few images needs
+ * no more CTAs per SM, and every re-stage it avoids is on its critical path.
  * gst_set_class_tuning sets a class (values as for gst_batch_set_tuning;
  * 0, 0 clears it); gst_autotune_class runs gst_batch_autotune on a
  * representative batch and sets the result for that batch's class, which it
- * returns in *size_class; gst_get_class_tuning reads a class's configuration.
+ * returns in *size_class; gst_get_class_tuning reads a class's configuration
+ * (the context's for a class without one).
  * The server keeps the two-kernel form for its launches (they run side by
  * side on its slots), with the class's CTAs per SM and staging depth. */
 int gst_size_class(uint64_t blocks);
@@ -275,7 +281,10 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
  *   "rans_blocks_per_sm"  register budget of the rANS kernel in CTAs of 128
  *                         threads per SM: 1-9 (eight, 64 registers), 10-13
  *                         (twelve, default) or 14-16 (sixteen).  The
- *                         persistent kernel always runs 8 per SM.
+ *                         persistent kernel always runs 8 per SM.  Setting
+ *                         this, "rans_stage_words" or "persistent" also
+ *                         turns off the size-dependent choice for launches
+ *                         of a few images (gst_get_class_tuning).
  *   "rans_stage_words"    16-bit renormalisation words each warp stages in
  *                         shared memory: a multiple of 8 in [520, 4352];
  *                         default 1016.  Deeper stages re-stage less often

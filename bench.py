@@ -919,20 +919,20 @@ def time_rans_section(ctx, sec, device, stream, flush, steps, warmup):
     d_o = torch.empty(sec.symbols.size, dtype=torch.uint8, device=device)
     fn = lambda: decoder.decode_rans_groups(ctx, d_f, d_b, len(sec.section) - 512, sec.n_groups, 32, d_o, stream)  # noqa: E731
     ctx.set_profiling(True)
-    best = None
-    for bps, words in RANS_CANDIDATES:
-        ctx.set_option("rans_blocks_per_sm", bps)
-        ctx.set_option("rans_stage_words", words)
-        _, k = time_steps(fn, 3, 1, stream, flush, ctx)
-        ms = statistics.mean(sum(m for _, m in step) for step in k)
-        if best is None or ms < best[2]:
-            best = (bps, words, ms)
+    per = {c: [] for c in RANS_CANDIDATES}
+    for _ in range(2):  # two rounds over the candidates, so that one slow step does not decide
+        for bps, words in RANS_CANDIDATES:
+            ctx.set_option("rans_blocks_per_sm", bps)
+            ctx.set_option("rans_stage_words", words)
+            _, k = time_steps(fn, 5, 1, stream, flush, ctx)
+            per[(bps, words)] += [sum(m for _, m in step) for step in k]
+    bps, words = min(per, key=lambda c: statistics.median(per[c]))
+    best = (bps, words)
     ctx.set_option("rans_blocks_per_sm", best[0])
     ctx.set_option("rans_stage_words", best[1])
     _, k = time_steps(fn, steps, warmup, stream, flush, ctx, clear=d_o)
     ctx.set_profiling(False)
-    ctx.set_option("rans_blocks_per_sm", 12)
-    ctx.set_option("rans_stage_words", 1016)
+    ctx.set_option("auto_tuning", 1)
     t = [sum(ms for _, ms in step) for step in k]
     ok = bool(np.array_equal(d_o.cpu().numpy(), sec.symbols)) and decoder.sync_status(ctx, stream) == decoder.GST_OK
     return t, ok, {"blocks_per_sm": best[0], "stage_words": best[1], "chosen_by": "timing each candidate"}

@@ -1407,6 +1407,12 @@ gst_status gst_set_option(gst_ctx *ctx, const char *name, int value) {
     ctx->wait_limit_ns = uint64_t(value) * 1000u;
     return GST_OK;
   }
+  if (strcmp(name, "auto_tuning") == 0) {  // back to the default configuration, chosen per launch size
+    if (value != 1) return GST_E_ARG;
+    ctx->tuning = GstTuning{};
+    ctx->tuning_explicit = false;
+    return GST_OK;
+  }
   if (strcmp(name, "balance_rans_items") == 0) {
     if (value != 0 && value != 1) return GST_E_ARG;
     ctx->balance_items = value != 0;

@@ -303,6 +303,9 @@ int gst_kernel_times(gst_ctx *ctx, float *ms, const char **names, int cap);
  *                         of an encoder group's look-back wait for the sizes
  *                         before it, microseconds (0 = 2 s, at most
  *                         2,000,000).
+ *   "auto_tuning"         1: back to the default configuration (12, 1016,
+ *                         two kernels) with the size-dependent choice for
+ *                         launches of a few images; other values GST_E_ARG.
  *   "balance_rans_items"  1 (default): where a launch's rANS groups fill its
  *                         one wave of CTAs (SMs x resident CTAs per SM of the
  *                         two-kernel form) with 3.5 groups an item or more,

@@ -411,6 +411,26 @@ def test_every_tuning_decodes_identically(gpu_ctx):
         b.close()
 
 
+def test_auto_tuning_option_restores_the_default():
+    """The context's tuning options replace the size-dependent default; the
+    "auto_tuning" option brings it back, and a one-image decode is exact
+    under either."""
+    ctx = decoder.GPUContext(0)
+    try:
+        im = workloads.encode_image(1024, 512, 731)
+        ctx.set_option("rans_blocks_per_sm", 8)
+        assert decoder.get_class_tuning(ctx, 0) == (8, 1016, 0)
+        assert np.array_equal(as_blocks(decoder.decompress_dxt(ctx, im.stream)), im.blocks)
+        ctx.set_option("auto_tuning", 1)
+        assert decoder.get_class_tuning(ctx, 0) == (12, 1016, 0)
+        assert np.array_equal(as_blocks(decoder.decompress_dxt(ctx, im.stream)), im.blocks)
+        with pytest.raises(decoder.GstError) as ei:
+            ctx.set_option("auto_tuning", 0)
+        assert ei.value.status == decoder.GST_E_ARG
+    finally:
+        ctx.close()
+
+
 def test_batch_autotune_and_tuning_validation(gpu_ctx):
     imgs = [workloads.encode_image(w, h, 720 + i) for i, (w, h) in enumerate([(2048, 2048), (1024, 512)])]
     hdrs, packed = decoder.pack_batch([im.stream for im in imgs])

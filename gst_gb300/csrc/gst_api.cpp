@@ -586,7 +586,7 @@ struct gst_batch {
   std::vector<int> hm_cut;
   std::vector<PlanLayout> hm_lay;
   std::vector<size_t> hm_plan_off;
-  uint32_t hm_cap = 0;  // the one-wave capacity the per-chunk plans were cut for
+  std::vector<GstTuning> hm_tun;  // each chunk's launch configuration (the plans are cut for it)
   std::vector<size_t> hm_scr_off;  // chunk c's scratch: b->scratch + hm_scr_off[c], disjoint per chunk
   cudaStream_t hm_stream[4] = {};  // copy in, decode (even chunks), copy out, decode (odd chunks)
   cudaGraphExec_t hm_graph = nullptr;
@@ -1246,16 +1246,22 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
       if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_status(e);
   }
-  const uint32_t hm_cap = plan_capacity(ctx, tuning);
-  if (b->hm_chunks != chunks || b->hm_cap != hm_cap) {
+  // Each chunk's configuration: the batch's own where it has one, else the
+  // chunk's size-dependent one (a chunk is a launch of a few images).
+  const std::vector<int> cut_now = chunk_cuts(hdrs, n, chunks, blocks);
+  std::vector<GstTuning> tun(cut_now.size() - 1, tuning);
+  if (!b->tuned)
+    for (size_t c = 0; c + 1 < cut_now.size(); ++c)
+      tun[c] = launch_tuning_locked(ctx, hdrs + cut_now[c], cut_now[c + 1] - cut_now[c]);
+  if (b->hm_chunks != chunks || b->hm_tun != tun) {
     // Per-chunk plans with absolute addresses in the mirrors, uploaded once
-    // per chunk count and one-wave capacity.
-    const std::vector<int> cut = chunk_cuts(hdrs, n, chunks, blocks);
+    // per chunk count and chunk configurations.
+    const std::vector<int> &cut = cut_now;
     const int nc = int(cut.size()) - 1;
     std::vector<PlanLayout> lay(nc);
     std::vector<size_t> off(nc + 1, 0);
     for (int c = 0; c < nc; ++c) {
-      lay[c] = plan_layout(hdrs + cut[c], cut[c + 1] - cut[c], hm_cap);
+      lay[c] = plan_layout(hdrs + cut[c], cut[c + 1] - cut[c], plan_capacity(ctx, tun[c]));
       off[c + 1] = align_up(off[c] + lay[c].bytes, 256);
     }
     if (b->hm_graph) cudaGraphExecDestroy(b->hm_graph);
@@ -1286,7 +1292,7 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
     b->hm_lay = std::move(lay);
     b->hm_plan_off = std::move(off);
     b->hm_chunks = chunks;
-    b->hm_cap = hm_cap;
+    b->hm_tun = tun;
   }
   if (!b->hm_graph || b->hm_graph_cmp != h_cmp || b->hm_graph_out != h_out || b->hm_graph_tuning != tuning) {
     // Capture the copies in, decodes and copies out of every chunk, enqueued
@@ -1339,7 +1345,8 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
       view.wait_limit_ns = ctx->wait_limit_ns;
       int launches = 0;
       if (e == cudaSuccess)
-        e = launch_decode(nullptr, b->scratch + b->hm_scr_off[c], nullptr, view, s, &launches, nullptr, tuning);
+        e = launch_decode(nullptr, b->scratch + b->hm_scr_off[c], nullptr, view, s, &launches, nullptr,
+                          b->hm_tun[c]);
       if (e == cudaSuccess) e = cudaEventRecord(evs[nc + c], s);
     }
     nvtxRangePop();

@@ -156,8 +156,10 @@ gst_status gst_batch_graph_launch(gst_batch *batch, const void *d_cmp, void *d_o
  * 0 = 3) with the batch's own device mirrors and per-run plans, built once per
  * chunk count, and the whole pipeline captured as one CUDA graph per (h_cmp,
  * h_out, chunks, tuning) and replayed: a call costs one graph launch of host
- * work, while every copy and decode runs each time.  The batch's device
- * launches and its host launches must not run concurrently. */
+ * work, while every copy and decode runs each time.  A batch without a tuning
+ * of its own decodes each run with the run's own size-dependent
+ * configuration (see gst_get_class_tuning).  The batch's device launches and
+ * its host launches must not run concurrently. */
 gst_status gst_batch_host_launch(gst_batch *batch, const void *h_cmp, void *h_out, int chunks, void *stream);
 
 /* Per-batch tuning of the launch (no counterpart in the reference).

@@ -513,7 +513,7 @@ def test_load_host_dxts_pipelined(gpu_ctx, chunks):
         assert np.array_equal(h_out.numpy().view(np.uint64), want)
 
 
-@pytest.mark.parametrize("chunks,persistent", [(1, 0), (3, 0), (5, 1), (6, 0)])
+@pytest.mark.parametrize("chunks,persistent", [(1, 0), (3, 0), (5, 1), (6, 0), (4, None)])
 def test_batch_host_launch_graph(gpu_ctx, chunks, persistent):
     # gst_batch_host_launch: the pipelined host-to-host decode replayed from a
     # captured graph; repeated calls (outputs cleared in between), a new
@@ -523,7 +523,8 @@ def test_batch_host_launch_graph(gpu_ctx, chunks, persistent):
     hdrs, packed = decoder.pack_batch([im.stream for im in imgs])
     want = np.concatenate([im.blocks for im in imgs])
     rb = decoder.ResidentBatch(gpu_ctx, hdrs)
-    rb.set_tuning(8, 1016, persistent)
+    if persistent is not None:  # None: untuned, each chunk its size-dependent configuration
+        rb.set_tuning(8, 1016, persistent)
     h_cmp = torch.from_numpy(packed).pin_memory()
     outs = [torch.zeros(sum(h.dxt_bytes for h in hdrs), dtype=torch.uint8).pin_memory() for _ in range(2)]
     s = torch.cuda.Stream()

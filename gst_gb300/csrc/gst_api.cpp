@@ -1176,12 +1176,16 @@ gst_status gst_batch_graph_launch(gst_batch *b, const void *d_cmp, void *d_out, 
   if (!b || !d_cmp || !d_out) return GST_E_ARG;
   gst_ctx *ctx = b->ctx;
   cudaSetDevice(ctx->device);
-  if (!capturing(static_cast<cudaStream_t>(stream))) {
+  GstTuning cur;
+  {
     std::lock_guard<std::mutex> lock(ctx->mu);
-    const cudaError_t e = ensure_plan_locked(b, batch_tuning(b));  // may drop the graph: captured again below
-    if (e != cudaSuccess) return cuda_status(e);
+    cur = batch_tuning(b);
+    if (!capturing(static_cast<cudaStream_t>(stream))) {
+      const cudaError_t e = ensure_plan_locked(b, cur);  // may drop the graph: captured again below
+      if (e != cudaSuccess) return cuda_status(e);
+    }
   }
-  if (!b->graph || b->graph_cmp != d_cmp || b->graph_out != d_out || b->graph_tuning != batch_tuning(b)) {
+  if (!b->graph || b->graph_cmp != d_cmp || b->graph_out != d_out || b->graph_tuning != cur) {
     // Capture the launch sequence once per (input, output) pair.
     cudaStream_t cs = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
@@ -1212,7 +1216,7 @@ gst_status gst_batch_graph_launch(gst_batch *b, const void *d_cmp, void *d_out, 
     if (e != cudaSuccess) return cuda_status(e);
     b->graph_cmp = d_cmp;
     b->graph_out = d_out;
-    b->graph_tuning = batch_tuning(b);
+    b->graph_tuning = cur;
   }
   return cuda_status(cudaGraphLaunch(b->graph, static_cast<cudaStream_t>(stream)));
 }
@@ -1226,7 +1230,6 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
   cudaSetDevice(ctx->device);
   cudaStream_t caller = static_cast<cudaStream_t>(stream);
   if (capturing(caller)) return GST_E_ARG;
-  const GstTuning tuning = batch_tuning(b);
   const gst_header *hdrs = b->hdrs.data();
   const size_t page = offsets_page_bytes(n);
   std::vector<uint64_t> body(n + 1), out(n + 1);
@@ -1249,10 +1252,16 @@ gst_status gst_batch_host_launch(gst_batch *b, const void *h_cmp, void *h_out, i
   // Each chunk's configuration: the batch's own where it has one, else the
   // chunk's size-dependent one (a chunk is a launch of a few images).
   const std::vector<int> cut_now = chunk_cuts(hdrs, n, chunks, blocks);
-  std::vector<GstTuning> tun(cut_now.size() - 1, tuning);
-  if (!b->tuned)
-    for (size_t c = 0; c + 1 < cut_now.size(); ++c)
-      tun[c] = launch_tuning_locked(ctx, hdrs + cut_now[c], cut_now[c + 1] - cut_now[c]);
+  GstTuning tuning;
+  std::vector<GstTuning> tun;
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    tuning = batch_tuning(b);
+    tun.assign(cut_now.size() - 1, tuning);
+    if (!b->tuned)
+      for (size_t c = 0; c + 1 < cut_now.size(); ++c)
+        tun[c] = launch_tuning_locked(ctx, hdrs + cut_now[c], cut_now[c + 1] - cut_now[c]);
+  }
   if (b->hm_chunks != chunks || b->hm_tun != tun) {
     // Per-chunk plans with absolute addresses in the mirrors, uploaded once
     // per chunk count and chunk configurations.

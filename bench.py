@@ -907,7 +907,7 @@ def cpu_baseline_reencode(imgs):
                       f"{dt:.2f} s"}
 
 
-RANS_CANDIDATES = ((16, 520), (12, 520), (12, 1016), (8, 1528), (8, 2040))
+RANS_CANDIDATES = ((16, 520), (12, 520), (12, 1016), (8, 1528), (8, 2040), (8, 2816))
 
 
 def time_rans_section(ctx, sec, device, stream, flush, steps, warmup):

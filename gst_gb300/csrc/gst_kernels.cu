@@ -706,22 +706,6 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
     }
   }
 
-  // 2. Palette indices of the rows this thread assembles (rows warp + kWarps i,
-  //    column lane): group prefix + prefix through the block's 32-block chunk
-  //    - the sum of the deltas after the block in its chunk.  Loads first, so
-  //    that they overlap the wavelet.
-  const int32_t *chunk_pref = reinterpret_cast<const int32_t *>(scratch + im.chunk_off);
-  const int32_t *gpref = reinterpret_cast<const int32_t *>(scratch + im.gsum_off) + im.sec_groups[3];
-  const int16_t *partial = reinterpret_cast<const int16_t *>(sym + im.sec_out[3]);
-  uint32_t d[kRows], base[kRows];
-#pragma unroll
-  for (int i = 0; i < kRows; ++i) {
-    const uint32_t p0 = (ty * 32 + warp + kWarps * i) * im.bx + tx * 32;  // first block of the row segment
-    d[i] = static_cast<uint32_t>(static_cast<int32_t>(ld_sym<COH>(partial + p0 + lane)));
-    base[i] = static_cast<uint32_t>(ld_sym<COH>(gpref + (p0 >> 13))) +
-              static_cast<uint32_t>(ld_sym<COH>(chunk_pref + (p0 >> 5)));
-  }
-
   // 3. (fewer than 192 threads) All coefficients to int32 shared memory
   //    (pitch kPlanePitch), byte - 128.
   if constexpr (!kRegRows) {
@@ -736,18 +720,6 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
         store_row<16>(dst, v);
       }
     }
-  }
-
-  // 4. The palette gathers.
-  const uint32_t *pal = reinterpret_cast<const uint32_t *>(sym + im.sec_out[2]);
-  uint32_t word[kRows];
-  bool bad = false;
-#pragma unroll
-  for (int i = 0; i < kRows; ++i) {
-    const uint32_t idx = base[i] - d[i];
-    word[i] = 0;
-    if (idx < im.palette_words) word[i] = ld_sym<COH>(pal + idx);
-    else bad = true;
   }
 
   // 5. Five levels of the inverse 5/3 wavelet.
@@ -797,6 +769,34 @@ __device__ __forceinline__ void tile_work(const uint8_t *__restrict__ scratch, u
 #pragma unroll
     for (int c = threadIdx.x; c < 6 * 32; c += NT) inv53_line<32>(pl + (c >> 5) * kPlaneWords + (c & 31), kPlanePitch);
     __syncthreads();
+  }
+
+  // 2. Palette indices of the rows this thread assembles (rows warp + kWarps i,
+  //    column lane): group prefix + prefix through the block's 32-block chunk
+  //    - the sum of the deltas after the block in its chunk.  Loaded after the
+  //    wavelet, so that nothing of them is live through it.
+  const int32_t *chunk_pref = reinterpret_cast<const int32_t *>(scratch + im.chunk_off);
+  const int32_t *gpref = reinterpret_cast<const int32_t *>(scratch + im.gsum_off) + im.sec_groups[3];
+  const int16_t *partial = reinterpret_cast<const int16_t *>(sym + im.sec_out[3]);
+  uint32_t d[kRows], base[kRows];
+#pragma unroll
+  for (int i = 0; i < kRows; ++i) {
+    const uint32_t p0 = (ty * 32 + warp + kWarps * i) * im.bx + tx * 32;  // first block of the row segment
+    d[i] = static_cast<uint32_t>(static_cast<int32_t>(ld_sym<COH>(partial + p0 + lane)));
+    base[i] = static_cast<uint32_t>(ld_sym<COH>(gpref + (p0 >> 13))) +
+              static_cast<uint32_t>(ld_sym<COH>(chunk_pref + (p0 >> 5)));
+  }
+
+  // 4. The palette gathers.
+  const uint32_t *pal = reinterpret_cast<const uint32_t *>(sym + im.sec_out[2]);
+  uint32_t word[kRows];
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < kRows; ++i) {
+    const uint32_t idx = base[i] - d[i];
+    word[i] = 0;
+    if (idx < im.palette_words) word[i] = ld_sym<COH>(pal + idx);
+    else bad = true;
   }
 
   // 6. YCoCg667 -> RGB565 endpoints and whole 8-byte DXT1 blocks (or the

@@ -143,7 +143,10 @@ struct gst_server {
   std::thread thread;
 
   // statistics since the last reset
-  std::vector<double> lat_us;
+  // Completed requests' latencies: chunked storage, so that appending under
+  // the lock never reallocates and copies the whole record (at 20k req/s a
+  // vector's doubling copied megabytes while submissions waited).
+  std::deque<double> lat_us;
   uint64_t submitted = 0, completed = 0, rejected = 0, cancelled = 0, launches = 0, launched_images = 0, pixels = 0;
   uint64_t t_stats = 0;
   size_t dev_peak = 0;
@@ -623,21 +626,31 @@ gst_status gst_server_cancel(gst_server *srv, uint64_t id) {
 
 gst_status gst_server_read_stats(gst_server *srv, gst_server_stats *st, int reset) {
   if (!srv || !st) return GST_E_ARG;
-  std::lock_guard<std::mutex> lk(srv->mu);
-  memset(st, 0, sizeof(*st));
-  st->submitted = srv->submitted;
-  st->completed = srv->completed;
-  st->rejected = srv->rejected;
-  st->cancelled = srv->cancelled;
-  st->launches = srv->launches;
-  st->launched_images = srv->launched_images;
-  st->pixels = srv->pixels;
-  st->queued = srv->queued.size();
-  st->device_bytes_in_use = srv->dev_arena.used();
-  st->device_bytes_peak = srv->dev_peak;
-  const uint64_t t = srv->now();
-  st->seconds = double(t - srv->t_stats) / 1e9;
-  std::vector<double> v = srv->lat_us;
+  std::vector<double> v;  // the latencies, sorted outside the lock
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    memset(st, 0, sizeof(*st));
+    st->submitted = srv->submitted;
+    st->completed = srv->completed;
+    st->rejected = srv->rejected;
+    st->cancelled = srv->cancelled;
+    st->launches = srv->launches;
+    st->launched_images = srv->launched_images;
+    st->pixels = srv->pixels;
+    st->queued = srv->queued.size();
+    st->device_bytes_in_use = srv->dev_arena.used();
+    st->device_bytes_peak = srv->dev_peak;
+    const uint64_t t = srv->now();
+    st->seconds = double(t - srv->t_stats) / 1e9;
+    v.assign(srv->lat_us.begin(), srv->lat_us.end());
+    if (reset) {
+      srv->lat_us.clear();
+      srv->submitted = srv->completed = srv->rejected = srv->cancelled = srv->launches = srv->launched_images =
+          srv->pixels = 0;
+      srv->dev_peak = srv->dev_arena.used();
+      srv->t_stats = t;
+    }
+  }
   if (!v.empty()) {
     std::sort(v.begin(), v.end());
     auto pct = [&](double p) {
@@ -650,13 +663,6 @@ gst_status gst_server_read_stats(gst_server *srv, gst_server_stats *st, int rese
     st->latency_p50_us = pct(50);
     st->latency_p99_us = pct(99);
     st->latency_max_us = v.back();
-  }
-  if (reset) {
-    srv->lat_us.clear();
-    srv->submitted = srv->completed = srv->rejected = srv->cancelled = srv->launches = srv->launched_images =
-        srv->pixels = 0;
-    srv->dev_peak = srv->dev_arena.used();
-    srv->t_stats = t;
   }
   return GST_OK;
 }
